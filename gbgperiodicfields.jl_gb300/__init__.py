@@ -1,0 +1,28 @@
+"""GB300-native (sm_103a) particle gather/scatter for GBGPeriodicFields.jl's spline
+transfer path: interpolate!/anterpolate! of periodic scalar, vector and tensor fields at
+points, the traversal order, and the resident precision/batched/served forms.
+
+The compute runs in hand-written CUDA kernels in libgbg_gb300.so, reached through the C
+ABI in include/gbg_transfer.h.  This package is the host-side mirror of the reference's
+API over that ABI (the Julia facade binds the same ABI with ccall)."""
+from . import _lib
+from ._lib import ArgumentError, DimensionMismatch, GBGError, InexactError
+from .api import (AbstractFieldPhysical, AbstractPointValues, Grid3D, LagrangeSpline, LalescuSpline,
+                  PointSet, PointTraversalOrder, PointTraversalOrderScratch, ScalarFieldPhysical,
+                  ScalarPointValues, TensorFieldPhysical, TensorPointValues, VectorFieldPhysical,
+                  VectorPointValues, anterpolate, anterpolate_, colmajor, empty_colmajor, field_data,
+                  field_grid, interpolate, interpolate_, npoints, point_positions,
+                  point_traversal_order, point_traversal_order_, point_values, sample_field,
+                  zeros_colmajor)
+
+
+def __getattr__(name):
+    if name == "CatmullRom":
+        from .api import _catmull_rom
+        return _catmull_rom()
+    raise AttributeError(name)
+
+
+def build(verbose: bool = False):
+    from . import builder
+    return builder.build(verbose)

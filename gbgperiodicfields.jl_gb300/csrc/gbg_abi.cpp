@@ -1,0 +1,68 @@
+// C-ABI plumbing: status text, per-thread error messages, stream-ordered scratch.
+#include <string>
+
+#include "gbg_common.cuh"
+
+namespace gbg {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+gbg_status set_error(gbg_status status, const std::string &message) {
+  g_last_error = message;
+  return status;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+gbg_status Scratch::acquire(void *user, size_t user_bytes, size_t need, cudaStream_t s) {
+  stream = s;
+  if (need == 0) return GBG_OK;
+  if (user) {
+    if (user_bytes < need)
+      return set_error(GBG_ENOMEM, "workspace too small: need " + std::to_string(need) + " bytes, got " +
+                                       std::to_string(user_bytes));
+    ptr = user;
+    return GBG_OK;
+  }
+  cudaError_t e = cudaMallocAsync(&ptr, need, s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    ptr = nullptr;
+    return set_error(GBG_ENOMEM, "cudaMallocAsync of " + std::to_string(need) + " bytes failed: " +
+                                     cudaGetErrorString(e));
+  }
+  owned = true;
+  return GBG_OK;
+}
+
+Scratch::~Scratch() {
+  if (owned && ptr) cudaFreeAsync(ptr, stream);
+}
+
+}  // namespace gbg
+
+extern "C" {
+
+int32_t gbg_abi_version(void) { return GBG_ABI_VERSION; }
+
+const char *gbg_status_string(gbg_status status) {
+  switch (status) {
+    case GBG_OK: return "ok";
+    case GBG_EARG: return "invalid argument (ArgumentError)";
+    case GBG_EDIM: return "dimension mismatch (DimensionMismatch)";
+    case GBG_ENOMEM: return "out of device memory or workspace too small";
+    case GBG_ECUDA: return "CUDA runtime error";
+    case GBG_ENONFINITE: return "non-finite or out-of-range position";
+    case GBG_ETIMEOUT: return "timed out";
+    case GBG_EUNSUPPORTED: return "unsupported size";
+    case GBG_EBUSY: return "busy: admission refused";
+    case GBG_ETRAVERSAL: return "traversal order is not a permutation";
+    default: return "unknown status";
+  }
+}
+
+const char *gbg_last_error(void) { return gbg::g_last_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,163 @@
+// Internal helpers shared by the sm_103a kernels and the C-ABI layer.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstddef>
+#include <string>
+
+#include "gbg_transfer.h"
+
+namespace gbg {
+
+// ------------------------------------------------------------------ errors
+
+// Records a message for gbg_last_error() (thread-local) and returns the status.
+gbg_status set_error(gbg_status status, const std::string &message);
+void clear_error();
+
+#define GBG_CUDA_TRY(expr)                                                                  \
+  do {                                                                                      \
+    cudaError_t _e = (expr);                                                                \
+    if (_e != cudaSuccess)                                                                  \
+      return ::gbg::set_error(GBG_ECUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+#define GBG_TRY(expr)                 \
+  do {                                \
+    gbg_status _s = (expr);           \
+    if (_s != GBG_OK) return _s;      \
+  } while (0)
+
+// ------------------------------------------------------------ arithmetic
+
+// Non-contractible multiply/add, so that the weight polynomials are evaluated with the
+// same roundings as the reference's Horner loop (Julia never fuses a*b+c).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double fma_rn(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Julia's integer mod for a positive divisor: the result lies in [0, n).
+__host__ __device__ __forceinline__ int64_t imod(int64_t a, int64_t n) {
+  int64_t r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+// Interpolation.jl:456-460 -- _locate: ci = (x - o) / dx (IEEE division in T),
+// base = floor(ci), t = ci - base.  Returns false for a non-finite or huge ci, for which
+// floor(Int, ci) throws in the reference.
+template <typename T>
+__device__ __forceinline__ bool locate(T x, T o, T d, int64_t &base, T &t) {
+  const T ci = (x - o) / d;
+  const T fl = floor(ci);
+  const bool ok = isfinite(ci) && fabs(fl) < T(9.0e18);
+  base = ok ? (int64_t)fl : 0;
+  t = ci - fl;
+  return ok;
+}
+
+// A scheme's coefficients converted to T (Interpolation.jl:1360, _coefficients_as),
+// sized for NMAX nodes and passed by value as a kernel parameter.
+template <typename T, int NMAX>
+struct SchemeT {
+  T c[NMAX * GBG_MAX_POWERS];  // [q + n2*p]
+  int32_t n2;
+  int32_t m2;
+};
+
+template <typename T, int NMAX>
+inline SchemeT<T, NMAX> make_scheme(const gbg_scheme &s) {
+  SchemeT<T, NMAX> r;
+  r.n2 = s.stencil_width;
+  r.m2 = s.num_powers;
+  for (int i = 0; i < NMAX * GBG_MAX_POWERS; ++i) r.c[i] = T(0);
+  for (int q = 0; q < s.stencil_width; ++q)
+    for (int p = 0; p < s.num_powers; ++p)
+      r.c[q + s.stencil_width * p] = T(s.coefficients[q + s.stencil_width * p]);
+  return r;
+}
+
+// Interpolation.jl:440-446 -- Horner from the highest power, w = w*t + c[:, p], with the
+// reference's roundings, for a compile-time width N2.  The loop is unrolled over every
+// possible power so that the coefficients stay in the parameter bank; powers >= m2 are
+// skipped (w starts at 0, and 0*t + c[:, m2-1] = c[:, m2-1] exactly for finite t).
+template <typename T, int N2>
+__device__ __forceinline__ void axis_weights(const SchemeT<T, N2> &s, T t, T (&w)[N2]) {
+#pragma unroll
+  for (int q = 0; q < N2; ++q) w[q] = T(0);
+#pragma unroll
+  for (int p = GBG_MAX_POWERS - 1; p >= 0; --p) {
+    if (p < s.m2) {
+#pragma unroll
+      for (int q = 0; q < N2; ++q) w[q] = add_rn(mul_rn(w[q], t), s.c[q + N2 * p]);
+    }
+  }
+}
+
+// The same for a run-time width, from coefficients staged in shared memory.
+template <typename T>
+__device__ __forceinline__ void axis_weights_dyn(const T *c, int n2, int m2, T t, T *w) {
+#pragma unroll 1
+  for (int q = 0; q < n2; ++q) w[q] = c[q + n2 * (m2 - 1)];
+#pragma unroll 1
+  for (int p = m2 - 2; p >= 0; --p) {
+#pragma unroll 1
+    for (int q = 0; q < n2; ++q) w[q] = add_rn(mul_rn(w[q], t), c[q + n2 * p]);
+  }
+}
+
+// Copies a scheme's coefficients into shared memory (run-time-width kernels).
+template <typename T, int NMAX>
+__device__ __forceinline__ void stage_coeffs(const SchemeT<T, NMAX> &s, T *c) {
+  for (int i = threadIdx.x; i < s.n2 * s.m2; i += blockDim.x) c[i] = s.c[i];
+  __syncthreads();
+}
+
+// ----------------------------------------------------------- workspace
+
+// Carves aligned sub-buffers out of one workspace; with base == nullptr it only sizes.
+struct Arena {
+  char *base = nullptr;
+  size_t used = 0;
+  template <typename U>
+  U *take(size_t count) {
+    used = (used + 255) & ~size_t(255);
+    U *p = base ? reinterpret_cast<U *>(base + used) : nullptr;
+    used += count * sizeof(U);
+    return p;
+  }
+};
+
+// Stream-ordered scratch: the caller's workspace when given, else cudaMallocAsync.
+struct Scratch {
+  void *ptr = nullptr;
+  bool owned = false;
+  cudaStream_t stream = nullptr;
+  gbg_status acquire(void *user, size_t user_bytes, size_t need, cudaStream_t s);
+  ~Scratch();
+};
+
+// ---------------------------------------------------------------- sort
+
+// Exclusive prefix sum of n uint32 values; tmp must hold scan_temp_elems(n) uint32.
+size_t scan_temp_elems(int64_t n);
+gbg_status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
+                              cudaStream_t stream);
+
+// Stable LSD radix sort of (key, value) pairs over the low key_bits bits of the keys.
+// vals_in == nullptr means the identity 0..n-1.  Results land in keys_out / vals_out;
+// keys_in is not modified.  Scratch sizes come from radix_sort_temp_bytes.
+size_t radix_sort_temp_bytes(int64_t n);
+gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
+                            uint32_t *vals_out, int64_t n, int key_bits, void *temp,
+                            cudaStream_t stream);
+
+// Grid-stride launch shape: a multiple of the SM count.
+int launch_blocks(int64_t work, int threads, int per_sm = 8);
+
+}  // namespace gbg

@@ -1,0 +1,703 @@
+// Drop-in transfers on the reference's own array layouts (sm_103a).
+//
+//   gbg_interpolate             interpolate!            Interpolation.jl:1181-1198, 1007-1052
+//   gbg_anterpolate             anterpolate!            Interpolation.jl:1299-1323, 1063-1106
+//   gbg_point_traversal_order   point_traversal_order   Interpolation.jl:816-833, 636-684
+//   gbg_validate_traversal      PointTraversalOrder     Interpolation.jl:560-589
+//
+// The gather is one thread per work item, as in the reference, with the stencil weight
+// of each node formed once and applied to every component of the chunk.  The scatter is
+// not the reference's atomic push: points are cell-sorted with a stable device radix sort
+// and every grid node then pulls, in a fixed order, the contributions of the points in
+// the cells that reach it.  No float atomics are used, so the scatter is bitwise
+// reproducible and independent of any traversal order.
+#include <string>
+
+#include "gbg_common.cuh"
+
+namespace gbg {
+namespace {
+
+constexpr int kThreads = 256;
+
+template <typename T>
+struct GridT {
+  int64_t nx, ny, nz, npf;
+  T ox, oy, oz;  // T.(grid.origin)
+  T dx, dy, dz;  // T.(grid.grid_spacing)
+};
+
+template <typename T>
+GridT<T> make_grid(const gbg_grid &g) {
+  GridT<T> r;
+  r.nx = g.n[0];
+  r.ny = g.n[1];
+  r.nz = g.n[2];
+  r.npf = g.n[0] * g.n[1] * g.n[2];
+  r.ox = T(g.origin[0]);
+  r.oy = T(g.origin[1]);
+  r.oz = T(g.origin[2]);
+  r.dx = T(g.spacing[0]);
+  r.dy = T(g.spacing[1]);
+  r.dz = T(g.spacing[2]);
+  return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T quiet_nan();
+template <>
+__device__ __forceinline__ double quiet_nan<double>() { return __longlong_as_double(0x7ff8000000000000LL); }
+template <>
+__device__ __forceinline__ float quiet_nan<float>() { return __int_as_float(0x7fc00000); }
+
+// The wrapped node offsets visited along one axis: the reference's wrapped start
+// mod(base - n, N) followed by its step rule (Interpolation.jl:1000, 1025-1027).
+template <int N2>
+__device__ __forceinline__ void walk_offsets(int64_t base, int64_t extent, int64_t stride,
+                                             int64_t (&off)[N2]) {
+  int64_t node = imod(base - (N2 - 2) / 2, extent);
+#pragma unroll
+  for (int i = 0; i < N2; ++i) {
+    off[i] = node * stride;
+    node = (node + 1 == extent) ? 0 : node + 1;
+  }
+}
+
+__device__ __forceinline__ int64_t step_up(int64_t node, int64_t extent) {
+  return (node + 1 == extent) ? 0 : node + 1;
+}
+__device__ __forceinline__ int64_t step_down(int64_t node, int64_t extent) {
+  return node == 0 ? extent - 1 : node - 1;
+}
+
+// Locates a point on the three axes; false if any coordinate is non-finite.
+template <typename T>
+__device__ __forceinline__ bool locate3(const GridT<T> &g, const T *__restrict__ pos, int64_t p,
+                                        int64_t m, int64_t (&b)[3], T (&t)[3]) {
+  bool ok = locate(__ldg(pos + p), g.ox, g.dx, b[0], t[0]);
+  ok &= locate(__ldg(pos + p + m), g.oy, g.dy, b[1], t[1]);
+  ok &= locate(__ldg(pos + p + 2 * m), g.oz, g.dz, b[2], t[2]);
+  return ok;
+}
+
+// _visit (Interpolation.jl:618-619), bounds-checked instead of trusted.
+__device__ __forceinline__ bool visit(const int32_t *__restrict__ trav, int64_t w, int64_t m,
+                                      int64_t &p, int32_t *status) {
+  p = w;
+  if (!trav) return true;
+  const int64_t v = (int64_t)__ldg(trav + w) - 1;
+  if (v < 0 || v >= m) {
+    if (status) atomicOr(status, GBG_DEV_TRAVERSAL);
+    return false;
+  }
+  p = v;
+  return true;
+}
+
+// ---------------------------------------------------------------- gather
+
+// Compile-time width N2: the (j, i) stencil plane is unrolled, z advances by the
+// reference's running walk.
+template <typename T, int N2, int CC>
+__global__ void __launch_bounds__(kThreads)
+    k_gather_plain(GridT<T> g, SchemeT<T, N2> s, int ncomp, const T *__restrict__ field,
+                   const T *__restrict__ pos, int64_t m, const int32_t *__restrict__ trav,
+                   T *__restrict__ out, int32_t *status) {
+  const int64_t nxny = g.nx * g.ny;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < m;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p;
+    if (!visit(trav, w, m, p, status)) continue;
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    T w1[N2], w2[N2], w3[N2];
+    axis_weights<T, N2>(s, t[0], w1);
+    axis_weights<T, N2>(s, t[1], w2);
+    axis_weights<T, N2>(s, t[2], w3);
+    int64_t ix[N2], iy[N2];
+    walk_offsets<N2>(b[0], g.nx, 1, ix);
+    walk_offsets<N2>(b[1], g.ny, g.nx, iy);
+    const int64_t z0 = imod(b[2] - (N2 - 2) / 2, g.nz);
+    for (int c0 = 0; c0 < ncomp; c0 += CC) {
+      T acc[CC];
+#pragma unroll
+      for (int c = 0; c < CC; ++c) acc[c] = T(0);
+      const T *fc = field + g.npf * c0;
+      int64_t node_z = z0;
+#pragma unroll 1
+      for (int k = 0; k < N2; ++k) {
+        T w3k = w3[0];
+#pragma unroll
+        for (int q = 1; q < N2; ++q)
+          if (q == k) w3k = w3[q];
+        const T *plane = fc + node_z * nxny;
+#pragma unroll
+        for (int j = 0; j < N2; ++j) {
+          const T wyz = mul_rn(w2[j], w3k);
+          const T *row = plane + iy[j];
+#pragma unroll
+          for (int i = 0; i < N2; ++i) {
+            const T wv = mul_rn(wyz, w1[i]);
+            const T *f = row + ix[i];
+#pragma unroll
+            for (int c = 0; c < CC; ++c) acc[c] = fma_rn(wv, __ldg(f + g.npf * c), acc[c]);
+          }
+        }
+        node_z = step_up(node_z, g.nz);
+      }
+#pragma unroll
+      for (int c = 0; c < CC; ++c) out[p + m * (c0 + c)] = ok ? acc[c] : quiet_nan<T>();
+    }
+  }
+}
+
+// Run-time width (stencils of 10..16 nodes): nothing unrolled.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_gather_plain_dyn(GridT<T> g, SchemeT<T, GBG_MAX_NODES> s, int ncomp,
+                       const T *__restrict__ field, const T *__restrict__ pos, int64_t m,
+                       const int32_t *__restrict__ trav, T *__restrict__ out, int32_t *status) {
+  __shared__ T cs[GBG_MAX_NODES * GBG_MAX_POWERS];
+  stage_coeffs(s, cs);
+  const int n2 = s.n2, nb = (n2 - 2) / 2;
+  for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < m;
+       w += (int64_t)gridDim.x * blockDim.x) {
+    int64_t p;
+    if (!visit(trav, w, m, p, status)) continue;
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    T w1[GBG_MAX_NODES], w2[GBG_MAX_NODES], w3[GBG_MAX_NODES];
+    axis_weights_dyn(cs, n2, s.m2, t[0], w1);
+    axis_weights_dyn(cs, n2, s.m2, t[1], w2);
+    axis_weights_dyn(cs, n2, s.m2, t[2], w3);
+    const int64_t x0 = imod(b[0] - nb, g.nx), y0 = imod(b[1] - nb, g.ny), z0 = imod(b[2] - nb, g.nz);
+#pragma unroll 1
+    for (int c = 0; c < ncomp; ++c) {
+      T acc = T(0);
+      int64_t node_z = z0;
+#pragma unroll 1
+      for (int k = 0; k < n2; ++k) {
+        int64_t node_y = y0;
+#pragma unroll 1
+        for (int j = 0; j < n2; ++j) {
+          const T wyz = mul_rn(w2[j], w3[k]);
+          const T *row = field + g.npf * c + g.nx * node_y + g.nx * g.ny * node_z;
+          int64_t node_x = x0;
+#pragma unroll 1
+          for (int i = 0; i < n2; ++i) {
+            acc = fma_rn(mul_rn(wyz, w1[i]), __ldg(row + node_x), acc);
+            node_x = step_up(node_x, g.nx);
+          }
+          node_y = step_up(node_y, g.ny);
+        }
+        node_z = step_up(node_z, g.nz);
+      }
+      out[p + m * c] = ok ? acc : quiet_nan<T>();
+    }
+  }
+}
+
+// --------------------------------------------------------------- scatter
+
+// The cell (of the base node) each point falls in, and the per-cell point count.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_cell_keys(GridT<T> g, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
+                uint32_t *__restrict__ counts, int32_t *status) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    const uint32_t key =
+        (uint32_t)(imod(b[0], g.nx) + g.nx * (imod(b[1], g.ny) + g.ny * imod(b[2], g.nz)));
+    keys[p] = key;
+    atomicAdd(counts + key, 1u);
+  }
+}
+
+// Per sorted slot: the point's three weight vectors and its alpha-scaled quantities
+// (quantity = T(alpha) * q, Interpolation.jl:1085), laid out slot-major for the pull.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_scatter_prep(GridT<T> g, SchemeT<T, GBG_MAX_NODES> s, int ncomp, const T *__restrict__ pos,
+                   const T *__restrict__ q, int64_t m, const uint32_t *__restrict__ perm, T alpha,
+                   T *__restrict__ rec, T *__restrict__ qs) {
+  __shared__ T cs[GBG_MAX_NODES * GBG_MAX_POWERS];
+  stage_coeffs(s, cs);
+  const int n2 = s.n2;
+  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
+       sl += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = perm[sl];
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    T *r = rec + sl * 3 * n2;
+#pragma unroll 1
+    for (int a = 0; a < 3; ++a) {
+      T w[GBG_MAX_NODES];
+      axis_weights_dyn(cs, n2, s.m2, t[a], w);
+#pragma unroll 1
+      for (int i = 0; i < n2; ++i) r[a * n2 + i] = ok ? w[i] : quiet_nan<T>();
+    }
+#pragma unroll 1
+    for (int c = 0; c < ncomp; ++c) qs[sl * ncomp + c] = mul_rn(alpha, q[p + m * c]);
+  }
+}
+
+// One thread per grid node: sum, in a fixed order, the contributions of the points in
+// every cell whose stencil reaches this node, then write alpha*W^T q + beta*field.  Weight
+// index i reaches node x from the cell (x + n - i) mod N; for a stencil wider than the
+// grid a cell is reached through several weight indices and each contributes, exactly as
+// the reference's wrapped walk deposits it several times.
+template <typename T, int CC>
+__global__ void __launch_bounds__(kThreads)
+    k_scatter_pull(GridT<T> g, int n2, int ncomp, const uint32_t *__restrict__ cell_start,
+                   const T *__restrict__ rec, const T *__restrict__ qs, T *__restrict__ field,
+                   T beta, int beta_zero) {
+  const int nb = (n2 - 2) / 2;
+  const int64_t nxny = g.nx * g.ny;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.npf;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = n % g.nx;
+    const int64_t yz = n / g.nx;
+    const int64_t y = yz % g.ny;
+    const int64_t z = yz / g.ny;
+    const int64_t cx0 = imod(x + nb, g.nx), cy0 = imod(y + nb, g.ny), cz0 = imod(z + nb, g.nz);
+    for (int c0 = 0; c0 < ncomp; c0 += CC) {
+      T acc[CC];
+#pragma unroll
+      for (int c = 0; c < CC; ++c) acc[c] = T(0);
+      int64_t cz = cz0;
+#pragma unroll 1
+      for (int k = 0; k < n2; ++k) {
+        int64_t cy = cy0;
+#pragma unroll 1
+        for (int j = 0; j < n2; ++j) {
+          const int64_t rowoff = g.nx * cy + nxny * cz;
+          int64_t cx = cx0;
+#pragma unroll 1
+          for (int i = 0; i < n2; ++i) {
+            const int64_t cell = cx + rowoff;
+            const uint32_t s0 = __ldg(cell_start + cell), s1 = __ldg(cell_start + cell + 1);
+#pragma unroll 1
+            for (uint32_t sl = s0; sl < s1; ++sl) {
+              const T *r = rec + (int64_t)sl * 3 * n2;
+              const T wv = mul_rn(mul_rn(__ldg(r + n2 + j), __ldg(r + 2 * n2 + k)), __ldg(r + i));
+              const T *qv = qs + (int64_t)sl * ncomp + c0;
+#pragma unroll
+              for (int c = 0; c < CC; ++c) acc[c] = fma_rn(wv, __ldg(qv + c), acc[c]);
+            }
+            cx = step_down(cx, g.nx);
+          }
+          cy = step_down(cy, g.ny);
+        }
+        cz = step_down(cz, g.nz);
+      }
+#pragma unroll
+      for (int c = 0; c < CC; ++c) {
+        T *f = field + n + g.npf * (c0 + c);
+        *f = beta_zero ? acc[c] : add_rn(mul_rn(beta, *f), acc[c]);
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------- traversal order
+
+// Interpolation.jl:636-642: the comparisons happen in floating point, before any
+// conversion, so non-finite and far-away coordinates saturate into a real tile.
+template <typename T>
+__device__ __forceinline__ int64_t tile_index(T c, T o, T inv, int64_t tiles) {
+  const T u = (c - o) * inv;
+  if (isnan(u)) return 0;
+  if (u <= T(0)) return 0;
+  if (u >= T(tiles)) return tiles - 1;
+  return (int64_t)u;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_tile_keys(const T *__restrict__ pos, int64_t m, T o0, T o1, T o2, T i0, T i1, T i2,
+                int64_t t0, int64_t t1, int64_t t2, uint32_t *__restrict__ keys) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = tile_index(pos[p], o0, i0, t0);
+    const int64_t b = tile_index(pos[p + m], o1, i1, t1);
+    const int64_t c = tile_index(pos[p + 2 * m], o2, i2, t2);
+    keys[p] = (uint32_t)(a + t0 * (b + t1 * c));  // the reference's key less its 2 offset
+  }
+}
+
+__global__ void k_to_one_based(const uint32_t *__restrict__ perm, int32_t *__restrict__ order,
+                               int64_t m) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x)
+    order[i] = (int32_t)perm[i] + 1;
+}
+
+__global__ void k_validate(const int32_t *__restrict__ order, int64_t m, uint32_t *seen,
+                           unsigned long long *stats) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const long long v = order[i];
+    atomicMin(reinterpret_cast<long long *>(stats), v);
+    atomicMax(reinterpret_cast<long long *>(stats + 1), v);
+    if (v >= 1 && v <= m && atomicExch(seen + (v - 1), 1u) == 0u) atomicAdd(stats + 2, 1ull);
+  }
+}
+
+__global__ void k_validate_init(unsigned long long *stats) {
+  reinterpret_cast<long long *>(stats)[0] = 0x7fffffffffffffffLL;
+  reinterpret_cast<long long *>(stats)[1] = (-0x7fffffffffffffffLL - 1);
+  stats[2] = 0ull;
+}
+
+__global__ void k_fill_or_scale(void *data, int64_t count, int is_f64, double beta) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    if (is_f64) {
+      double *d = static_cast<double *>(data);
+      d[i] = beta == 0.0 ? 0.0 : __dmul_rn(d[i], beta);
+    } else {
+      float *f = static_cast<float *>(data);
+      f[i] = beta == 0.0 ? 0.0f : __fmul_rn(f[i], (float)beta);
+    }
+  }
+}
+
+// ------------------------------------------------------------- dispatch
+
+int chunk_for(int ncomp) { return ncomp % 9 == 0 ? 9 : (ncomp % 3 == 0 ? 3 : 1); }
+
+template <typename T, int N2>
+gbg_status launch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncomp, const void *field,
+                         const void *pos, int64_t m, const int32_t *trav, void *out,
+                         int32_t *status, cudaStream_t st) {
+  const GridT<T> g = make_grid<T>(grid);
+  const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
+  const int blocks = launch_blocks(m, kThreads);
+  const T *f = static_cast<const T *>(field);
+  const T *x = static_cast<const T *>(pos);
+  T *o = static_cast<T *>(out);
+  switch (chunk_for(ncomp)) {
+    case 9: k_gather_plain<T, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 3: k_gather_plain<T, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    default: k_gather_plain<T, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+  }
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
+template <typename T>
+gbg_status dispatch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncomp, const void *field,
+                           const void *pos, int64_t m, const int32_t *trav, void *out,
+                           int32_t *status, cudaStream_t st) {
+  switch (sch.stencil_width) {
+    case 2: return launch_gather<T, 2>(grid, sch, ncomp, field, pos, m, trav, out, status, st);
+    case 4: return launch_gather<T, 4>(grid, sch, ncomp, field, pos, m, trav, out, status, st);
+    case 6: return launch_gather<T, 6>(grid, sch, ncomp, field, pos, m, trav, out, status, st);
+    case 8: return launch_gather<T, 8>(grid, sch, ncomp, field, pos, m, trav, out, status, st);
+    default: {
+      const GridT<T> g = make_grid<T>(grid);
+      const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
+      k_gather_plain_dyn<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
+          g, s, ncomp, static_cast<const T *>(field), static_cast<const T *>(pos), m, trav,
+          static_cast<T *>(out), status);
+      GBG_CUDA_TRY(cudaGetLastError());
+      return GBG_OK;
+    }
+  }
+}
+
+struct ScatterLayout {
+  uint32_t *keys, *counts, *skeys, *perm;
+  void *sort_tmp;
+  uint32_t *scan_tmp;
+  void *rec, *qs;
+};
+
+ScatterLayout scatter_layout(Arena &a, int64_t m, int64_t ncells, int ncomp, int n2, size_t esize) {
+  ScatterLayout L;
+  L.keys = a.take<uint32_t>((size_t)m);
+  L.counts = a.take<uint32_t>((size_t)ncells + 1);
+  L.skeys = a.take<uint32_t>((size_t)m);
+  L.perm = a.take<uint32_t>((size_t)m);
+  L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
+  L.scan_tmp = a.take<uint32_t>(scan_temp_elems(ncells + 1));
+  L.rec = a.take<char>((size_t)m * 3 * n2 * esize);
+  L.qs = a.take<char>((size_t)m * ncomp * esize);
+  return L;
+}
+
+int bits_for(uint64_t max_value) {
+  int b = 0;
+  while (b < 32 && (max_value >> b) != 0) ++b;
+  return b;
+}
+
+template <typename T>
+gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int ncomp, void *field,
+                            const void *pos, int64_t m, const void *q, double alpha, double beta,
+                            const ScatterLayout &L, int32_t *status, cudaStream_t st) {
+  const GridT<T> g = make_grid<T>(grid);
+  const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
+  const int64_t ncells = g.npf;
+  const T *x = static_cast<const T *>(pos);
+  GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(ncells + 1), st));
+  k_cell_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, x, m, L.keys, L.counts, status);
+  GBG_CUDA_TRY(cudaGetLastError());
+  GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(ncells - 1)),
+                           L.sort_tmp, st));
+  GBG_TRY(exclusive_scan_u32(L.counts, L.counts, ncells + 1, L.scan_tmp, st));
+  T *rec = static_cast<T *>(L.rec);
+  T *qs = static_cast<T *>(L.qs);
+  k_scatter_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
+      g, s, ncomp, x, static_cast<const T *>(q), m, L.perm, T(alpha), rec, qs);
+  GBG_CUDA_TRY(cudaGetLastError());
+  const int blocks = launch_blocks(ncells, kThreads);
+  T *f = static_cast<T *>(field);
+  const int bz = beta == 0.0;
+  const int n2 = sch.stencil_width;
+  switch (chunk_for(ncomp)) {
+    case 9: k_scatter_pull<T, 9><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+    case 3: k_scatter_pull<T, 3><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+    default: k_scatter_pull<T, 1><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+  }
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
+// ------------------------------------------------------- argument checks
+
+gbg_status check_grid(const gbg_grid *g) {
+  if (!g) return set_error(GBG_EARG, "null grid");
+  for (int d = 0; d < 3; ++d) {
+    if (g->n[d] <= 0) return set_error(GBG_EARG, "grid_size must be positive along every axis");
+    if (!(std::isfinite(g->domain[d]) && g->domain[d] > 0))
+      return set_error(GBG_EARG, "domain_size must be finite and positive along every axis");
+    if (!(std::isfinite(g->spacing[d]) && g->spacing[d] > 0))
+      return set_error(GBG_EARG, "grid_spacing must be finite and positive along every axis");
+    if (!std::isfinite(g->origin[d])) return set_error(GBG_EARG, "origin must be finite along every axis");
+  }
+  if (g->n[0] > (int64_t(1) << 31) || g->n[1] > (int64_t(1) << 31) || g->n[2] > (int64_t(1) << 31))
+    return set_error(GBG_EUNSUPPORTED, "grid axis longer than 2^31");
+  return GBG_OK;
+}
+
+gbg_status check_scheme(const gbg_scheme *s) {
+  if (!s) return set_error(GBG_EARG, "null scheme");
+  if (s->stencil_width < 2 || s->stencil_width % 2 || s->stencil_width > GBG_MAX_NODES)
+    return set_error(GBG_EARG, "scheme stencil_width must be even, 2..GBG_MAX_NODES");
+  if (s->num_powers < 1 || s->num_powers > GBG_MAX_POWERS)
+    return set_error(GBG_EARG, "scheme num_powers must be 1..GBG_MAX_POWERS");
+  return GBG_OK;
+}
+
+gbg_status check_common(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, int64_t m,
+                        const gbg_scheme *scheme) {
+  GBG_TRY(check_grid(grid));
+  GBG_TRY(check_scheme(scheme));
+  if (dtype != GBG_F32 && dtype != GBG_F64) return set_error(GBG_EARG, "dtype must be GBG_F32 or GBG_F64");
+  if (ncomp < 1) return set_error(GBG_EARG, "ncomp must be at least 1");
+  if (m < 0) return set_error(GBG_EDIM, "negative point count");
+  if (m > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "more than 2^31-1 points");
+  return GBG_OK;
+}
+
+}  // namespace
+}  // namespace gbg
+
+using namespace gbg;
+
+extern "C" {
+
+gbg_status gbg_interpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, const void *field,
+                           const void *positions, int64_t npoints, const int32_t *traversal,
+                           const gbg_scheme *scheme, void *out, int32_t *device_status,
+                           void *stream) {
+  clear_error();
+  try {
+    GBG_TRY(check_common(grid, dtype, ncomp, npoints, scheme));
+    if (npoints == 0) return GBG_OK;
+    if (!field || !positions || !out) return set_error(GBG_EARG, "interpolate: null array");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    if (dtype == GBG_F64)
+      return dispatch_gather<double>(*grid, *scheme, ncomp, field, positions, npoints, traversal,
+                                     out, device_status, st);
+    return dispatch_gather<float>(*grid, *scheme, ncomp, field, positions, npoints, traversal, out,
+                                  device_status, st);
+  } catch (...) {
+    return set_error(GBG_ENOMEM, "interpolate: host exception");
+  }
+}
+
+gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
+                                          int64_t npoints, const gbg_scheme *scheme, size_t *bytes) {
+  clear_error();
+  GBG_TRY(check_common(grid, dtype, ncomp, npoints, scheme));
+  if (!bytes) return set_error(GBG_EARG, "null bytes");
+  const int64_t ncells = grid->n[0] * grid->n[1] * grid->n[2];
+  if (ncells >= (int64_t(1) << 32) - 1)
+    return set_error(GBG_EUNSUPPORTED, "anterpolate: grids of 2^32 or more cells");
+  Arena a;
+  scatter_layout(a, npoints, ncells, ncomp, scheme->stencil_width, dtype == GBG_F64 ? 8 : 4);
+  *bytes = npoints == 0 ? 0 : a.used + 256;
+  return GBG_OK;
+}
+
+gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, void *field,
+                           const void *positions, int64_t npoints, const void *quantities,
+                           const int32_t *traversal, const gbg_scheme *scheme, double alpha,
+                           double beta, void *workspace, size_t workspace_bytes,
+                           int32_t *device_status, void *stream) {
+  clear_error();
+  (void)traversal;  // the deterministic pull is independent of the visiting order
+  try {
+    size_t need = 0;
+    GBG_TRY(gbg_anterpolate_workspace_size(grid, dtype, ncomp, npoints, scheme, &need));
+    if (!field) return set_error(GBG_EARG, "anterpolate: null field");
+    if (!std::isfinite(alpha) || !std::isfinite(beta)) {
+      // allowed by the reference (T(alpha) of an Inf is Inf); passed through as given
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int64_t total = grid->n[0] * grid->n[1] * grid->n[2] * (int64_t)ncomp;
+    if (npoints == 0) {
+      // Interpolation.jl:1309-1313: the prescale happens even with no points.
+      k_fill_or_scale<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(field, total,
+                                                                           dtype == GBG_F64, beta);
+      GBG_CUDA_TRY(cudaGetLastError());
+      return GBG_OK;
+    }
+    if (!positions || !quantities) return set_error(GBG_EARG, "anterpolate: null array");
+    Scratch scratch;
+    GBG_TRY(scratch.acquire(workspace, workspace_bytes, need, st));
+    Arena a;
+    a.base = static_cast<char *>(scratch.ptr);
+    const int64_t ncells = grid->n[0] * grid->n[1] * grid->n[2];
+    const ScatterLayout L =
+        scatter_layout(a, npoints, ncells, ncomp, scheme->stencil_width, dtype == GBG_F64 ? 8 : 4);
+    if (dtype == GBG_F64)
+      return dispatch_scatter<double>(*grid, *scheme, ncomp, field, positions, npoints, quantities,
+                                      alpha, beta, L, device_status, st);
+    return dispatch_scatter<float>(*grid, *scheme, ncomp, field, positions, npoints, quantities,
+                                   alpha, beta, L, device_status, st);
+  } catch (...) {
+    return set_error(GBG_ENOMEM, "anterpolate: host exception");
+  }
+}
+
+static gbg_status traversal_tiles(const gbg_grid *grid, int64_t tile_size, int64_t tiles[3]) {
+  if (tile_size < 1) return set_error(GBG_EARG, "tile_size must be at least 1, got " + std::to_string(tile_size));
+  for (int d = 0; d < 3; ++d) {
+    const int64_t t = (grid->n[d] + tile_size - 1) / tile_size;
+    tiles[d] = t > 1 ? t : 1;
+  }
+  const double total = (double)tiles[0] * (double)tiles[1] * (double)tiles[2];
+  if (total >= 4294967296.0) return set_error(GBG_EUNSUPPORTED, "traversal order: 2^32 or more tiles");
+  return GBG_OK;
+}
+
+gbg_status gbg_point_traversal_order_workspace_size(const gbg_grid *grid, int64_t npoints,
+                                                    int64_t tile_size, size_t *bytes) {
+  clear_error();
+  GBG_TRY(check_grid(grid));
+  int64_t tiles[3];
+  GBG_TRY(traversal_tiles(grid, tile_size, tiles));
+  if (!bytes) return set_error(GBG_EARG, "null bytes");
+  if (npoints < 0 || npoints > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "point count outside 0..2^31-1");
+  Arena a;
+  a.take<uint32_t>((size_t)npoints);
+  a.take<uint32_t>((size_t)npoints);
+  a.take<uint32_t>((size_t)npoints);
+  a.take<char>(radix_sort_temp_bytes(npoints));
+  *bytes = npoints == 0 ? 0 : a.used + 256;
+  return GBG_OK;
+}
+
+gbg_status gbg_point_traversal_order(const gbg_grid *grid, gbg_dtype dtype, const void *positions,
+                                     int64_t npoints, int64_t tile_size, int32_t *order,
+                                     void *workspace, size_t workspace_bytes, void *stream) {
+  clear_error();
+  try {
+    size_t need = 0;
+    GBG_TRY(gbg_point_traversal_order_workspace_size(grid, npoints, tile_size, &need));
+    if (dtype != GBG_F32 && dtype != GBG_F64) return set_error(GBG_EARG, "dtype must be GBG_F32 or GBG_F64");
+    if (npoints == 0) return GBG_OK;
+    if (!positions || !order) return set_error(GBG_EARG, "traversal order: null array");
+    int64_t tiles[3];
+    GBG_TRY(traversal_tiles(grid, tile_size, tiles));
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Scratch scratch;
+    GBG_TRY(scratch.acquire(workspace, workspace_bytes, need, st));
+    Arena a;
+    a.base = static_cast<char *>(scratch.ptr);
+    uint32_t *keys = a.take<uint32_t>((size_t)npoints);
+    uint32_t *skeys = a.take<uint32_t>((size_t)npoints);
+    uint32_t *perm = a.take<uint32_t>((size_t)npoints);
+    void *tmp = a.take<char>(radix_sort_temp_bytes(npoints));
+    const int blocks = launch_blocks(npoints, kThreads);
+    if (dtype == GBG_F64) {
+      // inverse_tile = T(tiles) / T(domain), origin = T(origin)  (Interpolation.jl:773-774)
+      k_tile_keys<double><<<blocks, kThreads, 0, st>>>(
+          static_cast<const double *>(positions), npoints, grid->origin[0], grid->origin[1],
+          grid->origin[2], (double)tiles[0] / grid->domain[0], (double)tiles[1] / grid->domain[1],
+          (double)tiles[2] / grid->domain[2], tiles[0], tiles[1], tiles[2], keys);
+    } else {
+      k_tile_keys<float><<<blocks, kThreads, 0, st>>>(
+          static_cast<const float *>(positions), npoints, (float)grid->origin[0],
+          (float)grid->origin[1], (float)grid->origin[2], (float)tiles[0] / (float)grid->domain[0],
+          (float)tiles[1] / (float)grid->domain[1], (float)tiles[2] / (float)grid->domain[2],
+          tiles[0], tiles[1], tiles[2], keys);
+    }
+    GBG_CUDA_TRY(cudaGetLastError());
+    const uint64_t max_key = (uint64_t)tiles[0] * (uint64_t)tiles[1] * (uint64_t)tiles[2] - 1;
+    GBG_TRY(radix_sort_pairs(keys, nullptr, skeys, perm, npoints, bits_for(max_key), tmp, st));
+    k_to_one_based<<<blocks, kThreads, 0, st>>>(perm, order, npoints);
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+  } catch (...) {
+    return set_error(GBG_ENOMEM, "traversal order: host exception");
+  }
+}
+
+gbg_status gbg_validate_traversal(const int32_t *order, int64_t npoints, int64_t *host_low,
+                                  int64_t *host_high, int64_t *host_visited, void *stream) {
+  clear_error();
+  if (npoints < 0 || npoints > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "point count outside 0..2^31-1");
+  if (npoints == 0) {
+    if (host_visited) *host_visited = 0;
+    return GBG_OK;
+  }
+  if (!order) return set_error(GBG_EARG, "validate traversal: null order");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Scratch scratch;
+  const size_t need = 256 + sizeof(uint32_t) * (size_t)npoints;
+  GBG_TRY(scratch.acquire(nullptr, 0, need, st));
+  unsigned long long *stats = static_cast<unsigned long long *>(scratch.ptr);
+  uint32_t *seen = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch.ptr) + 256);
+  GBG_CUDA_TRY(cudaMemsetAsync(seen, 0, sizeof(uint32_t) * (size_t)npoints, st));
+  k_validate_init<<<1, 1, 0, st>>>(stats);
+  k_validate<<<launch_blocks(npoints, kThreads), kThreads, 0, st>>>(order, npoints, seen, stats);
+  GBG_CUDA_TRY(cudaGetLastError());
+  long long h[3];
+  GBG_CUDA_TRY(cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GBG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (host_low) *host_low = h[0];
+  if (host_high) *host_high = h[1];
+  if (host_visited) *host_visited = h[2];
+  if (h[0] < 1 || h[1] > npoints)
+    return set_error(GBG_ETRAVERSAL, "a point traversal order must name points in 1:" + std::to_string(npoints) +
+                                         ", but it spans " + std::to_string(h[0]) + ":" + std::to_string(h[1]));
+  if (h[2] != npoints)
+    return set_error(GBG_ETRAVERSAL, "a point traversal order must name every point exactly once, but it names " +
+                                         std::to_string(h[2]) + " of " + std::to_string(npoints));
+  return GBG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,162 @@
+/*
+ * gbg_transfer.h -- C ABI of the GB300 (sm_103a) particle gather/scatter library.
+ *
+ * This library replaces the spline transfer path of GBGPeriodicFields.jl
+ * (src/Interpolation.jl, src/Points.jl, and the device storage of src/Fields.jl).
+ * Every entry point is extern "C" with plain pointers and sizes, returns a status
+ * code, never throws and never aborts.  A Julia facade binds these with ccall and
+ * maps the status codes to the reference's exceptions (ArgumentError,
+ * DimensionMismatch).
+ *
+ * Conventions (the reference's, 0-based here):
+ *   - arrays are column-major:
+ *       field      (Nx, Ny, Nz, ncomp):  f[x + Nx*y + Nx*Ny*z + N*c], N = Nx*Ny*Nz
+ *       positions  (M, 3):               pos[p + M*d]
+ *       values     (M, ncomp):           v[p + M*c]
+ *     ncomp = 3^R for a tensor field of order R (R = 0 scalar, 1 vector, ...); a
+ *     tensor fibre is itself column-major (Interpolation.jl:1038-1048).
+ *   - all array pointers are DEVICE pointers unless stated otherwise;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ *     Calls are stream-ordered and asynchronous; the reference's transfers are
+ *     synchronous, so a facade synchronizes the stream before returning;
+ *   - `device_status` (optional, may be NULL) is a device int32 that kernels OR
+ *     GBG_DEV_* bits into.  Device code never traps: invalid input found on the
+ *     device (a non-finite position, an out-of-range traversal entry) is reported
+ *     here and the affected point is skipped or yields NaN.
+ */
+#ifndef GBG_TRANSFER_H
+#define GBG_TRANSFER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBG_ABI_VERSION 1
+
+typedef int32_t gbg_status;
+#define GBG_OK 0
+#define GBG_EARG 1          /* ArgumentError: bad scheme, tensor order, precision, order ... */
+#define GBG_EDIM 2          /* DimensionMismatch: point counts differ */
+#define GBG_ENOMEM 3        /* device allocation failed or workspace too small */
+#define GBG_ECUDA 4         /* a CUDA runtime call failed */
+#define GBG_ENONFINITE 5    /* a non-finite or out-of-range position reached the locate step */
+#define GBG_ETIMEOUT 6      /* a bounded wait gave up */
+#define GBG_EUNSUPPORTED 7  /* outside the sizes this build handles (stated per entry point) */
+#define GBG_EBUSY 8         /* admission refused (serving) */
+#define GBG_ETRAVERSAL 9    /* a traversal order is not a permutation of 1:M */
+
+typedef int32_t gbg_dtype;
+#define GBG_F32 1
+#define GBG_F64 2
+
+/* Bits written to *device_status by kernels. */
+#define GBG_DEV_NONFINITE 1
+#define GBG_DEV_TRAVERSAL 2
+
+/* Grid3D (Fields.jl:165-200).  spacing is stored, as in the reference, and must equal
+ * domain ./ n in the transfer's element type. */
+typedef struct {
+  int64_t n[3];
+  double domain[3];
+  double spacing[3];
+  double origin[3];
+} gbg_grid;
+
+#define GBG_MAX_NODES 16
+#define GBG_MAX_POWERS 32
+#define GBG_SCHEME_CUSTOM 0
+#define GBG_SCHEME_LALESCU 1
+#define GBG_SCHEME_LAGRANGE 2
+
+/* A local spline scheme (Interpolation.jl:227-312): stencil_width = N2 = 2n+2 nodes
+ * per axis at offsets -n..n+1, weight polynomials of num_powers = M2 coefficients.
+ * coefficients[q + N2*r] is the t^r coefficient of node q, in Float64. */
+typedef struct {
+  int32_t kind;
+  int32_t stencil_width;
+  int32_t smoothness; /* LalescuSpline's m; -1 for the others */
+  int32_t num_powers;
+  double coefficients[GBG_MAX_NODES * GBG_MAX_POWERS];
+} gbg_scheme;
+
+/* ---------------------------------------------------------------- general */
+
+/* ABI version (GBG_ABI_VERSION). */
+int32_t gbg_abi_version(void);
+/* Static text for a status code. */
+const char *gbg_status_string(gbg_status status);
+/* The calling host thread's message for its last failed call ("" if none). */
+const char *gbg_last_error(void);
+
+/* ---------------------------------------------------------------- schemes */
+
+/* LalescuSpline(stencil_width; smoothness) -- Interpolation.jl:244-258 (with
+ * _stencil_neighbours 236-241, _fornberg 326-354, _hermite_weight_matrix 367-392).
+ * smoothness < 0 selects the default stencil_width/2 - 1.  CatmullRom is (4, 1)
+ * (Interpolation.jl:424).  GBG_EARG for an odd or < 2 width or m outside 0..2n. */
+gbg_status gbg_scheme_lalescu(int32_t stencil_width, int32_t smoothness, gbg_scheme *out);
+/* LagrangeSpline(stencil_width) -- Interpolation.jl:293-306 (_lagrange_weight_matrix
+ * 403-415). */
+gbg_status gbg_scheme_lagrange(int32_t stencil_width, gbg_scheme *out);
+/* A scheme from caller coefficients (N2 x M2, column-major, Float64): what a facade
+ * passes when it holds the reference's own SMatrix (spline_coefficients, 311-312). */
+gbg_status gbg_scheme_custom(int32_t stencil_width, int32_t num_powers,
+                             const double *host_coefficients, gbg_scheme *out);
+/* Host helper: the N2 per-axis weights at t (Interpolation.jl:440-446), Float64. */
+gbg_status gbg_axis_weights(const gbg_scheme *scheme, double t, double *host_weights);
+
+/* ---------------------------------------------------- drop-in transfers */
+
+/* interpolate! -- Interpolation.jl:1181-1198 (kernel 1007-1052).  Gathers the
+ * ncomp-component field at the M points into out (M, ncomp).  field, positions and
+ * out share dtype (the reference refuses mixed precision, 1125-1138).  traversal is
+ * NULL or a 1-based permutation of 1:M (PointTraversalOrder indices, 618-627); it
+ * changes only the visiting order and the result is bitwise the same with or
+ * without it.  M = 0 is legal. */
+gbg_status gbg_interpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
+                           const void *field, const void *positions, int64_t npoints,
+                           const int32_t *traversal, const gbg_scheme *scheme, void *out,
+                           int32_t *device_status, void *stream);
+
+/* anterpolate! -- Interpolation.jl:1299-1323 (kernel 1063-1106, prescale 1309-1313):
+ * field = alpha * W^T q + beta * field, with beta == 0 overwriting (NaN-safe).
+ * Deterministic: the result is bitwise identical run to run and independent of the
+ * traversal (points are cell-sorted on the device and every node sums its
+ * contributions in a fixed order, with no float atomics).  workspace: device scratch
+ * of at least gbg_anterpolate_workspace_size bytes, or NULL (the library then takes
+ * stream-ordered scratch with cudaMallocAsync and releases it before returning). */
+gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, void *field,
+                           const void *positions, int64_t npoints, const void *quantities,
+                           const int32_t *traversal, const gbg_scheme *scheme, double alpha,
+                           double beta, void *workspace, size_t workspace_bytes,
+                           int32_t *device_status, void *stream);
+gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
+                                          int64_t npoints, const gbg_scheme *scheme,
+                                          size_t *bytes);
+
+/* point_traversal_order / point_traversal_order! -- Interpolation.jl:816-833 and
+ * 953-980 (keys 645-661 with the saturating _tile_index 636-642).  Writes a 1-based
+ * permutation into order (M int32) grouping points by tile_size^3-cell tiles.  The
+ * device sort is stable, so within a tile points keep their index order: the result
+ * is deterministic and is one of the orders the reference can return.
+ * GBG_EUNSUPPORTED if the tile count reaches 2^32. */
+gbg_status gbg_point_traversal_order(const gbg_grid *grid, gbg_dtype dtype,
+                                     const void *positions, int64_t npoints, int64_t tile_size,
+                                     int32_t *order, void *workspace, size_t workspace_bytes,
+                                     void *stream);
+gbg_status gbg_point_traversal_order_workspace_size(const gbg_grid *grid, int64_t npoints,
+                                                    int64_t tile_size, size_t *bytes);
+
+/* PointTraversalOrder validation -- Interpolation.jl:560-589.  Synchronous: returns
+ * GBG_OK if order is a permutation of 1:M, GBG_ETRAVERSAL otherwise, and reports the
+ * extrema and the number of distinct points visited through the host pointers. */
+gbg_status gbg_validate_traversal(const int32_t *order, int64_t npoints, int64_t *host_low,
+                                  int64_t *host_high, int64_t *host_visited, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
