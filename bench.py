@@ -1,0 +1,403 @@
+#!/usr/bin/env python
+"""Benchmark of the particle gather/scatter path on GB300.
+
+Workload (the benchmark's plain-FP64-at-scale configuration): a 256^3 Float64
+3-component velocity field (random Fourier modes |k| <= 64, |k|^(-11/6) spectrum,
+divergence projected out) on [0, 2pi)^3 and 1e7 points, 70% uniform + 30% in 1000
+Gaussian blobs of sigma = 0.05.  One step = build the traversal order, then cubic
+(CatmullRom) gather + scatter and quintic (LalescuSpline(6)) gather + scatter: 4
+particle-evaluations per point per step (one evaluation = one point x one field, all
+components, one transfer).  Inputs are synthetic and seeded; the field (403 MB) and the
+point arrays are larger than L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0).  With --impl reference it times the reference's CPU path
+(the oracle's OpenMP restatement of the reference's KernelAbstractions CPU kernels) on
+the host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-evals/s (gather+scatter) at fixed error vs FP64; serving p50/p99 ms"
+UNIT = "particle-evals/s"
+N_GRID = (256, 256, 256)
+NCOMP = 3
+M_POINTS = 10_000_000
+KMAX = 64
+WORKLOAD = ("256^3 Float64 3-component velocity field (|k|<=64, |k|^-11/6, divergence-free), "
+            "1e7 points (70% uniform + 30% in 1000 Gaussian blobs, sigma=0.05), "
+            "cubic + quintic gather and scatter per step, traversal order rebuilt per step")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- workload
+
+def make_inputs_host(seed: int = 1):
+    from __graft_entry__ import load_package
+    load_package()
+    from gbgperiodicfields_gb300.workloads import clustered_points
+    pos = clustered_points(M_POINTS, seed=seed + 1)
+    q = np.asfortranarray(np.random.Generator(np.random.PCG64(seed + 2)).standard_normal((M_POINTS, NCOMP)))
+    return pos, q
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(m: int, ncomp: int, n: int, s: int, beta_nonzero=False) -> dict:
+    """Compulsory traffic per call: every input read once, every output written once."""
+    gather = m * (3 * s + ncomp * s) + n * ncomp * s
+    scatter = m * (3 * s + ncomp * s) + (2 if beta_nonzero else 1) * n * ncomp * s
+    return {"gather": gather, "scatter": scatter}
+
+
+# -------------------------------------------------------------- GB300 arm
+
+def run_gb300(args, rank, world):
+    import ctypes
+    import torch
+    from __graft_entry__ import load_package
+    gbg = load_package()
+    from gbgperiodicfields_gb300.workloads import spectral_field
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = gbg._lib.load()
+    grid = gbg.Grid3D(N_GRID, (2 * np.pi,) * 3)
+    gC = grid.c()
+    cubic, quintic = gbg.CatmullRom, gbg.LalescuSpline(6)
+    schemes = [cubic, quintic]
+
+    pos_h, q_h = make_inputs_host()
+    field = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device=dev)
+    pos = torch.from_numpy(pos_h).to(dev)
+    q = torch.from_numpy(q_h).to(dev)
+    out = gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev)
+    dep = gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev)
+    order = torch.empty(M_POINTS, dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+
+    nb = ctypes.c_size_t()
+    gbg._lib.check(lib.gbg_point_traversal_order_workspace_size(gC, M_POINTS, 4, ctypes.byref(nb)))
+    ws_order = torch.empty(nb.value, dtype=torch.uint8, device=dev)
+    need = 0
+    for s in schemes:
+        gbg._lib.check(lib.gbg_anterpolate_workspace_size(gC, gbg._lib.GBG_F64, NCOMP, M_POINTS, s.c(), ctypes.byref(nb)))
+        need = max(need, nb.value)
+    ws_scatter = torch.empty(need, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    # per-call CUDA events on the launching stream
+    timings = {"order": [], "gather_cubic": [], "scatter_cubic": [], "gather_quintic": [], "scatter_quintic": []}
+
+    def step(record):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        ev[0].record(stream)
+        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M_POINTS, 4,
+                                                     order.data_ptr(), ws_order.data_ptr(), ws_order.numel(), sh))
+        ev[1].record(stream)
+        k = 2
+        for name, s in (("cubic", cubic), ("quintic", quintic)):
+            gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, NCOMP, field.data_ptr(), pos.data_ptr(), M_POINTS,
+                                               order.data_ptr(), s.c(), out.data_ptr(), status.data_ptr(), sh))
+            ev[k].record(stream)
+            gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, NCOMP, dep.data_ptr(), pos.data_ptr(), M_POINTS,
+                                               q.data_ptr(), None, s.c(), 1.0, 0.0, ws_scatter.data_ptr(),
+                                               ws_scatter.numel(), status.data_ptr(), sh))
+            ev[k + 1].record(stream)
+            k += 2
+        if record is not None:
+            record.append(ev)
+
+    for _ in range(args.warmup):
+        step(None)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    launches0 = lib.gbg_kernel_launches()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    evs = []
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(args.steps):
+        step(evs)
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = lib.gbg_kernel_launches() - launches0
+    ms_total = start.elapsed_time(end)
+    for ev in evs:
+        names = list(timings)
+        for i, nm in enumerate(names):
+            timings[nm].append(ev[i].elapsed_time(ev[i + 1]))
+    if int(status.item()) != 0:
+        raise RuntimeError(f"device status {int(status.item())}")
+
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    evals_per_step = 4 * M_POINTS
+    value = world * evals_per_step * args.steps / (ms_total / 1e3)
+
+    # roofline of the dominant call (by measured time) against the HBM copy peak
+    avg = {k: float(np.mean(v)) for k, v in timings.items()}
+    peak, peak_kind = peaks()
+    ab = algorithmic_bytes(M_POINTS, NCOMP, int(np.prod(N_GRID)), 8)
+    dominant = max(avg, key=avg.get)
+    dom_bytes = ab["scatter"] if dominant.startswith("scatter") else (ab["gather"] if dominant.startswith("gather") else M_POINTS * 28)
+    achieved = dom_bytes / (avg[dominant] / 1e3) / 1e9
+
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "grid": list(N_GRID), "ncomp": NCOMP, "points": M_POINTS,
+                   "schemes": ["CatmullRom", "LalescuSpline(6)"], "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (field 403 MB)"},
+        "per_call_ms": avg,
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": None, "algorithmic_bytes": dom_bytes},
+        "clocks": clk,
+        "gpu_launches": int(launches),
+    }
+
+    if not args.no_e2e:
+        result["e2e"] = e2e_gb300(args, gbg, lib, grid, field, pos_h, q_h, dev, stream)
+    return result
+
+
+def e2e_gb300(args, gbg, lib, grid, field_dev, pos_h, q_h, dev, stream):
+    """The same step through the C ABI with host buffers: every step copies the inputs
+    from pinned host memory and reads every result back."""
+    import torch
+    gC = grid.c()
+    sh = stream.cuda_stream
+    f_h = field_dev.cpu().pin_memory()  # column-major (Nx,Ny,Nz,3) host copy
+    pos_p = torch.from_numpy(pos_h).pin_memory()
+    q_p = torch.from_numpy(q_h).pin_memory()
+    out_h = [torch.empty((NCOMP, M_POINTS), dtype=torch.float64).pin_memory() for _ in range(2)]
+    dep_h = [torch.empty(f_h.shape[::-1], dtype=torch.float64).pin_memory() for _ in range(2)]
+    f_d = gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev)
+    pos_d = gbg.empty_colmajor((M_POINTS, 3), torch.float64, dev)
+    q_d = gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev)
+    out_d = gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev)
+    dep_d = gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev)
+    order = torch.empty(M_POINTS, dtype=torch.int32, device=dev)
+    schemes = [gbg.CatmullRom, gbg.LalescuSpline(6)]
+
+    def step():
+        f_d.copy_(f_h, non_blocking=True)
+        pos_d.copy_(pos_p, non_blocking=True)
+        q_d.copy_(q_p, non_blocking=True)
+        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos_d.data_ptr(), M_POINTS, 4,
+                                                     order.data_ptr(), None, 0, sh))
+        for i, s in enumerate(schemes):
+            gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, NCOMP, f_d.data_ptr(), pos_d.data_ptr(),
+                                               M_POINTS, order.data_ptr(), s.c(), out_d.data_ptr(), None, sh))
+            out_h[i].copy_(out_d.T, non_blocking=True)
+            gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, NCOMP, dep_d.data_ptr(), pos_d.data_ptr(),
+                                               M_POINTS, q_d.data_ptr(), None, s.c(), 1.0, 0.0, None, 0, None, sh))
+            dep_h[i].copy_(dep_d.permute(3, 2, 1, 0), non_blocking=True)
+
+    step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = max(2, args.steps // 2)
+    e0.record(stream)
+    for _ in range(n):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / n
+    h2d = f_h.numel() * 8 + pos_p.numel() * 8 + q_p.numel() * 8
+    d2h = sum(t.numel() * 8 for t in out_h) + sum(t.numel() * 8 for t in dep_h)
+    return {"value": 4 * M_POINTS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+
+# ----------------------------------------------------------- CPU baseline
+
+def cpu_sample_rate(pos_h, q_h, field_h, target_seconds: float):
+    """Times the reference's CPU path (oracle, OpenMP over all host cores) on a bounded
+    sample of the points: the same four transfers per point as a GPU step."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    from __graft_entry__ import load_package
+    load_package()
+    g = oracle.grid_dict(N_GRID)
+    cubic, quintic = oracle.lalescu(4), oracle.lalescu(6)
+    cores = os.cpu_count() or 1
+    dep = np.zeros(field_h.shape, order="F")
+
+    def run(m):
+        p = np.asfortranarray(pos_h[:m])
+        qq = np.asfortranarray(q_h[:m])
+        t0 = time.perf_counter()
+        for c in (cubic, quintic):
+            trav = oracle.traversal_order(g, p)
+            oracle.gather(g, field_h, p, c, traversal=trav, nthreads=cores)
+            oracle.scatter(g, dep, p, qq, c, 1.0, 0.0, traversal=trav, nthreads=cores)
+        return time.perf_counter() - t0
+
+    m = 100_000
+    t = run(m)
+    m2 = int(min(M_POINTS, max(m, m * target_seconds / max(t, 1e-3) * 0.8)))
+    t2 = run(m2)
+    return {"value": 4 * m2 / t2, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{m2} of the {M_POINTS} points (all four transfers, traversal order per transfer), "
+                      f"full 256^3x3 field, {t2:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    from __graft_entry__ import load_package
+    load_package()
+    from gbgperiodicfields_gb300.workloads import spectral_field
+    import torch
+    torch.set_num_threads(os.cpu_count() or 1)
+    pos_h, q_h = make_inputs_host()
+    field_h = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device="cpu")
+    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
+    rates = []
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_sample_rate(pos_h, q_h, field_h, 1.0)
+    for _ in range(args.steps):
+        rates.append(cpu_sample_rate(pos_h, q_h, field_h, per_step))
+    value = float(np.median([r["value"] for r in rates]))
+    base = rates[-1]
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 4 * M_POINTS / value * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "grid": list(N_GRID), "ncomp": NCOMP, "points": M_POINTS,
+                       "schemes": ["CatmullRom", "LalescuSpline(6)"], "parallelism": "host threads"},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "gloo" if args.impl == "reference" else "nccl"
+        if backend == "nccl":
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        dist.init_process_group(backend)
+    if args.impl == "reference":
+        res = run_reference(args, rank, world)
+    else:
+        res = run_gb300(args, rank, world)
+        if rank == 0 and not args.no_cpu:
+            pos_h, q_h = make_inputs_host()
+            from gbgperiodicfields_gb300.workloads import spectral_field
+            field_h = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device="cpu")
+            res["cpu_baseline"] = cpu_sample_rate(pos_h, q_h, field_h, args.cpu_seconds)
+    if rank == 0 and res is not None:
+        print(json.dumps(res), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -550,13 +550,21 @@ def anterpolate_(field: AbstractFieldPhysical, points: PointSet, quantities: Abs
     m = points.npoints
     trav = _check_traversal(traversal, m, field.data.device)
     status = _status_buffer(field.data.device)
+    import ctypes
+    nbytes = ctypes.c_size_t()
+    lib = _lib.load()
+    _lib.check(lib.gbg_anterpolate_workspace_size(field.grid.c(), _DTYPE_CODE[field.data.dtype], field.ncomp,
+                                                  m, scheme.c(), ctypes.byref(nbytes)), "anterpolate!")
+    # scratch from torch's caching allocator, so repeated calls do not re-allocate
+    ws = torch.empty(max(int(nbytes.value), 1), dtype=torch.uint8, device=field.data.device)
     with torch.cuda.device(field.data.device):
         stream = torch.cuda.current_stream()
-        st = _lib.load().gbg_anterpolate(
+        st = lib.gbg_anterpolate(
             field.grid.c(), _DTYPE_CODE[field.data.dtype], field.ncomp, field.data.data_ptr(),
             points.positions.data_ptr() if m else None, m,
             quantities.data.data_ptr() if m else None, trav.data_ptr() if trav is not None else None,
-            scheme.c(), float(alpha), float(beta), None, 0, status.data_ptr(), stream.cuda_stream)
+            scheme.c(), float(alpha), float(beta), ws.data_ptr(), ws.numel(), status.data_ptr(),
+            stream.cuda_stream)
         _lib.check(st, "anterpolate!")
         stream.synchronize()
     _raise_device_status(status)

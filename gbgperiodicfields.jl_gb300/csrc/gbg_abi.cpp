@@ -1,4 +1,5 @@
 // C-ABI plumbing: status text, per-thread error messages, stream-ordered scratch.
+#include <atomic>
 #include <string>
 
 #include "gbg_common.cuh"
@@ -7,6 +8,7 @@ namespace gbg {
 
 namespace {
 thread_local std::string g_last_error;
+std::atomic<uint64_t> g_launches{0};
 }
 
 gbg_status set_error(gbg_status status, const std::string &message) {
@@ -15,6 +17,8 @@ gbg_status set_error(gbg_status status, const std::string &message) {
 }
 
 void clear_error() { g_last_error.clear(); }
+
+void note_launch(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
 gbg_status Scratch::acquire(void *user, size_t user_bytes, size_t need, cudaStream_t s) {
   stream = s;
@@ -25,6 +29,19 @@ gbg_status Scratch::acquire(void *user, size_t user_bytes, size_t need, cudaStre
                                        std::to_string(user_bytes));
     ptr = user;
     return GBG_OK;
+  }
+  // Keep freed blocks in the device's default pool: without a release threshold the pool
+  // hands its memory back at every synchronization and the next call pays a fresh
+  // allocation of the full scratch.
+  static thread_local int configured_device = -1;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev != configured_device) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    configured_device = dev;
   }
   cudaError_t e = cudaMallocAsync(&ptr, need, s);
   if (e != cudaSuccess) {
@@ -64,5 +81,7 @@ const char *gbg_status_string(gbg_status status) {
 }
 
 const char *gbg_last_error(void) { return gbg::g_last_error.c_str(); }
+
+uint64_t gbg_kernel_launches(void) { return gbg::g_launches.load(std::memory_order_relaxed); }
 
 }  // extern "C"

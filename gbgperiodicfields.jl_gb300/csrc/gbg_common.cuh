@@ -18,6 +18,9 @@ namespace gbg {
 gbg_status set_error(gbg_status status, const std::string &message);
 void clear_error();
 
+// Counts kernel launches (gbg_kernel_launches); called next to every <<<...>>>.
+void note_launch(int n = 1);
+
 #define GBG_CUDA_TRY(expr)                                                                  \
   do {                                                                                      \
     cudaError_t _e = (expr);                                                                \

@@ -386,9 +386,9 @@ gbg_status launch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncomp,
   const T *x = static_cast<const T *>(pos);
   T *o = static_cast<T *>(out);
   switch (chunk_for(ncomp)) {
-    case 9: k_gather_plain<T, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
-    case 3: k_gather_plain<T, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
-    default: k_gather_plain<T, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 9: k_gather_plain<T, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
+    case 3: k_gather_plain<T, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
+    default: k_gather_plain<T, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
   }
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
@@ -409,6 +409,7 @@ gbg_status dispatch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncom
       k_gather_plain_dyn<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
           g, s, ncomp, static_cast<const T *>(field), static_cast<const T *>(pos), m, trav,
           static_cast<T *>(out), status);
+      note_launch();
       GBG_CUDA_TRY(cudaGetLastError());
       return GBG_OK;
     }
@@ -451,6 +452,7 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   const T *x = static_cast<const T *>(pos);
   GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(ncells + 1), st));
   k_cell_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, x, m, L.keys, L.counts, status);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(ncells - 1)),
                            L.sort_tmp, st));
@@ -459,15 +461,16 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   T *qs = static_cast<T *>(L.qs);
   k_scatter_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
       g, s, ncomp, x, static_cast<const T *>(q), m, L.perm, T(alpha), rec, qs);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   const int blocks = launch_blocks(ncells, kThreads);
   T *f = static_cast<T *>(field);
   const int bz = beta == 0.0;
   const int n2 = sch.stencil_width;
   switch (chunk_for(ncomp)) {
-    case 9: k_scatter_pull<T, 9><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
-    case 3: k_scatter_pull<T, 3><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
-    default: k_scatter_pull<T, 1><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+    case 9: k_scatter_pull<T, 9><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
+    case 3: k_scatter_pull<T, 3><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
+    default: k_scatter_pull<T, 1><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
   }
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
@@ -571,6 +574,7 @@ gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
       // Interpolation.jl:1309-1313: the prescale happens even with no points.
       k_fill_or_scale<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(field, total,
                                                                            dtype == GBG_F64, beta);
+      note_launch();
       GBG_CUDA_TRY(cudaGetLastError());
       return GBG_OK;
     }
@@ -648,17 +652,20 @@ gbg_status gbg_point_traversal_order(const gbg_grid *grid, gbg_dtype dtype, cons
           static_cast<const double *>(positions), npoints, grid->origin[0], grid->origin[1],
           grid->origin[2], (double)tiles[0] / grid->domain[0], (double)tiles[1] / grid->domain[1],
           (double)tiles[2] / grid->domain[2], tiles[0], tiles[1], tiles[2], keys);
+      note_launch();
     } else {
       k_tile_keys<float><<<blocks, kThreads, 0, st>>>(
           static_cast<const float *>(positions), npoints, (float)grid->origin[0],
           (float)grid->origin[1], (float)grid->origin[2], (float)tiles[0] / (float)grid->domain[0],
           (float)tiles[1] / (float)grid->domain[1], (float)tiles[2] / (float)grid->domain[2],
           tiles[0], tiles[1], tiles[2], keys);
+      note_launch();
     }
     GBG_CUDA_TRY(cudaGetLastError());
     const uint64_t max_key = (uint64_t)tiles[0] * (uint64_t)tiles[1] * (uint64_t)tiles[2] - 1;
     GBG_TRY(radix_sort_pairs(keys, nullptr, skeys, perm, npoints, bits_for(max_key), tmp, st));
     k_to_one_based<<<blocks, kThreads, 0, st>>>(perm, order, npoints);
+    note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   } catch (...) {
@@ -683,7 +690,9 @@ gbg_status gbg_validate_traversal(const int32_t *order, int64_t npoints, int64_t
   uint32_t *seen = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch.ptr) + 256);
   GBG_CUDA_TRY(cudaMemsetAsync(seen, 0, sizeof(uint32_t) * (size_t)npoints, st));
   k_validate_init<<<1, 1, 0, st>>>(stats);
+  note_launch();
   k_validate<<<launch_blocks(npoints, kThreads), kThreads, 0, st>>>(order, npoints, seen, stats);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   long long h[3];
   GBG_CUDA_TRY(cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, st));

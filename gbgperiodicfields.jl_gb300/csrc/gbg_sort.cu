@@ -206,15 +206,18 @@ gbg_status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb == 1) {
     k_scan_tile<<<1, kScanThreads, 0, stream>>>(in, out, n, nullptr);
+    note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   }
   uint32_t *sums = tmp;
   uint32_t *rest = tmp + nb + 64;
   k_block_sums<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, n, sums);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   GBG_TRY(exclusive_scan_u32(sums, sums, nb, rest, stream));
   k_scan_tile<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, out, n, sums);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
 }
@@ -250,9 +253,11 @@ gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, ui
     uint32_t *kout = to_out ? keys_out : kt;
     uint32_t *vout = to_out ? vals_out : vt;
     k_rs_hist<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, n, 8 * p, hist, nb);
+    note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     GBG_TRY(exclusive_scan_u32(hist, hist, kRsBins * nb, scan_tmp, stream));
     k_rs_scatter<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, vin, n, 8 * p, hist, nb, kout, vout);
+    note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     kin = kout;
     vin = vout;

@@ -90,6 +90,8 @@ int32_t gbg_abi_version(void);
 const char *gbg_status_string(gbg_status status);
 /* The calling host thread's message for its last failed call ("" if none). */
 const char *gbg_last_error(void);
+/* Number of kernels this library has launched in this process (all threads). */
+uint64_t gbg_kernel_launches(void);
 
 /* ---------------------------------------------------------------- schemes */
 
@@ -155,6 +157,59 @@ gbg_status gbg_point_traversal_order_workspace_size(const gbg_grid *grid, int64_
  * extrema and the number of distinct points visited through the host pointers. */
 gbg_status gbg_validate_traversal(const int32_t *order, int64_t npoints, int64_t *host_low,
                                   int64_t *host_high, int64_t *host_visited, void *stream);
+
+/* ------------------------------------------- resident storage and binned transfers
+ *
+ * The device storage of a field (replacing Fields.jl's column-major (Nx,Ny,Nz,3^R)
+ * CuArray, 922-974) and a device cell-binned sort of a point set (replacing
+ * point_traversal_order, Interpolation.jl:519-980) that the staged gather and the
+ * deterministic scatter both consume.  Handles are opaque; every handle belongs to
+ * the device that was current when it was created. */
+
+typedef struct gbg_field_s *gbg_field;
+typedef struct gbg_bins_s *gbg_bins;
+
+/* A field of ncomp components on grid, stored as storage_dtype with the components
+ * of a node adjacent (padded to 16 bytes) and a periodic ghost layer wide enough for
+ * stencils up to max_stencil_width nodes, so a brick of cells plus its halo is one
+ * contiguous box.  Allocates on the current device. */
+gbg_status gbg_field_create(const gbg_grid *grid, int32_t ncomp, gbg_dtype storage_dtype,
+                            int32_t max_stencil_width, gbg_field *out);
+gbg_status gbg_field_destroy(gbg_field field);
+/* Copies a reference-layout (Nx,Ny,Nz,ncomp) array of src_dtype into the storage,
+ * converting, and fills the ghost layer. */
+gbg_status gbg_field_import(gbg_field field, gbg_dtype src_dtype, const void *src, void *stream);
+/* Copies the storage out to a reference-layout array of dst_dtype. */
+gbg_status gbg_field_export(gbg_field field, gbg_dtype dst_dtype, void *dst, void *stream);
+/* Device bytes the storage holds. */
+gbg_status gbg_field_bytes(gbg_field field, size_t *bytes);
+
+/* Bins for up to max_points points on grid, grouped by bricks of brick[0] x brick[1] x
+ * brick[2] cells (NULL selects 11 x 8 x 8; each edge 1..64).  Allocates on the current
+ * device. */
+gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32_t *brick,
+                           gbg_bins *out);
+gbg_status gbg_bins_destroy(gbg_bins bins);
+/* Bins the points: each position is wrapped periodically and split into a cell index
+ * and a fractional offset in the positions' own precision (FP64 positions keep FP64
+ * for this step), then the points are stably sorted by brick and cell on the device.
+ * A non-finite position sets GBG_DEV_NONFINITE and is placed in cell 0 with NaN
+ * weights. */
+gbg_status gbg_bins_build(gbg_bins bins, gbg_dtype pos_dtype, const void *positions,
+                          int64_t npoints, int32_t *device_status, void *stream);
+/* The binned order as a 1-based traversal order (point_traversal_order's output). */
+gbg_status gbg_bins_order(gbg_bins bins, int32_t *order, void *stream);
+
+/* Gather of a resident field at binned points into out (M, ncomp) of out_dtype, in the
+ * points' own order.  scheme width must not exceed the field's max_stencil_width. */
+gbg_status gbg_interpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
+                                  gbg_dtype out_dtype, void *out, void *stream);
+/* Deterministic scatter of q (M, ncomp) of q_dtype at binned points into a resident
+ * field: field = alpha * W^T q + beta * field.  No float atomics; the ghost layer is
+ * refreshed.  In FP32 storage each node's sum is compensated (Neumaier). */
+gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
+                                  gbg_dtype q_dtype, const void *q, double alpha, double beta,
+                                  void *stream);
 
 #ifdef __cplusplus
 }

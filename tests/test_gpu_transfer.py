@@ -55,8 +55,8 @@ def test_gather_matches_oracle(gbg, oracle, dev, dtype, R):
     field = gbg.AbstractFieldPhysical(to_dev(f.reshape(grid.grid_size + (3,) * R, order="F"), dev), grid, R)
     points = gbg.PointSet(to_dev(pos, dev))
     for scheme in scheme_list(gbg):
-        got = gbg.interpolate(field, points, scheme).data.reshape(M, C).cpu().numpy() if R else \
-            gbg.interpolate(field, points, scheme).data.cpu().numpy().reshape(M, 1)
+        # column-major fibres: component (a, b) is fibre a + 3b
+        got = gbg.interpolate(field, points, scheme).data.cpu().numpy().reshape((M, C), order="F")
         want = oracle.gather(g, f, pos, scheme.coefficients)
         assert relerr(got, want) <= TOL[dtype], (scheme, relerr(got, want))
 
