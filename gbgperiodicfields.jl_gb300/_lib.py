@@ -92,6 +92,17 @@ SIGNATURES = {
     "gbg_point_traversal_order_workspace_size": (_I32, [_GP, _I64, _I64, ctypes.POINTER(_SZ)]),
     "gbg_validate_traversal": (_I32, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                       ctypes.POINTER(_I64), _P]),
+    "gbg_field_create": (_I32, [_GP, _I32, _I32, _I32, ctypes.POINTER(_P)]),
+    "gbg_field_destroy": (_I32, [_P]),
+    "gbg_field_import": (_I32, [_P, _I32, _P, _P]),
+    "gbg_field_export": (_I32, [_P, _I32, _P, _P]),
+    "gbg_field_bytes": (_I32, [_P, ctypes.POINTER(_SZ)]),
+    "gbg_bins_create": (_I32, [_GP, _I64, ctypes.POINTER(_I32), ctypes.POINTER(_P)]),
+    "gbg_bins_destroy": (_I32, [_P]),
+    "gbg_bins_build": (_I32, [_P, _I32, _P, _I64, _P, _P]),
+    "gbg_bins_order": (_I32, [_P, _P, _P]),
+    "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P]),
+    "gbg_anterpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _D, _D, _P]),
 }
 
 

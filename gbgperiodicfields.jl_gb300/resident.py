@@ -1,0 +1,114 @@
+"""Resident precision form over the C ABI: GB300-owned field storage (FP32, ghost-padded,
+components adjacent) and device cell-binned point sets, with the staged gather and the
+deterministic scatter.  Positions may be Float64: they keep FP64 only for the periodic
+wrap and the cell/fraction split."""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+from .api import Grid3D, _DTYPE_CODE, colmajor, empty_colmajor
+
+
+def _stream():
+    return torch.cuda.current_stream().cuda_stream
+
+
+class ResidentField:
+    """A field of ncomp components held on the device in the library's own layout
+    (gbg_field_create)."""
+
+    def __init__(self, grid: Grid3D, ncomp: int, max_stencil_width: int = 6):
+        self.grid = grid
+        self.ncomp = int(ncomp)
+        self.max_stencil_width = int(max_stencil_width)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().gbg_field_create(grid.c(), self.ncomp, _lib.GBG_F32, self.max_stencil_width,
+                                                ctypes.byref(h)), "gbg_field_create")
+        self.handle = h
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbg_field_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    @property
+    def nbytes(self) -> int:
+        n = ctypes.c_size_t()
+        _lib.check(_lib.load().gbg_field_bytes(self.handle, ctypes.byref(n)))
+        return int(n.value)
+
+    def load(self, data: torch.Tensor):
+        """Import a reference-layout (Nx, Ny, Nz, ncomp) array (Float32 or Float64)."""
+        data = colmajor(data)
+        if tuple(data.shape[:3]) != self.grid.grid_size or data.numel() != self.grid.npoints * self.ncomp:
+            raise _lib.ArgumentError("field data does not match the resident field's shape")
+        _lib.check(_lib.load().gbg_field_import(self.handle, _DTYPE_CODE[data.dtype], data.data_ptr(), _stream()),
+                   "gbg_field_import")
+        return self
+
+    def read(self, dtype=torch.float64, device="cuda") -> torch.Tensor:
+        out = empty_colmajor(self.grid.grid_size + (self.ncomp,), dtype, device)
+        _lib.check(_lib.load().gbg_field_export(self.handle, _DTYPE_CODE[dtype], out.data_ptr(), _stream()),
+                   "gbg_field_export")
+        return out
+
+
+class PointBins:
+    """A device cell-binned sort of a point set (gbg_bins_create / gbg_bins_build)."""
+
+    def __init__(self, grid: Grid3D, max_points: int, brick=None):
+        self.grid = grid
+        self.max_points = int(max_points)
+        h = ctypes.c_void_p()
+        br = (ctypes.c_int32 * 3)(*brick) if brick is not None else None
+        _lib.check(_lib.load().gbg_bins_create(grid.c(), self.max_points, br, ctypes.byref(h)), "gbg_bins_create")
+        self.handle = h
+        self.npoints = 0
+        self.status = None
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbg_bins_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def build(self, positions: torch.Tensor, status: torch.Tensor | None = None):
+        positions = colmajor(positions)
+        self.npoints = int(positions.shape[0])
+        self.status = status
+        _lib.check(_lib.load().gbg_bins_build(self.handle, _DTYPE_CODE[positions.dtype], positions.data_ptr(),
+                                              self.npoints, status.data_ptr() if status is not None else None,
+                                              _stream()), "gbg_bins_build")
+        return self
+
+    def order(self) -> torch.Tensor:
+        o = torch.empty(self.npoints, dtype=torch.int32, device="cuda")
+        _lib.check(_lib.load().gbg_bins_order(self.handle, o.data_ptr(), _stream()), "gbg_bins_order")
+        return o
+
+
+def interpolate_binned(field: ResidentField, bins: PointBins, scheme, out: torch.Tensor | None = None,
+                       dtype=torch.float32) -> torch.Tensor:
+    if out is None:
+        out = empty_colmajor((bins.npoints, field.ncomp), dtype, "cuda")
+    _lib.check(_lib.load().gbg_interpolate_binned(field.handle, bins.handle, scheme.c(), _DTYPE_CODE[out.dtype],
+                                                  out.data_ptr(), _stream()), "gbg_interpolate_binned")
+    return out
+
+
+def anterpolate_binned(field: ResidentField, bins: PointBins, scheme, q: torch.Tensor, alpha=1.0, beta=0.0):
+    q = colmajor(q)
+    _lib.check(_lib.load().gbg_anterpolate_binned(field.handle, bins.handle, scheme.c(), _DTYPE_CODE[q.dtype],
+                                                  q.data_ptr(), float(alpha), float(beta), _stream()),
+               "gbg_anterpolate_binned")
+    return field

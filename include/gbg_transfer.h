@@ -55,6 +55,7 @@ typedef int32_t gbg_dtype;
 /* Bits written to *device_status by kernels. */
 #define GBG_DEV_NONFINITE 1
 #define GBG_DEV_TRAVERSAL 2
+#define GBG_DEV_TIMEOUT 4 /* a bounded wait on a shared-memory copy gave up */
 
 /* Grid3D (Fields.jl:165-200).  spacing is stored, as in the reference, and must equal
  * domain ./ n in the transfer's element type. */
@@ -138,6 +139,7 @@ gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
 gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
                                           int64_t npoints, const gbg_scheme *scheme,
                                           size_t *bytes);
+
 
 /* point_traversal_order / point_traversal_order! -- Interpolation.jl:816-833 and
  * 953-980 (keys 645-661 with the saturating _tile_index 636-642).  Writes a 1-based

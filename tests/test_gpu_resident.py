@@ -1,0 +1,121 @@
+"""GPU tests of the resident precision form: FP32 ghost-padded storage, FP64 positions
+binned on the device, the TMA-staged gather and the deterministic scatter.
+
+Errors are measured against the FP64 oracle on the FP64 field, relative to max|oracle|:
+the precision form's bar is 1e-5.  The binned order is integer work and is compared
+bitwise with a host-side stable sort of the same keys."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+TWO_PI = 2 * np.pi
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+def relerr(got, want):
+    return np.abs(np.asarray(got, np.float64) - want).max() / max(np.abs(want).max(), 1e-300)
+
+
+def setup(gbg, oracle, n, ncomp, m, seed, origin=(0.0, 0.0, 0.0), brick=None, width=6):
+    from gbgperiodicfields_gb300 import resident
+    rng = np.random.default_rng(seed)
+    grid = gbg.Grid3D(n, (TWO_PI,) * 3, origin=origin)
+    g = oracle.grid_dict(grid.grid_size, grid.domain_size, grid.origin)
+    f = np.asfortranarray(rng.standard_normal(n + (ncomp,)))
+    pos = np.asfortranarray(np.array(origin) + TWO_PI * (rng.random((m, 3)) * 1.3 - 0.15))
+    q = np.asfortranarray(rng.standard_normal((m, ncomp)))
+    field = resident.ResidentField(grid, ncomp, max_stencil_width=width).load(torch.from_numpy(f).cuda())
+    bins = resident.PointBins(grid, m, brick=brick).build(torch.from_numpy(pos).cuda())
+    return resident, grid, g, f, pos, q, field, bins
+
+
+@pytest.mark.parametrize("ncomp", [1, 3, 9, 12])
+@pytest.mark.parametrize("width", [2, 4, 6, 8])
+def test_staged_gather_matches_fp64_oracle(gbg, oracle, dev, ncomp, width):
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (24, 20, 18), ncomp, 3000, 10 + width,
+                                                       origin=(0.3, -0.7, 1.1), width=8)
+    scheme = {2: gbg.LalescuSpline(2, 0), 4: gbg.CatmullRom, 6: gbg.LalescuSpline(6), 8: gbg.LagrangeSpline(8)}[width]
+    got = resident.interpolate_binned(field, bins, scheme, dtype=torch.float64).cpu().numpy()
+    want = oracle.gather(g, f, pos, scheme.coefficients)
+    assert relerr(got, want) <= 1e-5
+    # and against the FP64 oracle on the FP32-rounded field: the arithmetic alone
+    f32 = np.asfortranarray(f.astype(np.float32).astype(np.float64))
+    assert relerr(got, oracle.gather(g, f32, pos, scheme.coefficients)) <= 2e-6
+
+
+@pytest.mark.parametrize("ncomp", [1, 3, 12])
+@pytest.mark.parametrize("width", [4, 6])
+def test_staged_scatter_matches_fp64_oracle_and_is_deterministic(gbg, oracle, dev, ncomp, width):
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (20, 22, 18), ncomp, 4000, 30 + width)
+    scheme = gbg.CatmullRom if width == 4 else gbg.LalescuSpline(6)
+    qt = torch.from_numpy(q).cuda()
+    resident.anterpolate_binned(field, bins, scheme, qt, 1.0, 0.0)
+    a = field.read()
+    want = oracle.scatter(g, np.zeros(grid.grid_size + (ncomp,), order="F"), pos, q, scheme.coefficients)
+    assert relerr(a.cpu().numpy(), want) <= 1e-5
+    resident.anterpolate_binned(field, bins, scheme, qt, 1.0, 0.0)
+    assert torch.equal(a, field.read())
+    # alpha / beta: field = 2*W^T q - 0.5*field
+    resident.anterpolate_binned(field, bins, scheme, qt, 2.0, -0.5)
+    want2 = 2 * want - 0.5 * want
+    assert relerr(field.read().cpu().numpy(), want2) <= 1e-5
+
+
+def test_clustered_points_and_empty_bins(gbg, oracle, dev):
+    from gbgperiodicfields_gb300.workloads import clustered_points
+    resident, grid, g, f, _, _, field, bins = setup(gbg, oracle, (32, 32, 32), 3, 10, 5)
+    pos = clustered_points(20000, seed=4, nblobs=5, sigma=0.05)
+    q = np.asfortranarray(np.random.default_rng(6).standard_normal((20000, 3)))
+    bins = resident.PointBins(grid, 20000).build(torch.from_numpy(pos).cuda())
+    got = resident.interpolate_binned(field, bins, gbg.CatmullRom, dtype=torch.float64).cpu().numpy()
+    assert relerr(got, oracle.gather(g, f, pos, gbg.CatmullRom.coefficients)) <= 1e-5
+    resident.anterpolate_binned(field, bins, gbg.CatmullRom, torch.from_numpy(q).cuda())
+    want = oracle.scatter(g, np.zeros((32, 32, 32, 3), order="F"), pos, q, gbg.CatmullRom.coefficients)
+    assert relerr(field.read().cpu().numpy(), want) <= 1e-5
+    # zero points: the scatter with beta = 0 clears the field
+    empty = resident.PointBins(grid, 0).build(torch.zeros((0, 3), dtype=torch.float64, device="cuda"))
+    resident.anterpolate_binned(field, empty, gbg.CatmullRom, torch.zeros((0, 3), dtype=torch.float64, device="cuda"))
+    assert field.read().abs().max().item() == 0.0
+
+
+def test_bins_order_is_a_stable_brick_sort(gbg, oracle, dev):
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (30, 26, 22), 3, 5000, 8, brick=(11, 8, 8))
+    order = bins.order().cpu().numpy()
+    # host restatement of the keys: brick-major, then cell within the brick
+    n = np.array(grid.grid_size)
+    b = np.array([11, 8, 8])
+    nb = -(-n // b)
+    inv = n / np.array(grid.domain_size)
+    u = np.floor((pos - np.array(grid.origin)) * inv).astype(np.int64)
+    c = np.mod(u, n)
+    br = c // b
+    loc = c - br * b
+    key = ((br[:, 2] * nb[1] + br[:, 1]) * nb[0] + br[:, 0]) * b.prod() + (loc[:, 2] * b[1] + loc[:, 1]) * b[0] + loc[:, 0]
+    want = np.argsort(key, kind="stable") + 1
+    assert np.array_equal(order, want)
+
+
+def test_positions_far_outside_wrap(gbg, oracle, dev):
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (16, 16, 16), 3, 500, 9)
+    shifted = pos + TWO_PI * np.array([3.0, -7.0, 12.0])
+    b2 = resident.PointBins(grid, 500).build(torch.from_numpy(np.asfortranarray(shifted)).cuda())
+    a = resident.interpolate_binned(field, bins, gbg.CatmullRom).cpu().numpy()
+    b = resident.interpolate_binned(field, b2, gbg.CatmullRom).cpu().numpy()
+    assert np.abs(a - b).max() <= 1e-5 * np.abs(a).max()
+
+
+def test_nonfinite_position_flagged(gbg, oracle, dev):
+    from gbgperiodicfields_gb300 import resident
+    grid = gbg.Grid3D((16, 16, 16), (TWO_PI,) * 3)
+    pos = torch.tensor([[1.0, 2.0, 3.0], [float("nan"), 0.0, 0.0]], dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    resident.PointBins(grid, 2).build(pos, status)
+    torch.cuda.synchronize()
+    assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE
