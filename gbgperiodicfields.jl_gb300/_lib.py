@@ -92,6 +92,7 @@ SIGNATURES = {
     "gbg_point_traversal_order_workspace_size": (_I32, [_GP, _I64, _I64, ctypes.POINTER(_SZ)]),
     "gbg_validate_traversal": (_I32, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(_I64),
                                       ctypes.POINTER(_I64), _P]),
+    "gbg_anterpolate_noalloc": (_I32, [_GP, _I32, _I32, _P, _P, _I64, _P, _SP, _D, _D, _P, _P]),
     "gbg_field_create": (_I32, [_GP, _I32, _I32, _I32, ctypes.POINTER(_P)]),
     "gbg_field_destroy": (_I32, [_P]),
     "gbg_field_import": (_I32, [_P, _I32, _P, _P]),

@@ -11,6 +11,7 @@
 // and every grid node then pulls, in a fixed order, the contributions of the points in
 // the cells that reach it.  No float atomics are used, so the scatter is bitwise
 // reproducible and independent of any traversal order.
+#include <mutex>
 #include <string>
 
 #include "gbg_common.cuh"
@@ -593,6 +594,59 @@ gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
                                    alpha, beta, L, device_status, st);
   } catch (...) {
     return set_error(GBG_ENOMEM, "anterpolate: host exception");
+  }
+}
+
+// ------------------------------------------------ allocation-free scatter
+//
+// The scratch of gbg_anterpolate_noalloc: one fixed array per device, part of this
+// library's device image, so the entry point never allocates.  Host code must not pass
+// the array's name to a kernel (on the host it names a host-side stand-in); its device
+// address is looked up once per device with that device current.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[GBG_NOALLOC_SCRATCH_BYTES];
+
+static gbg_status noalloc_scratch(void **out) {
+  constexpr int kMaxDevices = 64;
+  static std::mutex mu;
+  static void *addr[kMaxDevices] = {};
+  int dev = 0;
+  GBG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return set_error(GBG_EUNSUPPORTED, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return set_error(GBG_ECUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
+                                      cudaGetErrorString(e));
+    addr[dev] = p;
+  }
+  *out = addr[dev];
+  return GBG_OK;
+}
+
+gbg_status gbg_anterpolate_noalloc(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, void *field,
+                                   const void *positions, int64_t npoints, const void *quantities,
+                                   const gbg_scheme *scheme, double alpha, double beta,
+                                   int32_t *device_status, void *stream) {
+  clear_error();
+  try {
+    size_t need = 0;
+    GBG_TRY(gbg_anterpolate_workspace_size(grid, dtype, ncomp, npoints, scheme, &need));
+    if (need > GBG_NOALLOC_SCRATCH_BYTES)
+      return set_error(GBG_EUNSUPPORTED, "anterpolate (no-alloc): this problem needs " + std::to_string(need) +
+                                             " bytes of scratch; the static scratch holds " +
+                                             std::to_string((size_t)GBG_NOALLOC_SCRATCH_BYTES));
+    void *scratch = nullptr;
+    if (need > 0) GBG_TRY(noalloc_scratch(&scratch));
+    // The shared path: with a caller workspace it allocates nothing, and it clears the
+    // per-cell counts (the only buffer that must start at zero) before every use.
+    const gbg_status st = gbg_anterpolate(grid, dtype, ncomp, field, positions, npoints, quantities, nullptr,
+                                          scheme, alpha, beta, scratch, GBG_NOALLOC_SCRATCH_BYTES,
+                                          device_status, stream);
+    return st;
+  } catch (...) {
+    return set_error(GBG_ENOMEM, "anterpolate (no-alloc): host exception");
   }
 }
 

@@ -140,6 +140,26 @@ gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype,
                                           int64_t npoints, const gbg_scheme *scheme,
                                           size_t *bytes);
 
+/* anterpolate! for callers that cannot allocate device memory.  This entry point has no
+ * counterpart in the reference.  It computes exactly what gbg_anterpolate computes, but
+ * its scratch is a fixed array compiled into this library (GBG_NOALLOC_SCRATCH_BYTES,
+ * 64 MiB, held on every device that loads the library until the process exits), so it
+ * calls no cudaMalloc, cudaFree or other allocating routine.  It exists for callers
+ * whose device memory is not theirs to allocate mid-run: a host that reserves the
+ * GPU's memory up front through its own pool, and a caller held to the reference's
+ * in-place contract that anterpolate! allocates nothing (test/allocations.jl:335-361).
+ * A problem whose scratch (gbg_anterpolate_workspace_size) exceeds the array is
+ * refused with GBG_EUNSUPPORTED.  The first call on a device looks up the array's
+ * device address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  Every call shares the one array: calls that overlap on
+ * the GPU (different streams, or different host threads, on the same device) race and
+ * must be serialized by the caller. */
+#define GBG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
+gbg_status gbg_anterpolate_noalloc(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
+                                   void *field, const void *positions, int64_t npoints,
+                                   const void *quantities, const gbg_scheme *scheme,
+                                   double alpha, double beta, int32_t *device_status,
+                                   void *stream);
 
 /* point_traversal_order / point_traversal_order! -- Interpolation.jl:816-833 and
  * 953-980 (keys 645-661 with the saturating _tile_index 636-642).  Writes a 1-based
