@@ -102,6 +102,21 @@ __device__ __forceinline__ void axis_weights(const SchemeT<T, N2> &s, T t, T (&w
   }
 }
 
+// Horner with a compile-time number of powers M2 (M2 == 0: the guarded form above).
+template <typename T, int N2, int M2>
+__device__ __forceinline__ void axis_weights_m(const SchemeT<T, N2> &s, T t, T (&w)[N2]) {
+  if constexpr (M2 > 0) {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = s.c[q + N2 * (M2 - 1)];
+#pragma unroll
+    for (int p = M2 - 2; p >= 0; --p)
+#pragma unroll
+      for (int q = 0; q < N2; ++q) w[q] = add_rn(mul_rn(w[q], t), s.c[q + N2 * p]);
+  } else {
+    axis_weights<T, N2>(s, t, w);
+  }
+}
+
 // The same for a run-time width, from coefficients staged in shared memory.
 template <typename T>
 __device__ __forceinline__ void axis_weights_dyn(const T *c, int n2, int m2, T t, T *w) {

@@ -7,9 +7,10 @@
 //
 // The gather is one thread per work item, as in the reference, with the stencil weight
 // of each node formed once and applied to every component of the chunk.  The scatter is
-// not the reference's atomic push: points are cell-sorted with a stable device radix sort
-// and every grid node then pulls, in a fixed order, the contributions of the points in
-// the cells that reach it.  No float atomics are used, so the scatter is bitwise
+// not the reference's atomic push: points are sorted by brick and cell with a stable
+// device radix sort, and each brick's nodes are accumulated in shared memory by colour
+// classes of cells with disjoint stencils (or, for a stencil wider than the grid, every
+// node pulls its contributions).  No float atomics are used, so the scatter is bitwise
 // reproducible and independent of any traversal order.
 #include <mutex>
 #include <string>
@@ -309,6 +310,183 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ------------------------------------------------------ colored scatter
+//
+// The default scatter.  Points are sorted by brick and by cell within the brick (a stable
+// radix sort, so the order is fixed).  A CTA owns one brick of nodes and accumulates, in
+// shared memory and in the transfer's own precision, every contribution of the points in
+// the cells whose stencils reach the brick (the extended region).  Two cells whose
+// extended-region coordinates agree modulo N2 on every axis have disjoint stencils, so the
+// cells are processed in N2^3 colour classes, one class at a time: within a class each
+// node is written by at most one thread, with no atomics, and every node receives its
+// contributions in a fixed order (class, then cell, then the sorted points of the cell).
+// The result is deterministic and each node is written to HBM once.
+
+struct BrickGeo {
+  int32_t b[3];
+  int64_t nb[3];
+  int64_t bvol;
+};
+
+template <typename T>
+struct alignas(16) RecT {
+  T t[3];
+  uint32_t loc;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_brick_keys(GridT<T> g, BrickGeo bg, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
+                 uint32_t *__restrict__ counts, int32_t *status) {
+  const int64_t n[3] = {g.nx, g.ny, g.nz};
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    int64_t brick = 0, local = 0;
+#pragma unroll
+    for (int d = 2; d >= 0; --d) {
+      const int64_t c = imod(b[d], n[d]);
+      brick = brick * bg.nb[d] + c / bg.b[d];
+      local = local * bg.b[d] + c % bg.b[d];
+    }
+    const uint32_t key = (uint32_t)(brick * bg.bvol + local);
+    keys[p] = key;
+    atomicAdd(counts + key, 1u);
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_brick_prep(GridT<T> g, BrickGeo bg, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
+                 int64_t m, const uint32_t *__restrict__ perm, T alpha, RecT<T> *__restrict__ rec,
+                 T *__restrict__ qs) {
+  const int64_t n[3] = {g.nx, g.ny, g.nz};
+  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
+       sl += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = perm[sl];
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
+    int64_t local = 0;
+#pragma unroll
+    for (int d = 2; d >= 0; --d) local = local * bg.b[d] + imod(b[d], n[d]) % bg.b[d];
+    RecT<T> r;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) r.t[d] = ok ? t[d] : quiet_nan<T>();
+    r.loc = (uint32_t)local;
+    rec[sl] = r;
+    for (int c = 0; c < ncomp; ++c) qs[sl * ncomp + c] = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
+  }
+}
+
+template <int N, typename T>
+__device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
+  T v = w[0];
+#pragma unroll
+  for (int i = 1; i < N; ++i)
+    if (i == q) v = w[i];
+  return v;
+}
+
+// FIXED: the scheme has M2 == N2 powers (CatmullRom, the default LalescuSpline of each
+// width, LagrangeSpline): Horner with constant indices; otherwise the coefficients are
+// staged in shared memory and Horner runs over the scheme's own powers.
+template <typename T, int N2, bool FIXED>
+__global__ void __launch_bounds__(kThreads)
+    k_scatter_colored(GridT<T> g, BrickGeo bg, SchemeT<T, N2> s, int ncomp,
+                      const uint32_t *__restrict__ cell_start, const RecT<T> *__restrict__ rec,
+                      const T *__restrict__ qs, T *__restrict__ field, T beta, int beta_zero) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *acc = reinterpret_cast<T *>(smem_raw);  // bvol * ncomp, node-major
+  uint32_t *ranges = reinterpret_cast<uint32_t *>(acc + bg.bvol * ncomp);
+  __shared__ T cs[N2 * GBG_MAX_POWERS];
+  if (!FIXED) stage_coeffs(s, cs);
+  constexpr int nbw = (N2 - 2) / 2;
+  const int E0 = bg.b[0] + N2 - 1, E1 = bg.b[1] + N2 - 1, E2 = bg.b[2] + N2 - 1;
+  const int ecount = E0 * E1 * E2;
+  const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
+  const int64_t n[3] = {g.nx, g.ny, g.nz};
+  for (int64_t brick = blockIdx.x; brick < nbricks; brick += gridDim.x) {
+    const int64_t bc[3] = {brick % bg.nb[0], (brick / bg.nb[0]) % bg.nb[1], brick / (bg.nb[0] * bg.nb[1])};
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < bg.bvol * ncomp; i += blockDim.x) acc[i] = T(0);
+    for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+      const int ee[3] = {e % E0, (e / E0) % E1, e / (E0 * E1)};
+      int64_t kb = 0, kl = 0;
+#pragma unroll
+      for (int d = 2; d >= 0; --d) {
+        const int64_t c = imod(bc[d] * bg.b[d] - nbw - 1 + ee[d], n[d]);
+        kb = kb * bg.nb[d] + c / bg.b[d];
+        kl = kl * bg.b[d] + c % bg.b[d];
+      }
+      const int64_t key = kb * bg.bvol + kl;
+      ranges[2 * e] = __ldg(cell_start + key);
+      ranges[2 * e + 1] = __ldg(cell_start + key + 1);
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int cls = 0; cls < N2 * N2 * N2; ++cls) {
+      const int a0 = cls % N2, a1 = (cls / N2) % N2, a2 = cls / (N2 * N2);
+      const int nu = (E0 - a0 + N2 - 1) / N2, nv = (E1 - a1 + N2 - 1) / N2, nw = (E2 - a2 + N2 - 1) / N2;
+      for (int idx = threadIdx.x; idx < nu * nv * nw; idx += blockDim.x) {
+        const int ex = a0 + N2 * (idx % nu), ey = a1 + N2 * ((idx / nu) % nv), ez = a2 + N2 * (idx / (nu * nv));
+        const int e = (ez * E1 + ey) * E0 + ex;
+        const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
+        for (uint32_t sl = r0; sl < r1; ++sl) {
+          const RecT<T> r = rec[sl];
+          T w1[N2], w2[N2], w3[N2];
+          if constexpr (FIXED) {
+            axis_weights_m<T, N2, N2>(s, r.t[0], w1);
+            axis_weights_m<T, N2, N2>(s, r.t[1], w2);
+            axis_weights_m<T, N2, N2>(s, r.t[2], w3);
+          } else {
+            axis_weights_dyn(cs, N2, s.m2, r.t[0], w1);
+            axis_weights_dyn(cs, N2, s.m2, r.t[1], w2);
+            axis_weights_dyn(cs, N2, s.m2, r.t[2], w3);
+          }
+          const T *qv = qs + (int64_t)sl * ncomp;
+#pragma unroll 1
+          for (int k = 0; k < N2; ++k) {
+            const int lz = ez + k - (N2 - 1);
+            if (lz < 0 || lz >= bg.b[2] || bc[2] * bg.b[2] + lz >= g.nz) continue;
+            const T w3k = pick_t(w3, k);
+#pragma unroll 1
+            for (int j = 0; j < N2; ++j) {
+              const int ly = ey + j - (N2 - 1);
+              if (ly < 0 || ly >= bg.b[1] || bc[1] * bg.b[1] + ly >= g.ny) continue;
+              const T wyz = mul_rn(pick_t(w2, j), w3k);
+              T *arow = acc + ((lz * bg.b[1] + ly) * bg.b[0]) * ncomp;
+#pragma unroll
+              for (int i = 0; i < N2; ++i) {
+                const int lx = ex + i - (N2 - 1);
+                if (lx < 0 || lx >= bg.b[0] || bc[0] * bg.b[0] + lx >= g.nx) continue;
+                const T w = mul_rn(wyz, w1[i]);
+                T *an = arow + lx * ncomp;
+                for (int c = 0; c < ncomp; ++c) an[c] = fma_rn(w, __ldg(qv + c), an[c]);
+              }
+            }
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // write-back in the reference layout: node fastest, so a warp writes a contiguous row
+    for (int64_t i = threadIdx.x; i < bg.bvol * ncomp; i += blockDim.x) {
+      const int c = (int)(i / bg.bvol);
+      const int64_t nl = i - (int64_t)c * bg.bvol;
+      const int lx = (int)(nl % bg.b[0]), ly = (int)((nl / bg.b[0]) % bg.b[1]), lz = (int)(nl / (bg.b[0] * bg.b[1]));
+      const int64_t x = bc[0] * bg.b[0] + lx, y = bc[1] * bg.b[1] + ly, z = bc[2] * bg.b[2] + lz;
+      if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
+      T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
+      const T v = acc[nl * ncomp + c];
+      *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
+    }
+  }
+}
+
 // ------------------------------------------------------- traversal order
 
 // Interpolation.jl:636-642: the comparisons happen in floating point, before any
@@ -417,6 +595,35 @@ gbg_status dispatch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncom
   }
 }
 
+// Which scatter runs, and its bricks: the coloured push whenever every axis is at least
+// a stencil wide and a brick's accumulators fit in shared memory, else the node pull
+// (which also handles a stencil wider than the grid, reached several times per node).
+struct ScatterPlan {
+  bool colored = false;
+  BrickGeo bg{};
+  int64_t nkeys = 0;
+  size_t smem = 0;
+};
+
+ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
+  ScatterPlan p;
+  const int base[3] = {(size_t)ncomp * esize > 24 ? 8 : 16, 8, 8};
+  bool wide_enough = n2 <= 8;
+  int64_t nbricks = 1;
+  for (int d = 0; d < 3; ++d) {
+    p.bg.b[d] = (int32_t)std::min<int64_t>(base[d], g.n[d]);
+    p.bg.nb[d] = (g.n[d] + p.bg.b[d] - 1) / p.bg.b[d];
+    nbricks *= p.bg.nb[d];
+    if (g.n[d] < n2) wide_enough = false;
+  }
+  p.bg.bvol = (int64_t)p.bg.b[0] * p.bg.b[1] * p.bg.b[2];
+  p.smem = (size_t)p.bg.bvol * ncomp * esize +
+           sizeof(uint32_t) * 2 * (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
+  p.colored = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;
+  p.nkeys = p.colored ? nbricks * p.bg.bvol : g.n[0] * g.n[1] * g.n[2];
+  return p;
+}
+
 struct ScatterLayout {
   uint32_t *keys, *counts, *skeys, *perm;
   void *sort_tmp;
@@ -424,15 +631,16 @@ struct ScatterLayout {
   void *rec, *qs;
 };
 
-ScatterLayout scatter_layout(Arena &a, int64_t m, int64_t ncells, int ncomp, int n2, size_t esize) {
+ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncomp, int n2, size_t esize) {
   ScatterLayout L;
   L.keys = a.take<uint32_t>((size_t)m);
-  L.counts = a.take<uint32_t>((size_t)ncells + 1);
+  L.counts = a.take<uint32_t>((size_t)P.nkeys + 1);
   L.skeys = a.take<uint32_t>((size_t)m);
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
-  L.scan_tmp = a.take<uint32_t>(scan_temp_elems(ncells + 1));
-  L.rec = a.take<char>((size_t)m * 3 * n2 * esize);
+  L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
+  const size_t rec_bytes = P.colored ? (esize == 8 ? sizeof(RecT<double>) : sizeof(RecT<float>)) : 3 * n2 * esize;
+  L.rec = a.take<char>((size_t)m * rec_bytes);
   L.qs = a.take<char>((size_t)m * ncomp * esize);
   return L;
 }
@@ -443,15 +651,57 @@ int bits_for(uint64_t max_value) {
   return b;
 }
 
+template <typename T, int N2, bool FIXED>
+gbg_status launch_colored(const GridT<T> &g, const ScatterPlan &P, const gbg_scheme &sch, int ncomp,
+                          const ScatterLayout &L, T *field, double beta, cudaStream_t st) {
+  const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
+  auto kernel = k_scatter_colored<T, N2, FIXED>;
+  GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
+  const int64_t nbricks = P.bg.nb[0] * P.bg.nb[1] * P.bg.nb[2];
+  int dev = 0, sms = 1, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, P.smem);
+  const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
+  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, s, ncomp, L.counts, static_cast<const RecT<T> *>(L.rec),
+                                           static_cast<const T *>(L.qs), field, T(beta), beta == 0.0);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
 template <typename T>
 gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int ncomp, void *field,
                             const void *pos, int64_t m, const void *q, double alpha, double beta,
-                            const ScatterLayout &L, int32_t *status, cudaStream_t st) {
+                            const ScatterPlan &P, const ScatterLayout &L, int32_t *status, cudaStream_t st) {
   const GridT<T> g = make_grid<T>(grid);
+  const T *x = static_cast<const T *>(pos);
+  T *f = static_cast<T *>(field);
+  GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(P.nkeys + 1), st));
+  if (P.colored) {
+    k_brick_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, status);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
+    GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
+    k_brick_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, ncomp, x, static_cast<const T *>(q), m,
+                                                                     L.perm, T(alpha), static_cast<RecT<T> *>(L.rec),
+                                                                     static_cast<T *>(L.qs));
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    const int w = sch.stencil_width;
+    const bool fixed = sch.num_powers == w;
+    if (w == 2) return fixed ? launch_colored<T, 2, true>(g, P, sch, ncomp, L, f, beta, st)
+                             : launch_colored<T, 2, false>(g, P, sch, ncomp, L, f, beta, st);
+    if (w == 4) return fixed ? launch_colored<T, 4, true>(g, P, sch, ncomp, L, f, beta, st)
+                             : launch_colored<T, 4, false>(g, P, sch, ncomp, L, f, beta, st);
+    if (w == 6) return fixed ? launch_colored<T, 6, true>(g, P, sch, ncomp, L, f, beta, st)
+                             : launch_colored<T, 6, false>(g, P, sch, ncomp, L, f, beta, st);
+    return fixed ? launch_colored<T, 8, true>(g, P, sch, ncomp, L, f, beta, st)
+                 : launch_colored<T, 8, false>(g, P, sch, ncomp, L, f, beta, st);
+  }
   const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
   const int64_t ncells = g.npf;
-  const T *x = static_cast<const T *>(pos);
-  GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(ncells + 1), st));
   k_cell_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, x, m, L.keys, L.counts, status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
@@ -465,7 +715,6 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   const int blocks = launch_blocks(ncells, kThreads);
-  T *f = static_cast<T *>(field);
   const int bz = beta == 0.0;
   const int n2 = sch.stencil_width;
   switch (chunk_for(ncomp)) {
@@ -549,8 +798,10 @@ gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype,
   const int64_t ncells = grid->n[0] * grid->n[1] * grid->n[2];
   if (ncells >= (int64_t(1) << 32) - 1)
     return set_error(GBG_EUNSUPPORTED, "anterpolate: grids of 2^32 or more cells");
+  const size_t es = dtype == GBG_F64 ? 8 : 4;
+  const ScatterPlan P = plan_scatter(*grid, ncomp, es, scheme->stencil_width);
   Arena a;
-  scatter_layout(a, npoints, ncells, ncomp, scheme->stencil_width, dtype == GBG_F64 ? 8 : 4);
+  scatter_layout(a, npoints, P, ncomp, scheme->stencil_width, es);
   *bytes = npoints == 0 ? 0 : a.used + 256;
   return GBG_OK;
 }
@@ -584,14 +835,14 @@ gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
     GBG_TRY(scratch.acquire(workspace, workspace_bytes, need, st));
     Arena a;
     a.base = static_cast<char *>(scratch.ptr);
-    const int64_t ncells = grid->n[0] * grid->n[1] * grid->n[2];
-    const ScatterLayout L =
-        scatter_layout(a, npoints, ncells, ncomp, scheme->stencil_width, dtype == GBG_F64 ? 8 : 4);
+    const size_t es = dtype == GBG_F64 ? 8 : 4;
+    const ScatterPlan P = plan_scatter(*grid, ncomp, es, scheme->stencil_width);
+    const ScatterLayout L = scatter_layout(a, npoints, P, ncomp, scheme->stencil_width, es);
     if (dtype == GBG_F64)
       return dispatch_scatter<double>(*grid, *scheme, ncomp, field, positions, npoints, quantities,
-                                      alpha, beta, L, device_status, st);
+                                      alpha, beta, P, L, device_status, st);
     return dispatch_scatter<float>(*grid, *scheme, ncomp, field, positions, npoints, quantities,
-                                   alpha, beta, L, device_status, st);
+                                   alpha, beta, P, L, device_status, st);
   } catch (...) {
     return set_error(GBG_ENOMEM, "anterpolate: host exception");
   }

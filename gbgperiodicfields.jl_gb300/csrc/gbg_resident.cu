@@ -19,10 +19,10 @@
 // pitch makes the 8 lanes of a quarter-warp hit 8 distinct 16-byte bank groups), and the
 // quarter-warp reduces its partial sums with shuffles.
 //
-// Scatter: a CTA per brick stages the point ranges of the cells around the brick in
-// shared memory; each thread owns grid nodes and pulls, in a fixed order, the weighted
-// quantities of the points whose stencils reach them, with Neumaier-compensated FP32
-// sums.  No float atomics: the result is bitwise reproducible.
+// Scatter: a CTA owns a brick's nodes and adds every contribution of the points whose
+// stencils reach the brick into two-level int32 fixed-point accumulators in shared memory
+// (exact, order-independent integer sums: no float atomics, bitwise reproducible), then
+// writes each node once.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -54,6 +54,7 @@ struct gbg_bins_s {
   void *sort_tmp = nullptr;
   uint32_t *scan_tmp = nullptr;
   float *qs = nullptr;  // sorted, alpha-scaled quantities for the scatter (max_points x 12)
+  unsigned *qmax_bits = nullptr;  // largest |alpha q| of the last scatter, as float bits
   void *block = nullptr;
   size_t bytes = 0;
 };
@@ -285,6 +286,38 @@ __device__ __forceinline__ void tma_load_tile(void *dst, const CUtensorMap *map,
       : "memory");
 }
 
+// All N2 weights at t by Horner (Interpolation.jl:440-446) in FP32.  With a compile-time
+// number of powers M2 every coefficient index is a constant (the coefficients stay in the
+// parameter bank); M2 == 0 is the guarded fallback for unusual schemes.
+template <int N2, int M2>
+__device__ __forceinline__ void weights_all(const SchemeT<float, N2> &s, float t, float (&w)[N2]) {
+  if constexpr (M2 > 0) {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = s.c[q + N2 * (M2 - 1)];
+#pragma unroll
+    for (int p = M2 - 2; p >= 0; --p)
+#pragma unroll
+      for (int q = 0; q < N2; ++q) w[q] = fmaf(w[q], t, s.c[q + N2 * p]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = 0.0f;
+#pragma unroll
+    for (int p = GBG_MAX_POWERS - 1; p >= 0; --p)
+      if (p < s.m2)
+#pragma unroll
+        for (int q = 0; q < N2; ++q) w[q] = fmaf(w[q], t, s.c[q + N2 * p]);
+  }
+}
+
+template <int N>
+__device__ __forceinline__ float pick(const float (&w)[N], int q) {
+  float v = w[0];
+#pragma unroll
+  for (int i = 1; i < N; ++i)
+    if (i == q) v = w[i];
+  return v;
+}
+
 // Horner for one node q of a compile-time-width scheme (Interpolation.jl:440-446), in FP32.
 template <int N2>
 __device__ __forceinline__ float poly(const SchemeT<float, N2> &s, int q, float t) {
@@ -312,9 +345,11 @@ __device__ __forceinline__ void brick_coords(const StagedGeo &g, int64_t b, int6
   bz = b / (g.nb[0] * g.nb[1]);
 }
 
-// Gather: width-4 stencils, a point per quarter-warp.
-template <int CP, typename TO>
-__global__ void __launch_bounds__(kThreads, 1)
+// Gather: width-4 stencils, a point per quarter-warp, 512 threads (64 quarter-warps) per
+// CTA; each quarter-warp loads its next point's record and index while it computes.
+constexpr int kGatherThreads = 512;
+template <int M2, int CP, typename TO>
+__global__ void __launch_bounds__(kGatherThreads, 1)
     k_gather_staged4(const __grid_constant__ CUtensorMap tmap, StagedGeo g, SchemeT<float, 4> s,
                      const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                      const uint32_t *__restrict__ perm, TO *__restrict__ out, int32_t *status, int nbuf,
@@ -331,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int qi = sub & 3, jj = sub >> 2;
   const unsigned seg_mask = 0xFFu << (lane & ~7);
   const int qw = threadIdx.x >> 3;  // quarter-warp id within the CTA
-  const int nqw = kThreads / 8;
+  const int nqw = kGatherThreads / 8;
   uint32_t phase[2] = {0, 0};
   bool failed = false;
 
@@ -359,15 +394,24 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       phase[buf] ^= 1;
       const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
-      for (uint32_t sl = s0 + qw; sl < s1; sl += nqw) {
-        const float4 r = __ldg(rec + sl);
+      uint32_t sl = s0 + qw;
+      float4 r_next = sl < s1 ? __ldg(rec + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
+      uint32_t p_next = sl < s1 ? __ldg(perm + sl) : 0u;
+      for (; sl < s1; sl += nqw) {
+        const float4 r = r_next;
+        const int64_t p = p_next;
+        if (sl + nqw < s1) {
+          r_next = __ldg(rec + sl + nqw);
+          p_next = __ldg(perm + sl + nqw);
+        }
         const uint32_t loc = __float_as_uint(r.w);
         const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
-        const float w1 = poly<4>(s, qi, r.x);
-        const float w2a = poly<4>(s, 2 * jj, r.y), w2b = poly<4>(s, 2 * jj + 1, r.y);
-        float w3[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) w3[k] = poly<4>(s, k, r.z);
+        float wx[4], wy[4], w3[4];
+        weights_all<4, M2>(s, r.x, wx);
+        weights_all<4, M2>(s, r.y, wy);
+        weights_all<4, M2>(s, r.z, w3);
+        const float w1 = pick(wx, qi);
+        const float w2a = pick(wy, 2 * jj), w2b = pick(wy, 2 * jj + 1);
         float acc[CP];
 #pragma unroll
         for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
@@ -408,7 +452,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
         for (int v = 0; v < Q; ++v) qv[v] += __shfl_xor_sync(seg_mask, qv[v], 1, 8);
         if ((sub & 1) == 0) {
-          const int64_t p = perm[sl];
           const int cbase = (up2 ? H : 0) + (up1 ? Q : 0);
 #pragma unroll
           for (int v = 0; v < Q; ++v)
@@ -426,7 +469,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // Gather for other widths: a point per thread over its N2^3 stencil in the tile.
-template <int N2, int CP, typename TO>
+template <int N2, int M2, int CP, typename TO>
 __global__ void __launch_bounds__(kThreads, 1)
     k_gather_staged_generic(const __grid_constant__ CUtensorMap tmap, StagedGeo g, SchemeT<float, N2> s,
                             const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
@@ -469,12 +512,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         const uint32_t loc = __float_as_uint(r.w);
         const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
         float w1[N2], w2[N2], w3[N2];
-#pragma unroll
-        for (int q = 0; q < N2; ++q) {
-          w1[q] = poly<N2>(s, q, r.x);
-          w2[q] = poly<N2>(s, q, r.y);
-          w3[q] = poly<N2>(s, q, r.z);
-        }
+        weights_all<N2, M2>(s, r.x, w1);
+        weights_all<N2, M2>(s, r.y, w2);
+        weights_all<N2, M2>(s, r.z, w3);
         float acc[CP];
 #pragma unroll
         for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
@@ -519,49 +559,87 @@ __global__ void __launch_bounds__(kThreads, 1)
 // ------------------------------------------------------------ staged scatter
 
 // Sorted, alpha-scaled quantities: qs[s*CP + c] = T(alpha) * q[perm[s] + M*c].
+// Also the largest |alpha q| (as ordered float bits; NaN orders above every number, so a
+// NaN quantity shows as a non-finite bound).
 template <typename TQ>
 __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__restrict__ perm, int64_t m,
-                                int ncomp, int cp, float alpha, float *__restrict__ qs) {
+                                int ncomp, int cp, float alpha, float *__restrict__ qs,
+                                unsigned *__restrict__ qmax_bits) {
+  unsigned mx = 0u;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m;
        s += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[s];
-    for (int c = 0; c < cp; ++c) qs[s * cp + c] = c < ncomp ? alpha * (float)q[p + m * c] : 0.0f;
+    for (int c = 0; c < cp; ++c) {
+      const float v = c < ncomp ? alpha * (float)q[p + m * c] : 0.0f;
+      qs[s * cp + c] = v;
+      const unsigned bits = __float_as_uint(fabsf(v));
+      mx = bits > mx ? bits : mx;
+    }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned other = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = other > mx ? other : mx;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
-struct PullGeo {
+struct FixGeo {
   int32_t b[3];
   int64_t nb[3];
   int64_t n[3];
   int32_t e[3];  // extended cell region = brick + width - 1
   int64_t nbricks, bvol;
   int64_t px, py;
-  int32_t halo, cp;
+  int32_t halo, cp, ncomp;
+  double l3;  // bound on |w1*w2*w3|: (max_q sum_r |c[q,r]|)^3
 };
 
-__device__ __forceinline__ void neumaier(float &sum, float &comp, float v) {
-  const float t = __fadd_rn(sum, v);
-  if (fabsf(sum) >= fabsf(v))
-    comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(sum, t), v));
-  else
-    comp = __fadd_rn(comp, __fadd_rn(__fsub_rn(v, t), sum));
-  sum = t;
+// Deterministic scatter.  A CTA owns a brick's nodes; it walks the points of every cell
+// whose stencil reaches the brick (the extended region) and adds each contribution
+// w*alpha*q to fixed-point accumulators in shared memory.  Integer addition is
+// associative, so the sums -- and the result -- do not depend on the order in which the
+// threads add, and no float atomics are involved.
+//
+// Each contribution x = w*q*S1 (S1 a power of two) is split into its nearest integer hi
+// and the residual r = x - hi, |r| <= 1/2, kept as lo = round(r * 2^k); hi and lo go to
+// two int32 accumulators.  Both roundings use the float "magic number" 1.5*2^23 (an FMA
+// lands the value where the float's ulp is 1), so no slow int64 conversion or atomic is
+// needed.  S1 and k come from bounds on one contribution (max|alpha q| * l3) and on a
+// node's sum (points in the region times that), so neither accumulator can overflow; the
+// result carries about 2^-41 of max|alpha q| * l3 per contribution.
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kMagicBits = 0x4B400000;
+
+__device__ __forceinline__ void add_fixed(int *hi_acc, int *lo_acc, int idx, float w, float q, float lo_scale) {
+  const float h = fmaf(w, q, kMagic);
+  const float hi_f = h - kMagic;  // exact: an integer below 2^22
+  const float r = fmaf(w, q, -hi_f);
+  const float l = fmaf(r, lo_scale, kMagic);
+  atomicAdd(hi_acc + idx, __float_as_int(h) - kMagicBits);
+  atomicAdd(lo_acc + idx, __float_as_int(l) - kMagicBits);
 }
 
-// One CTA per brick (persistent): stage the point ranges of the cells whose stencils
-// reach the brick, then each thread pulls for its nodes.  Weight index i reaches node x
-// from cell x + n - i; in the extended region that cell is at ex = lx + N2 - 1 - i.
-template <int N2, int CP>
-__global__ void __launch_bounds__(kThreads)
-    k_scatter_pull_staged(PullGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
-                          const float4 *__restrict__ rec, const float *__restrict__ qs, float *__restrict__ field,
-                          float beta, int beta_zero, int compensated) {
-  extern __shared__ uint32_t ranges[];  // 2 per extended cell
+template <int N2, int M2, int CP>
+__global__ void __launch_bounds__(kThreads, 2)
+    k_scatter_fixed(FixGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
+                    const float4 *__restrict__ rec, const float *__restrict__ qs,
+                    const unsigned *__restrict__ qmax_bits, float *__restrict__ field, float beta,
+                    int beta_zero, int32_t *status) {
+  extern __shared__ int acc_hi[];  // bvol * CP hi, bvol * CP lo, then the cell ranges
+  int *acc_lo = acc_hi + g.bvol * CP;
+  uint32_t *ranges = reinterpret_cast<uint32_t *>(acc_lo + g.bvol * CP);
+  __shared__ unsigned int s_count;
   constexpr int nbw = (N2 - 2) / 2;
   const int ecount = g.e[0] * g.e[1] * g.e[2];
+  const float qmax = __uint_as_float(*qmax_bits);
   for (int64_t b = blockIdx.x; b < g.nbricks; b += gridDim.x) {
     const int64_t bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
     __syncthreads();
+    for (int64_t i = threadIdx.x; i < 2 * g.bvol * CP; i += blockDim.x) acc_hi[i] = 0;
+    if (threadIdx.x == 0) s_count = 0u;
+    __syncthreads();
+    unsigned mine = 0;
     for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
       const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
       const int64_t cx = imod(bx * g.b[0] - nbw - 1 + ex, g.n[0]);
@@ -569,53 +647,118 @@ __global__ void __launch_bounds__(kThreads)
       const int64_t cz = imod(bz * g.b[2] - nbw - 1 + ez, g.n[2]);
       const int64_t kb = ((cz / g.b[2]) * g.nb[1] + cy / g.b[1]) * g.nb[0] + cx / g.b[0];
       const int64_t key = kb * g.bvol + ((cz % g.b[2]) * g.b[1] + cy % g.b[1]) * g.b[0] + cx % g.b[0];
-      ranges[2 * e] = __ldg(cell_start + key);
-      ranges[2 * e + 1] = __ldg(cell_start + key + 1);
+      const uint32_t r0 = __ldg(cell_start + key), r1 = __ldg(cell_start + key + 1);
+      ranges[2 * e] = r0;
+      ranges[2 * e + 1] = r1;
+      mine += r1 - r0;
     }
+    atomicAdd(&s_count, mine);
     __syncthreads();
-    const int nodes = g.b[0] * g.b[1] * g.b[2];
-    for (int nl = threadIdx.x; nl < nodes; nl += blockDim.x) {
-      const int lx = nl % g.b[0], ly = (nl / g.b[0]) % g.b[1], lz = nl / (g.b[0] * g.b[1]);
-      const int64_t x = bx * g.b[0] + lx, y = by * g.b[1] + ly, z = bz * g.b[2] + lz;
-      if (x >= g.n[0] || y >= g.n[1] || z >= g.n[2]) continue;
-      float sum[CP], comp[CP];
+    const unsigned count = s_count;
+    const double one = (double)qmax * g.l3;        // bound on one contribution
+    const double bound = one * (double)count;      // bound on a node's sum
+    const bool finite = isfinite(bound);
+    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
+    int e1 = 0, es = 0;
+    frexp(one, &e1);
+    frexp(bound, &es);
+    int s1 = min(20 - e1, 29 - es);
+    s1 = max(-120, min(120, s1));
+    const int kbits = min(21, 30 - (32 - __clz((int)count)));
+    const float S1 = exp2f((float)s1), LS = exp2f((float)kbits);
+    if (finite && count > 0 && one > 0.0) {
+      if constexpr (N2 == 4) {
+        const int qw = threadIdx.x >> 3, sub = threadIdx.x & 7, qi = sub & 3, jj = sub >> 2;
+        for (int e = qw; e < ecount; e += kThreads / 8) {
+          const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
+          if (r0 == r1) continue;
+          const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
+          const int lx = ex + qi - 3;
+          const bool inx = lx >= 0 && lx < g.b[0] && bx * g.b[0] + lx < g.n[0];
+          for (uint32_t sl = r0; sl < r1; ++sl) {
+            const float4 r = __ldg(rec + sl);
+            float wx[4], wy[4], wz[4];
+            weights_all<4, M2>(s, r.x, wx);
+            weights_all<4, M2>(s, r.y, wy);
+            weights_all<4, M2>(s, r.z, wz);
+            const float w1s = pick(wx, qi) * S1;
+            float q[CP];
+            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
 #pragma unroll
-      for (int c = 0; c < CP; ++c) sum[c] = comp[c] = 0.0f;
-#pragma unroll 1
-      for (int k = 0; k < N2; ++k) {
-#pragma unroll 1
-        for (int j = 0; j < N2; ++j) {
-#pragma unroll 1
-          for (int i = 0; i < N2; ++i) {
-            const int e = ((lz + N2 - 1 - k) * g.e[1] + (ly + N2 - 1 - j)) * g.e[0] + (lx + N2 - 1 - i);
-            const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
-            for (uint32_t sl = r0; sl < r1; ++sl) {
-              const float4 r = __ldg(rec + sl);
-              const float w = __fmul_rn(__fmul_rn(poly<N2>(s, j, r.y), poly<N2>(s, k, r.z)), poly<N2>(s, i, r.x));
-              const float4 *qv = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+            for (int v = 0; v < CP / 4; ++v) {
+              const float4 t = __ldg(q4 + v);
+              q[4 * v] = t.x;
+              q[4 * v + 1] = t.y;
+              q[4 * v + 2] = t.z;
+              q[4 * v + 3] = t.w;
+            }
+            if (!inx) continue;
 #pragma unroll
-              for (int q4 = 0; q4 < CP / 4; ++q4) {
-                const float4 v = __ldg(qv + q4);
-                const float vv[4] = {v.x, v.y, v.z, v.w};
+            for (int jp = 0; jp < 2; ++jp) {
+              const int ly = ey + 2 * jj + jp - 3;
+              if (ly < 0 || ly >= g.b[1] || by * g.b[1] + ly >= g.n[1]) continue;
+              const float wxy = w1s * pick(wy, 2 * jj + jp);
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                  const float add = __fmul_rn(w, vv[u]);
-                  if (compensated)
-                    neumaier(sum[4 * q4 + u], comp[4 * q4 + u], add);
-                  else
-                    sum[4 * q4 + u] = __fadd_rn(sum[4 * q4 + u], add);
+              for (int k = 0; k < 4; ++k) {
+                const int lz = ez + k - 3;
+                if (lz < 0 || lz >= g.b[2] || bz * g.b[2] + lz >= g.n[2]) continue;
+                const float w = wxy * wz[k];
+                const int node = (lz * g.b[1] + ly) * g.b[0] + lx;
+#pragma unroll
+                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * (int)g.bvol + node, w, q[c], LS);
+              }
+            }
+          }
+        }
+      } else {
+        for (int e = threadIdx.x; e < ecount; e += kThreads) {
+          const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
+          if (r0 == r1) continue;
+          const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
+          for (uint32_t sl = r0; sl < r1; ++sl) {
+            const float4 r = __ldg(rec + sl);
+            float wx[N2], wy[N2], wz[N2];
+            weights_all<N2, M2>(s, r.x, wx);
+            weights_all<N2, M2>(s, r.y, wy);
+            weights_all<N2, M2>(s, r.z, wz);
+            const float *q = qs + (int64_t)sl * CP;
+#pragma unroll 1
+            for (int k = 0; k < N2; ++k) {
+              const int lz = ez + k - (N2 - 1);
+              if (lz < 0 || lz >= g.b[2] || bz * g.b[2] + lz >= g.n[2]) continue;
+#pragma unroll 1
+              for (int j = 0; j < N2; ++j) {
+                const int ly = ey + j - (N2 - 1);
+                if (ly < 0 || ly >= g.b[1] || by * g.b[1] + ly >= g.n[1]) continue;
+#pragma unroll
+                for (int i = 0; i < N2; ++i) {
+                  const int lx = ex + i - (N2 - 1);
+                  if (lx < 0 || lx >= g.b[0] || bx * g.b[0] + lx >= g.n[0]) continue;
+                  const float w = wx[i] * wy[j] * wz[k] * S1;
+                  const int node = (lz * g.b[1] + ly) * g.b[0] + lx;
+                  for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * (int)g.bvol + node, w, __ldg(q + c), LS);
                 }
               }
             }
           }
         }
       }
-      float *d = field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP;
-#pragma unroll
-      for (int c = 0; c < CP; ++c) {
-        const float total = __fadd_rn(sum[c], comp[c]);
-        d[c] = beta_zero ? total : __fadd_rn(__fmul_rn(beta, d[c]), total);
-      }
+    }
+    __syncthreads();
+    // ordered write-back: every node of the brick is written once (in FP32: the value is
+    // hi * 2^-s1 + lo * 2^-(s1+k); both products are exact scalings)
+    const float to_value = exp2f((float)-s1), lo_value = exp2f((float)(-s1 - kbits));
+    for (int64_t i = threadIdx.x; i < g.bvol * CP; i += blockDim.x) {
+      const int64_t nl = i / CP;
+      const int c = (int)(i - nl * CP);
+      const int lx = (int)(nl % g.b[0]), ly = (int)((nl / g.b[0]) % g.b[1]), lz = (int)(nl / (g.b[0] * g.b[1]));
+      const int64_t x = bx * g.b[0] + lx, y = by * g.b[1] + ly, z = bz * g.b[2] + lz;
+      if (x >= g.n[0] || y >= g.n[1] || z >= g.n[2]) continue;
+      float *d = field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP + c;
+      const int64_t a = (int64_t)c * g.bvol + nl;
+      float v = finite ? fmaf((float)acc_hi[a], to_value, (float)acc_lo[a] * lo_value) : __int_as_float(0x7fc00000);
+      if (c >= g.ncomp) v = 0.0f;
+      *d = beta_zero ? v : __fadd_rn(__fmul_rn(beta, *d), v);
     }
   }
 }
@@ -655,7 +798,7 @@ StagedGeo staged_geo(const gbg_field_s *f, const gbg_bins_s *b, int width) {
   return g;
 }
 
-template <int N2, typename TO>
+template <int N2, int M2, typename TO>
 gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, TO *out, cudaStream_t st) {
   CUtensorMap *map = nullptr;
   GBG_TRY(tensor_map_for(f, N2, b->b, &map));
@@ -672,27 +815,39 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms);
   int32_t *status = nullptr;
+  const int threads = N2 == 4 ? kGatherThreads : kThreads;
   auto go = [&](auto kernel) -> gbg_status {
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<blocks, kThreads, smem, st>>>(*map, g, s, b->cell_start, b->rec, b->perm, out, status, nbuf, tile_bytes,
-                                            box_bytes);
+    kernel<<<blocks, threads, smem, st>>>(*map, g, s, b->cell_start, b->rec, b->perm, out, status, nbuf, tile_bytes,
+                                           box_bytes);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   };
   if constexpr (N2 == 4) {
-    if (f->cp == 4) return go(k_gather_staged4<4, TO>);
-    return go(k_gather_staged4<12, TO>);
+    if (f->cp == 4) return go(k_gather_staged4<M2, 4, TO>);
+    return go(k_gather_staged4<M2, 12, TO>);
   } else {
-    if (f->cp == 4) return go(k_gather_staged_generic<N2, 4, TO>);
-    return go(k_gather_staged_generic<N2, 12, TO>);
+    if (f->cp == 4) return go(k_gather_staged_generic<N2, M2, 4, TO>);
+    return go(k_gather_staged_generic<N2, M2, 12, TO>);
   }
 }
 
-template <int N2>
+// Per-axis weight bound of a scheme: max over nodes of sum_r |c[q, r]| (|t| <= 1).
+double axis_bound(const gbg_scheme &sch) {
+  double best = 0.0;
+  for (int q = 0; q < sch.stencil_width; ++q) {
+    double s = 0.0;
+    for (int r = 0; r < sch.num_powers; ++r) s += std::fabs(sch.coefficients[q + sch.stencil_width * r]);
+    best = s > best ? s : best;
+  }
+  return best;
+}
+
+template <int N2, int M2>
 gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, double beta,
-                                 cudaStream_t st) {
-  PullGeo g;
+                                 const unsigned *qmax_bits, int32_t *status, cudaStream_t st) {
+  FixGeo g;
   for (int d = 0; d < 3; ++d) {
     g.b[d] = b->b[d];
     g.nb[d] = b->nb[d];
@@ -705,22 +860,27 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   g.py = f->py;
   g.halo = f->halo;
   g.cp = f->cp;
+  g.ncomp = f->ncomp;
+  const double L = axis_bound(sch);
+  g.l3 = L * L * L;
   const SchemeT<float, N2> s = make_scheme<float, N2>(sch);
-  const size_t smem = sizeof(uint32_t) * 2 * g.e[0] * g.e[1] * g.e[2];
-  if (smem > 200 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's cell ranges");
+  const size_t smem = 2 * sizeof(int) * (size_t)g.bvol * f->cp +
+                      sizeof(uint32_t) * 2 * (size_t)g.e[0] * g.e[1] * g.e[2];
+  if (smem > 200 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared accumulators");
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * 4);
+  const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * 2);
   auto go = [&](auto kernel) -> gbg_status {
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<blocks, kThreads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, f->data, (float)beta, beta == 0.0, 1);
+    kernel<<<blocks, kThreads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
+                                           beta == 0.0, status);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   };
-  if (f->cp == 4) return go(k_scatter_pull_staged<N2, 4>);
-  return go(k_scatter_pull_staged<N2, 12>);
+  if (f->cp == 4) return go(k_scatter_fixed<N2, M2, 4>);
+  return go(k_scatter_fixed<N2, M2, 12>);
 }
 
 }  // namespace
@@ -840,6 +1000,7 @@ gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32
   a.take<char>(radix_sort_temp_bytes(m));
   a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
   a.take<float>((size_t)m * 12);
+  a.take<unsigned>(64);
   b->bytes = a.used + 256;
   if (cudaMalloc(&b->block, b->bytes) != cudaSuccess) {
     cudaGetLastError();
@@ -857,6 +1018,7 @@ gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32
   b->sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   b->scan_tmp = a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
   b->qs = a.take<float>((size_t)m * 12);
+  b->qmax_bits = a.take<unsigned>(64);
   cudaMemset(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1));
   *out = b;
   return GBG_OK;
@@ -933,10 +1095,16 @@ gbg_status gbg_interpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   auto run = [&](auto *o) -> gbg_status {
     switch (scheme->stencil_width) {
-      case 2: return launch_staged_gather<2>(f, b, *scheme, o, st);
-      case 4: return launch_staged_gather<4>(f, b, *scheme, o, st);
-      case 6: return launch_staged_gather<6>(f, b, *scheme, o, st);
-      default: return launch_staged_gather<8>(f, b, *scheme, o, st);
+      // compile-time (width, powers) for the common schemes, guarded Horner otherwise
+      case 2: return scheme->num_powers == 2 ? launch_staged_gather<2, 2>(f, b, *scheme, o, st)
+                                             : launch_staged_gather<2, 0>(f, b, *scheme, o, st);
+      case 4: return scheme->num_powers == 4 ? launch_staged_gather<4, 4>(f, b, *scheme, o, st)
+                                             : launch_staged_gather<4, 0>(f, b, *scheme, o, st);
+      case 6: return scheme->num_powers == 6 ? launch_staged_gather<6, 6>(f, b, *scheme, o, st)
+                     : scheme->num_powers == 4 ? launch_staged_gather<6, 4>(f, b, *scheme, o, st)
+                                               : launch_staged_gather<6, 0>(f, b, *scheme, o, st);
+      default: return scheme->num_powers == 8 ? launch_staged_gather<8, 8>(f, b, *scheme, o, st)
+                                              : launch_staged_gather<8, 0>(f, b, *scheme, o, st);
     }
   };
   if (out_dtype == GBG_F64) return run(static_cast<double *>(out));
@@ -951,25 +1119,33 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   if (b->npoints > 0 && !q) return set_error(GBG_EARG, "null quantities");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int64_t m = b->npoints;
+  GBG_CUDA_TRY(cudaMemsetAsync(b->qmax_bits, 0, sizeof(unsigned), st));
   if (m > 0) {
     const int blocks = launch_blocks(m, kThreads);
     if (q_dtype == GBG_F64)
       k_scatter_qprep<double><<<blocks, kThreads, 0, st>>>(static_cast<const double *>(q), b->perm, m, f->ncomp, f->cp,
-                                                           (float)alpha, b->qs);
+                                                           (float)alpha, b->qs, b->qmax_bits);
     else
       k_scatter_qprep<float><<<blocks, kThreads, 0, st>>>(static_cast<const float *>(q), b->perm, m, f->ncomp, f->cp,
-                                                          (float)alpha, b->qs);
+                                                          (float)alpha, b->qs, b->qmax_bits);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
   }
-  // With no points the pull still runs: it writes beta * field (beta == 0 clears).
+  // With no points the push still runs: it writes beta * field (beta == 0 clears).
+  const int w = scheme->stencil_width, p = scheme->num_powers;
   gbg_status s;
-  switch (scheme->stencil_width) {
-    case 2: s = launch_staged_scatter<2>(f, b, *scheme, beta, st); break;
-    case 4: s = launch_staged_scatter<4>(f, b, *scheme, beta, st); break;
-    case 6: s = launch_staged_scatter<6>(f, b, *scheme, beta, st); break;
-    default: s = launch_staged_scatter<8>(f, b, *scheme, beta, st); break;
-  }
+  if (w == 2)
+    s = p == 2 ? launch_staged_scatter<2, 2>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+               : launch_staged_scatter<2, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+  else if (w == 4)
+    s = p == 4 ? launch_staged_scatter<4, 4>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+               : launch_staged_scatter<4, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+  else if (w == 6)
+    s = p == 6 ? launch_staged_scatter<6, 6>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+               : launch_staged_scatter<6, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+  else
+    s = p == 8 ? launch_staged_scatter<8, 8>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+               : launch_staged_scatter<8, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   GBG_TRY(s);
   const int64_t total = f->px * f->py * f->pz;
   k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
