@@ -135,5 +135,6 @@ def test_c_abi_checks_before_launch(gbg):
     assert "grid_size" in gbg._lib.last_error()
     nbytes = ctypes.c_size_t()
     assert lib.gbg_anterpolate_workspace_size(grid, 2, 3, 1000, scheme, ctypes.byref(nbytes)) == 0
-    assert nbytes.value > 1000 * (3 * 4 + 3) * 8
+    # keys, sorted keys, permutation, a 32-byte record and 3 quantities per point, at least
+    assert nbytes.value > 1000 * (3 * 4 + 32 + 3 * 8)
     assert lib.gbg_point_traversal_order_workspace_size(grid, 1000, 0, ctypes.byref(nbytes)) == gbg._lib.GBG_EARG
