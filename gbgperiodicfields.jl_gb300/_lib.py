@@ -64,6 +64,38 @@ class SchemeC(ctypes.Structure):
                 ("coefficients", ctypes.c_double * (GBG_MAX_NODES * GBG_MAX_POWERS))]
 
 
+class BatchItemC(ctypes.Structure):
+    _fields_ = [("field", ctypes.c_void_p), ("bins", ctypes.c_void_p), ("scheme", SchemeC),
+                ("out", ctypes.c_void_p), ("dest", ctypes.c_void_p), ("q", ctypes.c_void_p),
+                ("alpha", ctypes.c_double), ("beta", ctypes.c_double)]
+
+
+class ServerConfigC(ctypes.Structure):
+    _fields_ = [("slots", ctypes.c_int32), ("max_batch", ctypes.c_int32), ("brick", ctypes.c_int32 * 3),
+                ("reserved", ctypes.c_int32), ("hbm_budget_bytes", ctypes.c_size_t),
+                ("timeout_seconds", ctypes.c_double)]
+
+
+class RequestC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("pos_dtype", ctypes.c_int32), ("field", ctypes.c_void_p),
+                ("scheme", SchemeC), ("positions", ctypes.c_void_p), ("npoints", ctypes.c_int64),
+                ("out", ctypes.c_void_p), ("q", ctypes.c_void_p), ("alpha", ctypes.c_double),
+                ("beta", ctypes.c_double), ("ready_event", ctypes.c_void_p)]
+
+
+class ServerCountersC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int64) for n in ("submitted", "completed", "failed", "queued", "in_flight", "runs",
+                                               "points")] + \
+               [(n, ctypes.c_double) for n in ("p50_ms", "p99_ms", "mean_ms", "max_ms", "first_submit_s",
+                                                "last_done_s")] + \
+               [(n, ctypes.c_size_t) for n in ("hbm_in_use", "hbm_peak", "hbm_budget")]
+
+
+GBG_REQ_INTERPOLATE = 1
+GBG_REQ_ANTERPOLATE = 2
+GBG_FAULT_ALLOC = 1
+GBG_FAULT_DEADLINE = 2
+
 _lib = None
 
 _P = ctypes.c_void_p
@@ -104,6 +136,18 @@ SIGNATURES = {
     "gbg_bins_order": (_I32, [_P, _P, _P]),
     "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P]),
     "gbg_anterpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _D, _D, _P]),
+    "gbg_batch_create": (_I32, [ctypes.POINTER(BatchItemC), _I32, ctypes.POINTER(_P)]),
+    "gbg_batch_run": (_I32, [_P, _P, _P]),
+    "gbg_batch_destroy": (_I32, [_P]),
+    "gbg_server_create": (_I32, [ctypes.POINTER(ServerConfigC), ctypes.POINTER(_P)]),
+    "gbg_server_submit": (_I32, [_P, ctypes.POINTER(RequestC), ctypes.POINTER(_I64)]),
+    "gbg_server_wait": (_I32, [_P, _I64, _D, ctypes.POINTER(_I32)]),
+    "gbg_server_drain": (_I32, [_P, _D]),
+    "gbg_server_stats": (_I32, [_P, _I32, ctypes.POINTER(ServerCountersC)]),
+    "gbg_server_inject": (_I32, [_P, _I32, _I32]),
+    "gbg_server_destroy": (_I32, [_P]),
+    "gbg_server_plan": (_I32, [ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_SZ), _I32,
+                               _SZ, _I32, ctypes.POINTER(_I32)]),
 }
 
 

@@ -136,6 +136,48 @@ __device__ __forceinline__ void stage_coeffs(const SchemeT<T, NMAX> &s, T *c) {
   __syncthreads();
 }
 
+// Block-wide exclusive scan of n counts in shared memory (n <= 32 * blockDim.x * 8);
+// returns the total.  Every thread must call it.
+__device__ __forceinline__ uint32_t block_scan_counts(uint32_t *v, int n, uint32_t *warp_tot) {
+  const int per = (n + blockDim.x - 1) / blockDim.x;
+  const int lo = threadIdx.x * per, hi = min(n, lo + per);
+  uint32_t run = 0;
+  for (int i = lo; i < hi; ++i) run += v[i];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t t = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < (int)(blockDim.x >> 5)) warp_tot[lane] = t;
+  }
+  __syncthreads();
+  uint32_t prefix = (warp ? warp_tot[warp - 1] : 0u) + x - run;
+  const uint32_t total = warp_tot[(blockDim.x >> 5) - 1];
+  for (int i = lo; i < hi; ++i) {
+    const uint32_t c = v[i];
+    v[i] = prefix;
+    prefix += c;
+  }
+  __syncthreads();
+  return total;
+}
+
+// Bound of |w_q(t)| over the nodes q and t in [0, 1] (Bernstein form), plus horner_slack
+// times sum_r |c[q, r]| for the rounding of the weight evaluation.  Used to size the
+// fixed-point scales of the deterministic scatters.
+double weight_bound(const gbg_scheme &sch, double horner_slack);
+
 // ----------------------------------------------------------- workspace
 
 // Carves aligned sub-buffers out of one workspace; with base == nullptr it only sizes.
@@ -177,5 +219,23 @@ gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, ui
 
 // Grid-stride launch shape: a multiple of the SM count.
 int launch_blocks(int64_t work, int threads, int per_sm = 8);
+
+// Bins whose device memory is taken and returned in stream order (cudaMallocAsync /
+// cudaFreeAsync on `stream`), for the serving loop: no call here synchronizes the device.
+gbg_status bins_create_async(const gbg_grid &grid, int64_t max_points, const int32_t *brick,
+                             cudaStream_t stream, gbg_bins *out, size_t *bytes);
+gbg_status bins_destroy_async(gbg_bins bins, cudaStream_t stream);
+size_t bins_bytes(const gbg_grid &grid, int64_t max_points, const int32_t *brick);
+
+// The grid, component count and widest stencil of a resident field.
+gbg_status field_info(gbg_field f, gbg_grid *grid, int32_t *ncomp, int32_t *max_width);
+
+// Batches whose device tables are allocated in stream order and uploaded from the
+// caller's pinned staging memory (at least batch_table_bytes(count) bytes, left untouched
+// until the copy has run).
+size_t batch_table_bytes(int32_t count);
+gbg_status batch_create_async(const gbg_batch_item *items, int32_t count, cudaStream_t stream, void *pinned,
+                              size_t pinned_bytes, gbg_batch *out);
+gbg_status batch_destroy_async(gbg_batch bt, cudaStream_t stream);
 
 }  // namespace gbg

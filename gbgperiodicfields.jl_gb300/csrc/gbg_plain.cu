@@ -8,10 +8,10 @@
 // The gather is one thread per work item, as in the reference, with the stencil weight
 // of each node formed once and applied to every component of the chunk.  The scatter is
 // not the reference's atomic push: points are sorted by brick and cell with a stable
-// device radix sort, and each brick's nodes are accumulated in shared memory by colour
-// classes of cells with disjoint stencils (or, for a stencil wider than the grid, every
-// node pulls its contributions).  No float atomics are used, so the scatter is bitwise
-// reproducible and independent of any traversal order.
+// device radix sort, and each brick's nodes are accumulated in shared memory as int64
+// fixed-point sums (or, for a stencil wider than the grid, every node pulls its
+// contributions).  No float atomics are used, so the scatter is bitwise reproducible and
+// independent of any traversal order.
 #include <mutex>
 #include <string>
 
@@ -310,17 +310,13 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// ------------------------------------------------------ colored scatter
+// ------------------------------------------------------ brick scatter
 //
 // The default scatter.  Points are sorted by brick and by cell within the brick (a stable
 // radix sort, so the order is fixed).  A CTA owns one brick of nodes and accumulates, in
-// shared memory and in the transfer's own precision, every contribution of the points in
-// the cells whose stencils reach the brick (the extended region).  Two cells whose
-// extended-region coordinates agree modulo N2 on every axis have disjoint stencils, so the
-// cells are processed in N2^3 colour classes, one class at a time: within a class each
-// node is written by at most one thread, with no atomics, and every node receives its
-// contributions in a fixed order (class, then cell, then the sorted points of the cell).
-// The result is deterministic and each node is written to HBM once.
+// shared memory, every contribution of the points in the cells whose stencils reach the
+// brick (the extended region) as an integer, so the sum does not depend on the order
+// in which threads add.  Each node is written to HBM once.
 
 struct BrickGeo {
   int32_t b[3];
@@ -362,8 +358,9 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_brick_prep(GridT<T> g, BrickGeo bg, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
                  int64_t m, const uint32_t *__restrict__ perm, T alpha, RecT<T> *__restrict__ rec,
-                 T *__restrict__ qs) {
+                 T *__restrict__ qs, unsigned long long *__restrict__ qmax_bits) {
   const int64_t n[3] = {g.nx, g.ny, g.nz};
+  unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[sl];
@@ -378,8 +375,19 @@ __global__ void __launch_bounds__(kThreads)
     for (int d = 0; d < 3; ++d) r.t[d] = ok ? t[d] : quiet_nan<T>();
     r.loc = (uint32_t)local;
     rec[sl] = r;
-    for (int c = 0; c < ncomp; ++c) qs[sl * ncomp + c] = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
+    for (int c = 0; c < ncomp; ++c) {
+      const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
+      qs[sl * ncomp + c] = v;
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs((double)v));
+      mx = bits > mx ? bits : mx;
+    }
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = other > mx ? other : mx;
+  }
+  if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
 template <int N, typename T>
@@ -391,51 +399,112 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
   return v;
 }
 
-// FIXED: the scheme has M2 == N2 powers (CatmullRom, the default LalescuSpline of each
-// width, LagrangeSpline): Horner with constant indices; otherwise the coefficients are
-// staged in shared memory and Horner runs over the scheme's own powers.
+// The default scatter (deterministic, FP64-grade).  A CTA owns one brick of nodes.  It
+// lists the points of every cell whose stencil reaches the brick (the extended region),
+// gives each thread a point, and adds every contribution w*alpha*q, scaled by a power of
+// two S and rounded once to an integer with the FP64 "magic number" 1.5*2^52 (one FMA),
+// to an int64 accumulator in shared memory.  Integer addition is associative, so the
+// result does not depend on which thread adds first, and no float atomics are used.  S is
+// chosen per brick from max|alpha q| (over all points) * l3 (bound on |w1 w2 w3|, from
+// the Bernstein form of the weights: 1 for the spline schemes) and the region's point
+// count so that no sum can overflow and every contribution is kept to 2^-50 of that bound.
+constexpr int kFlatChunk = 2048;
+
 template <typename T, int N2, bool FIXED>
 __global__ void __launch_bounds__(kThreads)
-    k_scatter_colored(GridT<T> g, BrickGeo bg, SchemeT<T, N2> s, int ncomp,
+    k_scatter_fixed64(GridT<T> g, BrickGeo bg, SchemeT<T, N2> s, int ncomp,
                       const uint32_t *__restrict__ cell_start, const RecT<T> *__restrict__ rec,
-                      const T *__restrict__ qs, T *__restrict__ field, T beta, int beta_zero) {
+                      const T *__restrict__ qs, const unsigned long long *__restrict__ qmax_bits, double l3,
+                      T *__restrict__ field, T beta, int beta_zero, int32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *acc = reinterpret_cast<T *>(smem_raw);  // bvol * ncomp, node-major
-  uint32_t *ranges = reinterpret_cast<uint32_t *>(acc + bg.bvol * ncomp);
-  __shared__ T cs[N2 * GBG_MAX_POWERS];
-  if (!FIXED) stage_coeffs(s, cs);
-  constexpr int nbw = (N2 - 2) / 2;
+  constexpr int half = N2 / 2;
   const int E0 = bg.b[0] + N2 - 1, E1 = bg.b[1] + N2 - 1, E2 = bg.b[2] + N2 - 1;
   const int ecount = E0 * E1 * E2;
+  const int bvol = (int)bg.bvol;
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw);  // ncomp * bvol, comp-major
+  uint32_t *off = reinterpret_cast<uint32_t *>(acc + (size_t)bvol * ncomp);  // ecount: exclusive prefix
+  uint32_t *r0s = off + ecount;                                              // ecount: first slot
+  uint32_t *pslot = r0s + ecount;                                            // kFlatChunk: point slot
+  uint32_t *pxyz = pslot + kFlatChunk;                                       // kFlatChunk: packed cell
+  uint32_t *kx = pxyz + kFlatChunk, *ky = kx + E0, *kz = ky + E1;             // per-axis key tables
+  __shared__ uint32_t warp_tot[32];
+  __shared__ T cs[N2 * GBG_MAX_POWERS];
+  if (!FIXED) stage_coeffs(s, cs);
+  const double qmax = __longlong_as_double((long long)*qmax_bits);
   const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
-  const int64_t n[3] = {g.nx, g.ny, g.nz};
+  const int n[3] = {(int)g.nx, (int)g.ny, (int)g.nz};
+  const int nb0 = (int)bg.nb[0], nb1 = (int)bg.nb[1];
+  // each thread's first region cell and node, and its stride, as coordinates
+  const int ex0 = (int)threadIdx.x % E0, ey0 = ((int)threadIdx.x / E0) % E1, ez0 = (int)threadIdx.x / (E0 * E1);
+  const int esx = (int)blockDim.x % E0, esy = ((int)blockDim.x / E0) % E1, esz = (int)blockDim.x / (E0 * E1);
+  const int B0 = bg.b[0], B1 = bg.b[1];
+  const int lx0 = (int)threadIdx.x % B0, ly0 = ((int)threadIdx.x / B0) % B1, lz0 = (int)threadIdx.x / (B0 * B1);
+  const int lsx = (int)blockDim.x % B0, lsy = ((int)blockDim.x / B0) % B1, lsz = (int)blockDim.x / (B0 * B1);
   for (int64_t brick = blockIdx.x; brick < nbricks; brick += gridDim.x) {
-    const int64_t bc[3] = {brick % bg.nb[0], (brick / bg.nb[0]) % bg.nb[1], brick / (bg.nb[0] * bg.nb[1])};
+    const int bc[3] = {(int)(brick % nb0), (int)((brick / nb0) % nb1), (int)(brick / ((int64_t)nb0 * nb1))};
+    const int vx = min(B0, n[0] - bc[0] * B0), vy = min(B1, n[1] - bc[1] * B1), vz = min(bg.b[2], n[2] - bc[2] * bg.b[2]);
     __syncthreads();
-    for (int64_t i = threadIdx.x; i < bg.bvol * ncomp; i += blockDim.x) acc[i] = T(0);
-    for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
-      const int ee[3] = {e % E0, (e / E0) % E1, e / (E0 * E1)};
-      int64_t kb = 0, kl = 0;
-#pragma unroll
-      for (int d = 2; d >= 0; --d) {
-        const int64_t c = imod(bc[d] * bg.b[d] - nbw - 1 + ee[d], n[d]);
-        kb = kb * bg.nb[d] + c / bg.b[d];
-        kl = kl * bg.b[d] + c % bg.b[d];
-      }
-      const int64_t key = kb * bg.bvol + kl;
-      ranges[2 * e] = __ldg(cell_start + key);
-      ranges[2 * e + 1] = __ldg(cell_start + key + 1);
+    for (int i = threadIdx.x; i < bvol * ncomp; i += blockDim.x) acc[i] = 0ull;
+    for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
+      const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
+      const int e = t - (d == 0 ? 0 : (d == 1 ? E0 : E0 + E1));
+      int c = (bc[d] * bg.b[d] - half + e) % n[d];
+      if (c < 0) c += n[d];
+      const uint32_t cb = (uint32_t)c / (uint32_t)bg.b[d], cl = (uint32_t)c - cb * (uint32_t)bg.b[d];
+      if (d == 0) kx[e] = cb * (uint32_t)bvol + cl;
+      else if (d == 1) ky[e] = cb * (uint32_t)nb0 * (uint32_t)bvol + cl * (uint32_t)B0;
+      else kz[e] = cb * (uint32_t)nb1 * (uint32_t)nb0 * (uint32_t)bvol + cl * (uint32_t)(B0 * B1);
     }
     __syncthreads();
-#pragma unroll 1
-    for (int cls = 0; cls < N2 * N2 * N2; ++cls) {
-      const int a0 = cls % N2, a1 = (cls / N2) % N2, a2 = cls / (N2 * N2);
-      const int nu = (E0 - a0 + N2 - 1) / N2, nv = (E1 - a1 + N2 - 1) / N2, nw = (E2 - a2 + N2 - 1) / N2;
-      for (int idx = threadIdx.x; idx < nu * nv * nw; idx += blockDim.x) {
-        const int ex = a0 + N2 * (idx % nu), ey = a1 + N2 * ((idx / nu) % nv), ez = a2 + N2 * (idx / (nu * nv));
-        const int e = (ez * E1 + ey) * E0 + ex;
-        const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
-        for (uint32_t sl = r0; sl < r1; ++sl) {
+    {
+      int ex = ex0, ey = ey0, ez = ez0;
+      for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+        const uint32_t key = kx[ex] + ky[ey] + kz[ez];
+        const uint32_t r0 = __ldg(cell_start + key);
+        r0s[e] = r0;
+        off[e] = __ldg(cell_start + key + 1) - r0;
+        ex += esx;
+        ey += esy;
+        ez += esz;
+        if (ex >= E0) { ex -= E0; ++ey; }
+        if (ey >= E1) { ey -= E1; ++ez; }
+      }
+    }
+    __syncthreads();
+    const uint32_t count = block_scan_counts(off, ecount, warp_tot);
+    const double one = qmax * l3, bound = one * (double)count;
+    const bool finite = isfinite(bound);
+    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
+    int e1 = 0, es = 0;
+    frexp(one, &e1);
+    frexp(bound, &es);
+    const int s1 = max(-1000, min(1000, min(50 - e1, 61 - es)));
+    const double S = ldexp(1.0, s1);
+    const double magic = 6755399441055744.0;  // 1.5 * 2^52
+    if (finite && count > 0 && one > 0.0) {
+      for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk) {
+        const uint32_t c1 = min(count, c0 + kFlatChunk);
+        {
+          int ex = ex0, ey = ey0, ez = ez0;
+          for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+            const uint32_t lo = max(off[e], c0), hi = min(e + 1 < ecount ? off[e + 1] : count, c1);
+            const uint32_t base = r0s[e] - off[e];
+            const uint32_t packed = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16);
+            for (uint32_t t = lo; t < hi; ++t) {
+              pslot[t - c0] = base + t;
+              pxyz[t - c0] = packed;
+            }
+            ex += esx;
+            ey += esy;
+            ez += esz;
+            if (ex >= E0) { ex -= E0; ++ey; }
+            if (ey >= E1) { ey -= E1; ++ez; }
+          }
+        }
+        __syncthreads();
+        for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+          const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+          const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
           const RecT<T> r = rec[sl];
           T w1[N2], w2[N2], w3[N2];
           if constexpr (FIXED) {
@@ -448,41 +517,53 @@ __global__ void __launch_bounds__(kThreads)
             axis_weights_dyn(cs, N2, s.m2, r.t[2], w3);
           }
           const T *qv = qs + (int64_t)sl * ncomp;
+          const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
+          const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
+          const int lxb = ex - (N2 - 1);
 #pragma unroll 1
-          for (int k = 0; k < N2; ++k) {
+          for (int k = kz0; k < kz1; ++k) {
             const int lz = ez + k - (N2 - 1);
-            if (lz < 0 || lz >= bg.b[2] || bc[2] * bg.b[2] + lz >= g.nz) continue;
-            const T w3k = pick_t(w3, k);
+            const double wz = (double)pick_t(w3, k) * S;
 #pragma unroll 1
-            for (int j = 0; j < N2; ++j) {
+            for (int j = ky0; j < ky1; ++j) {
               const int ly = ey + j - (N2 - 1);
-              if (ly < 0 || ly >= bg.b[1] || bc[1] * bg.b[1] + ly >= g.ny) continue;
-              const T wyz = mul_rn(pick_t(w2, j), w3k);
-              T *arow = acc + ((lz * bg.b[1] + ly) * bg.b[0]) * ncomp;
+              const double wyz = (double)pick_t(w2, j) * wz;
+              const int row = (lz * B1 + ly) * B0;
 #pragma unroll
               for (int i = 0; i < N2; ++i) {
-                const int lx = ex + i - (N2 - 1);
-                if (lx < 0 || lx >= bg.b[0] || bc[0] * bg.b[0] + lx >= g.nx) continue;
-                const T w = mul_rn(wyz, w1[i]);
-                T *an = arow + lx * ncomp;
-                for (int c = 0; c < ncomp; ++c) an[c] = fma_rn(w, __ldg(qv + c), an[c]);
+                const int lx = lxb + i;
+                if (lx < 0 || lx >= vx) continue;
+                const double w = (double)w1[i] * wyz;
+                for (int c = 0; c < ncomp; ++c) {
+                  const double h = fma(w, (double)__ldg(qv + c), magic);
+                  atomicAdd(acc + c * bvol + row + lx,
+                            (unsigned long long)(__double_as_longlong(h) - __double_as_longlong(magic)));
+                }
               }
             }
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
     }
+    __syncthreads();
     // write-back in the reference layout: node fastest, so a warp writes a contiguous row
-    for (int64_t i = threadIdx.x; i < bg.bvol * ncomp; i += blockDim.x) {
-      const int c = (int)(i / bg.bvol);
-      const int64_t nl = i - (int64_t)c * bg.bvol;
-      const int lx = (int)(nl % bg.b[0]), ly = (int)((nl / bg.b[0]) % bg.b[1]), lz = (int)(nl / (bg.b[0] * bg.b[1]));
-      const int64_t x = bc[0] * bg.b[0] + lx, y = bc[1] * bg.b[1] + ly, z = bc[2] * bg.b[2] + lz;
-      if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
-      T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-      const T v = acc[nl * ncomp + c];
-      *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
+    const double to_value = ldexp(1.0, -s1);
+    for (int c = 0; c < ncomp; ++c) {
+      int lx = lx0, ly = ly0, lz = lz0;
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+        if (lx < vx && ly < vy && lz < vz) {
+          const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
+          T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
+          const T v = finite ? (T)((double)(long long)acc[c * bvol + nl] * to_value) : quiet_nan<T>();
+          *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
+        }
+        lx += lsx;
+        ly += lsy;
+        lz += lsz;
+        if (lx >= B0) { lx -= B0; ++ly; }
+        if (ly >= B1) { ly -= B1; ++lz; }
+      }
     }
   }
 }
@@ -595,11 +676,11 @@ gbg_status dispatch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncom
   }
 }
 
-// Which scatter runs, and its bricks: the coloured push whenever every axis is at least
-// a stencil wide and a brick's accumulators fit in shared memory, else the node pull
+// Which scatter runs, and its bricks: the brick push whenever every axis is at least a
+// stencil wide and a brick's accumulators fit in shared memory, else the node pull
 // (which also handles a stencil wider than the grid, reached several times per node).
 struct ScatterPlan {
-  bool colored = false;
+  bool bricked = false;
   BrickGeo bg{};
   int64_t nkeys = 0;
   size_t smem = 0;
@@ -614,13 +695,17 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
     p.bg.b[d] = (int32_t)std::min<int64_t>(base[d], g.n[d]);
     p.bg.nb[d] = (g.n[d] + p.bg.b[d] - 1) / p.bg.b[d];
     nbricks *= p.bg.nb[d];
-    if (g.n[d] < n2) wide_enough = false;
+    if (g.n[d] < n2 || g.n[d] >= (int64_t(1) << 31)) wide_enough = false;
   }
   p.bg.bvol = (int64_t)p.bg.b[0] * p.bg.b[1] * p.bg.b[2];
-  p.smem = (size_t)p.bg.bvol * ncomp * esize +
-           sizeof(uint32_t) * 2 * (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
-  p.colored = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;
-  p.nkeys = p.colored ? nbricks * p.bg.bvol : g.n[0] * g.n[1] * g.n[2];
+  const size_t ecount = (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
+  p.smem = (size_t)p.bg.bvol * ncomp * sizeof(unsigned long long) + 2 * sizeof(uint32_t) * ecount +
+           2 * sizeof(uint32_t) * kFlatChunk +
+           sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1));
+  (void)esize;
+  if (ecount > 65535) wide_enough = false;
+  p.bricked = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;
+  p.nkeys = p.bricked ? nbricks * p.bg.bvol : g.n[0] * g.n[1] * g.n[2];
   return p;
 }
 
@@ -629,6 +714,7 @@ struct ScatterLayout {
   void *sort_tmp;
   uint32_t *scan_tmp;
   void *rec, *qs;
+  unsigned long long *qmax_bits;
 };
 
 ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncomp, int n2, size_t esize) {
@@ -639,9 +725,10 @@ ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncom
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  const size_t rec_bytes = P.colored ? (esize == 8 ? sizeof(RecT<double>) : sizeof(RecT<float>)) : 3 * n2 * esize;
+  const size_t rec_bytes = P.bricked ? (esize == 8 ? sizeof(RecT<double>) : sizeof(RecT<float>)) : 3 * n2 * esize;
   L.rec = a.take<char>((size_t)m * rec_bytes);
   L.qs = a.take<char>((size_t)m * ncomp * esize);
+  L.qmax_bits = a.take<unsigned long long>(4);
   return L;
 }
 
@@ -652,10 +739,10 @@ int bits_for(uint64_t max_value) {
 }
 
 template <typename T, int N2, bool FIXED>
-gbg_status launch_colored(const GridT<T> &g, const ScatterPlan &P, const gbg_scheme &sch, int ncomp,
-                          const ScatterLayout &L, T *field, double beta, cudaStream_t st) {
+gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_scheme &sch, int ncomp,
+                          const ScatterLayout &L, T *field, double beta, int32_t *status, cudaStream_t st) {
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
-  auto kernel = k_scatter_colored<T, N2, FIXED>;
+  auto kernel = k_scatter_fixed64<T, N2, FIXED>;
   GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
   const int64_t nbricks = P.bg.nb[0] * P.bg.nb[1] * P.bg.nb[2];
   int dev = 0, sms = 1, per_sm = 1;
@@ -663,8 +750,10 @@ gbg_status launch_colored(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, P.smem);
   const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
+  const double L3 = std::pow(weight_bound(sch, std::ldexp(1.0, -40)), 3);
   kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, s, ncomp, L.counts, static_cast<const RecT<T> *>(L.rec),
-                                           static_cast<const T *>(L.qs), field, T(beta), beta == 0.0);
+                                           static_cast<const T *>(L.qs), L.qmax_bits, L3, field, T(beta),
+                                           beta == 0.0, status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
@@ -678,27 +767,28 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   const T *x = static_cast<const T *>(pos);
   T *f = static_cast<T *>(field);
   GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(P.nkeys + 1), st));
-  if (P.colored) {
+  if (P.bricked) {
     k_brick_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, status);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
     GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
+    GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
     k_brick_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, ncomp, x, static_cast<const T *>(q), m,
                                                                      L.perm, T(alpha), static_cast<RecT<T> *>(L.rec),
-                                                                     static_cast<T *>(L.qs));
+                                                                     static_cast<T *>(L.qs), L.qmax_bits);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     const int w = sch.stencil_width;
     const bool fixed = sch.num_powers == w;
-    if (w == 2) return fixed ? launch_colored<T, 2, true>(g, P, sch, ncomp, L, f, beta, st)
-                             : launch_colored<T, 2, false>(g, P, sch, ncomp, L, f, beta, st);
-    if (w == 4) return fixed ? launch_colored<T, 4, true>(g, P, sch, ncomp, L, f, beta, st)
-                             : launch_colored<T, 4, false>(g, P, sch, ncomp, L, f, beta, st);
-    if (w == 6) return fixed ? launch_colored<T, 6, true>(g, P, sch, ncomp, L, f, beta, st)
-                             : launch_colored<T, 6, false>(g, P, sch, ncomp, L, f, beta, st);
-    return fixed ? launch_colored<T, 8, true>(g, P, sch, ncomp, L, f, beta, st)
-                 : launch_colored<T, 8, false>(g, P, sch, ncomp, L, f, beta, st);
+    if (w == 2) return fixed ? launch_bricked<T, 2, true>(g, P, sch, ncomp, L, f, beta, status, st)
+                             : launch_bricked<T, 2, false>(g, P, sch, ncomp, L, f, beta, status, st);
+    if (w == 4) return fixed ? launch_bricked<T, 4, true>(g, P, sch, ncomp, L, f, beta, status, st)
+                             : launch_bricked<T, 4, false>(g, P, sch, ncomp, L, f, beta, status, st);
+    if (w == 6) return fixed ? launch_bricked<T, 6, true>(g, P, sch, ncomp, L, f, beta, status, st)
+                             : launch_bricked<T, 6, false>(g, P, sch, ncomp, L, f, beta, status, st);
+    return fixed ? launch_bricked<T, 8, true>(g, P, sch, ncomp, L, f, beta, status, st)
+                 : launch_bricked<T, 8, false>(g, P, sch, ncomp, L, f, beta, status, st);
   }
   const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
   const int64_t ncells = g.npf;

@@ -26,7 +26,11 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
+#include <cstring>
 #include <string>
+#include <type_traits>
+#include <vector>
 
 #include "gbg_common.cuh"
 
@@ -57,7 +61,25 @@ struct gbg_bins_s {
   unsigned *qmax_bits = nullptr;  // largest |alpha q| of the last scatter, as float bits
   void *block = nullptr;
   size_t bytes = 0;
+  bool async = false;  // block from cudaMallocAsync (serving loop)
 };
+
+namespace gbg {
+// The arrays of a bins' device block, in order; with a.base == nullptr this only sizes.
+inline void bins_layout(Arena &a, gbg_bins_s *b) {
+  const int64_t m = b->max_points > 0 ? b->max_points : 1;
+  b->keys = a.take<uint32_t>(m);
+  b->skeys = a.take<uint32_t>(m);
+  b->perm = a.take<uint32_t>(m);
+  b->cell_start = a.take<uint32_t>((size_t)b->nkeys + 1);
+  b->rec_user = a.take<float4>(m);
+  b->rec = a.take<float4>(m);
+  b->sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
+  b->scan_tmp = a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
+  b->qs = a.take<float>((size_t)m * 12);
+  b->qmax_bits = a.take<unsigned>(64);
+}
+}  // namespace gbg
 
 namespace gbg {
 namespace {
@@ -387,7 +409,8 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
     if (nbuf == 2 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
-      if (!mbar_wait(bars + buf, phase[buf])) {
+      // every thread must take the same exit, so the outcome of the bounded wait is voted
+      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
         failed = true;
         if (threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_TIMEOUT);
         break;
@@ -500,7 +523,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
     if (nbuf == 2 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
-      if (!mbar_wait(bars + buf, phase[buf])) {
+      // every thread must take the same exit, so the outcome of the bounded wait is voted
+      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
         failed = true;
         if (threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_TIMEOUT);
         break;
@@ -586,13 +610,14 @@ __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__rest
 
 struct FixGeo {
   int32_t b[3];
-  int64_t nb[3];
-  int64_t n[3];
+  int32_t nb[3];
+  int32_t n[3];
   int32_t e[3];  // extended cell region = brick + width - 1
   int64_t nbricks, bvol;
   int64_t px, py;
   int32_t halo, cp, ncomp;
-  double l3;  // bound on |w1*w2*w3|: (max_q sum_r |c[q,r]|)^3
+  int32_t neighbour_skip;  // every brick edge >= width/2: the region lies in the 27 neighbouring bricks
+  double l3;  // bound on |w1*w2*w3| (the cube of the scheme's Bernstein weight bound)
 };
 
 // Deterministic scatter.  A CTA owns a brick's nodes; it walks the points of every cell
@@ -620,147 +645,254 @@ __device__ __forceinline__ void add_fixed(int *hi_acc, int *lo_acc, int idx, flo
   atomicAdd(lo_acc + idx, __float_as_int(l) - kMagicBits);
 }
 
-template <int N2, int M2, int CP>
+// All N2 weights from coefficients in memory ([q + N2*p], M2 == N2 powers).
+template <int N2>
+__device__ __forceinline__ void weights_ptr(const float *c, float t, float (&w)[N2]) {
+#pragma unroll
+  for (int q = 0; q < N2; ++q) w[q] = c[q + N2 * (N2 - 1)];
+#pragma unroll
+  for (int p = N2 - 2; p >= 0; --p)
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = fmaf(w[q], t, c[q + N2 * p]);
+}
+
+// The same for any number of powers m2.
+template <int N2>
+__device__ __forceinline__ void weights_rt(const float *c, int m2, float t, float (&w)[N2]) {
+#pragma unroll
+  for (int q = 0; q < N2; ++q) w[q] = c[q + N2 * (m2 - 1)];
+#pragma unroll 1
+  for (int p = m2 - 2; p >= 0; --p)
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = fmaf(w[q], t, c[q + N2 * p]);
+}
+
+constexpr int kFlatChunk32 = 2048;
+
+// Shared memory of one scatter CTA: two int32 accumulators per node and component, the
+// exclusive prefix of the extended region's per-cell counts and their first slots, one
+// chunk of the region's points (slot and packed cell coordinates), and the per-axis key
+// tables of the region's cells.
+size_t scatter32_smem(const FixGeo &g, int cp) {
+  const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
+  return 2 * sizeof(int) * (size_t)g.bvol * cp + 2 * sizeof(uint32_t) * ecount + 2 * sizeof(uint32_t) * kFlatChunk32 +
+         sizeof(uint32_t) * (size_t)(g.e[0] + g.e[1] + g.e[2]);
+}
+
+// The scatter of one brick: list the region's points, give each thread a point, and add
+// its contributions to the brick's fixed-point accumulators; then write every node once.
+// All index arithmetic is 32-bit and division-free inside the loops: the region's cell
+// keys come from three per-axis tables (key = kx[ex] + ky[ey] + kz[ez]) and each thread
+// steps its (ex, ey, ez) incrementally.
+template <int N2, bool FIXED, int CP>
+__device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int64_t b,
+                                const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
+                                const float *__restrict__ qs, float qmax, float *__restrict__ field, float beta,
+                                int beta_zero, unsigned char *smem, uint32_t *warp_tot, int32_t *status) {
+  const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
+  const int ecount = E0 * E1 * E2;
+  const int bvol = (int)g.bvol;
+  int *acc_hi = reinterpret_cast<int *>(smem);
+  int *acc_lo = acc_hi + bvol * CP;
+  uint32_t *off = reinterpret_cast<uint32_t *>(acc_lo + bvol * CP);
+  uint32_t *r0s = off + ecount;
+  uint32_t *pslot = r0s + ecount;
+  uint32_t *pxyz = pslot + kFlatChunk32;
+  uint32_t *kx = pxyz + kFlatChunk32, *ky = kx + E0, *kz = ky + E1;
+  constexpr int half = N2 / 2;
+  const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]), bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
+  // nodes of this brick inside the grid
+  const int vx = min(g.b[0], g.n[0] - bx * g.b[0]), vy = min(g.b[1], g.n[1] - by * g.b[1]),
+            vz = min(g.b[2], g.n[2] - bz * g.b[2]);
+  // is any point near?  (the 27 neighbouring bricks hold the whole region)
+  bool any = true;
+  if (g.neighbour_skip) {
+    bool mine = false;
+    if (threadIdx.x < 27) {
+      const int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
+      const uint32_t nx = (uint32_t)((bx + dx + g.nb[0]) % g.nb[0]), ny = (uint32_t)((by + dy + g.nb[1]) % g.nb[1]),
+                     nz = (uint32_t)((bz + dz + g.nb[2]) % g.nb[2]);
+      const uint64_t k = ((uint64_t)nz * (uint32_t)g.nb[1] + ny) * (uint32_t)g.nb[0] + nx;
+      mine = __ldg(cell_start + (k + 1) * (uint64_t)bvol) != __ldg(cell_start + k * (uint64_t)bvol);
+    }
+    any = __syncthreads_or(mine);
+  }
+  if (!any && !beta_zero && beta == 1.0f) return;  // the brick keeps its values
+  uint32_t count = 0;
+  int s1 = 0, kbits = 0;
+  bool finite = true;
+  if (any) {
+    for (int i = threadIdx.x; i < 2 * bvol * CP; i += blockDim.x) acc_hi[i] = 0;
+    // per-axis key tables of the region's cells (periodic wrap, then brick and local index)
+    for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
+      const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
+      const int e = t - (d == 0 ? 0 : (d == 1 ? E0 : E0 + E1));
+      const int bc = d == 0 ? bx : (d == 1 ? by : bz);
+      int c = (bc * g.b[d] - half + e) % g.n[d];
+      if (c < 0) c += g.n[d];
+      const uint32_t cb = (uint32_t)c / (uint32_t)g.b[d], cl = (uint32_t)c - cb * (uint32_t)g.b[d];
+      if (d == 0) kx[e] = cb * (uint32_t)bvol + cl;
+      else if (d == 1) ky[e] = (cb * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)g.b[0];
+      else kz[e] = (cb * (uint32_t)g.nb[1] * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)(g.b[0] * g.b[1]);
+    }
+    __syncthreads();
+    {
+      int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
+      const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
+      for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+        const uint32_t key = kx[ex] + ky[ey] + kz[ez];
+        const uint32_t r0 = __ldg(cell_start + key);
+        r0s[e] = r0;
+        off[e] = __ldg(cell_start + key + 1) - r0;
+        ex += sx;
+        ey += sy;
+        ez += sz;
+        if (ex >= E0) { ex -= E0; ++ey; }
+        if (ey >= E1) { ey -= E1; ++ez; }
+      }
+    }
+    __syncthreads();
+    count = block_scan_counts(off, ecount, warp_tot);
+    const double one = (double)qmax * g.l3, bound = one * (double)count;
+    finite = isfinite(bound);
+    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
+    int e1 = 0, es = 0;
+    frexp(one, &e1);
+    frexp(bound, &es);
+    s1 = max(-120, min(120, min(20 - e1, 29 - es)));
+    kbits = min(21, 30 - (32 - __clz((int)max(count, 1u))));
+    const float S1 = exp2f((float)s1), LS = exp2f((float)kbits);
+    if (finite && count > 0 && one > 0.0) {
+      for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk32) {
+        const uint32_t c1 = min(count, c0 + kFlatChunk32);
+        {
+          int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
+          const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
+          for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+            const uint32_t lo = max(off[e], c0), hi = min(e + 1 < ecount ? off[e + 1] : count, c1);
+            const uint32_t base = r0s[e] - off[e];
+            const uint32_t packed = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16);
+            for (uint32_t t = lo; t < hi; ++t) {
+              pslot[t - c0] = base + t;
+              pxyz[t - c0] = packed;
+            }
+            ex += sx;
+            ey += sy;
+            ez += sz;
+            if (ex >= E0) { ex -= E0; ++ey; }
+            if (ey >= E1) { ey -= E1; ++ez; }
+          }
+        }
+        __syncthreads();
+        for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+          const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+          const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
+          const float4 r = __ldg(rec + sl);
+          float wx[N2], wy[N2], wz[N2];
+          if constexpr (FIXED) {
+            weights_ptr<N2>(coef, r.x, wx);
+            weights_ptr<N2>(coef, r.y, wy);
+            weights_ptr<N2>(coef, r.z, wz);
+          } else {
+            weights_rt<N2>(coef, m2, r.x, wx);
+            weights_rt<N2>(coef, m2, r.y, wy);
+            weights_rt<N2>(coef, m2, r.z, wz);
+          }
+          float q[CP];
+          const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+#pragma unroll
+          for (int v = 0; v < CP / 4; ++v) {
+            const float4 tq = __ldg(q4 + v);
+            q[4 * v] = tq.x;
+            q[4 * v + 1] = tq.y;
+            q[4 * v + 2] = tq.z;
+            q[4 * v + 3] = tq.w;
+          }
+          // node l = e + k - (N2 - 1) along each axis; the k that land inside the brick
+          const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
+          const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
+          const int lx0 = ex - (N2 - 1);
+#pragma unroll 1
+          for (int k = kz0; k < kz1; ++k) {
+            const int lz = ez + k - (N2 - 1);
+            const float wzk = pick(wz, k) * S1;
+#pragma unroll 1
+            for (int j = ky0; j < ky1; ++j) {
+              const int ly = ey + j - (N2 - 1);
+              const float wyz = pick(wy, j) * wzk;
+              const int row = (lz * g.b[1] + ly) * g.b[0];
+#pragma unroll
+              for (int i = 0; i < N2; ++i) {
+                const int lx = lx0 + i;
+                if (lx < 0 || lx >= vx) continue;
+                const float w = wx[i] * wyz;
+#pragma unroll
+                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + row + lx, w, q[c], LS);
+              }
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+  }
+  // ordered write-back: every node of the brick is written once, its CP components as
+  // float4 stores (FP32: hi * 2^-s1 + lo * 2^-(s1+k), both exact scalings)
+  const float to_value = exp2f((float)-s1), lo_value = exp2f((float)(-s1 - kbits));
+  {
+    const int B0 = g.b[0], B1 = g.b[1];
+    int lx = (int)threadIdx.x % B0, ly = ((int)threadIdx.x / B0) % B1, lz = (int)threadIdx.x / (B0 * B1);
+    const int sx = (int)blockDim.x % B0, sy = ((int)blockDim.x / B0) % B1, sz = (int)blockDim.x / (B0 * B1);
+    for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+      if (lx < vx && ly < vy && lz < vz) {
+        const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ly, z = (int64_t)bz * g.b[2] + lz;
+        float4 *d = reinterpret_cast<float4 *>(field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP);
+#pragma unroll
+        for (int v4 = 0; v4 < CP / 4; ++v4) {
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int c = 4 * v4 + u;
+            const int a = c * bvol + nl;
+            float val = 0.0f;
+            if (any) val = finite ? fmaf((float)acc_hi[a], to_value, (float)acc_lo[a] * lo_value) : __int_as_float(0x7fc00000);
+            v[u] = c < g.ncomp ? val : 0.0f;
+          }
+          if (beta_zero) {
+            d[v4] = make_float4(v[0], v[1], v[2], v[3]);
+          } else {
+            const float4 o = d[v4];
+            d[v4] = make_float4(__fadd_rn(__fmul_rn(beta, o.x), v[0]), __fadd_rn(__fmul_rn(beta, o.y), v[1]),
+                                __fadd_rn(__fmul_rn(beta, o.z), v[2]), __fadd_rn(__fmul_rn(beta, o.w), v[3]));
+          }
+        }
+      }
+      lx += sx;
+      ly += sy;
+      lz += sz;
+      if (lx >= B0) { lx -= B0; ++ly; }
+      if (ly >= B1) { ly -= B1; ++lz; }
+    }
+  }
+  __syncthreads();
+}
+
+template <int N2, bool FIXED, int CP>
 __global__ void __launch_bounds__(kThreads, 2)
     k_scatter_fixed(FixGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
                     const float4 *__restrict__ rec, const float *__restrict__ qs,
                     const unsigned *__restrict__ qmax_bits, float *__restrict__ field, float beta,
                     int beta_zero, int32_t *status) {
-  extern __shared__ int acc_hi[];  // bvol * CP hi, bvol * CP lo, then the cell ranges
-  int *acc_lo = acc_hi + g.bvol * CP;
-  uint32_t *ranges = reinterpret_cast<uint32_t *>(acc_lo + g.bvol * CP);
-  __shared__ unsigned int s_count;
-  constexpr int nbw = (N2 - 2) / 2;
-  const int ecount = g.e[0] * g.e[1] * g.e[2];
+  extern __shared__ __align__(16) unsigned char smem_scatter[];
+  __shared__ uint32_t warp_tot[32];
+  __shared__ float coef[N2 * GBG_MAX_POWERS];
+  for (int i = threadIdx.x; i < N2 * s.m2; i += blockDim.x) coef[i] = s.c[i];
+  __syncthreads();
   const float qmax = __uint_as_float(*qmax_bits);
-  for (int64_t b = blockIdx.x; b < g.nbricks; b += gridDim.x) {
-    const int64_t bx = b % g.nb[0], by = (b / g.nb[0]) % g.nb[1], bz = b / (g.nb[0] * g.nb[1]);
-    __syncthreads();
-    for (int64_t i = threadIdx.x; i < 2 * g.bvol * CP; i += blockDim.x) acc_hi[i] = 0;
-    if (threadIdx.x == 0) s_count = 0u;
-    __syncthreads();
-    unsigned mine = 0;
-    for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
-      const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
-      const int64_t cx = imod(bx * g.b[0] - nbw - 1 + ex, g.n[0]);
-      const int64_t cy = imod(by * g.b[1] - nbw - 1 + ey, g.n[1]);
-      const int64_t cz = imod(bz * g.b[2] - nbw - 1 + ez, g.n[2]);
-      const int64_t kb = ((cz / g.b[2]) * g.nb[1] + cy / g.b[1]) * g.nb[0] + cx / g.b[0];
-      const int64_t key = kb * g.bvol + ((cz % g.b[2]) * g.b[1] + cy % g.b[1]) * g.b[0] + cx % g.b[0];
-      const uint32_t r0 = __ldg(cell_start + key), r1 = __ldg(cell_start + key + 1);
-      ranges[2 * e] = r0;
-      ranges[2 * e + 1] = r1;
-      mine += r1 - r0;
-    }
-    atomicAdd(&s_count, mine);
-    __syncthreads();
-    const unsigned count = s_count;
-    const double one = (double)qmax * g.l3;        // bound on one contribution
-    const double bound = one * (double)count;      // bound on a node's sum
-    const bool finite = isfinite(bound);
-    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
-    int e1 = 0, es = 0;
-    frexp(one, &e1);
-    frexp(bound, &es);
-    int s1 = min(20 - e1, 29 - es);
-    s1 = max(-120, min(120, s1));
-    const int kbits = min(21, 30 - (32 - __clz((int)count)));
-    const float S1 = exp2f((float)s1), LS = exp2f((float)kbits);
-    if (finite && count > 0 && one > 0.0) {
-      if constexpr (N2 == 4) {
-        const int qw = threadIdx.x >> 3, sub = threadIdx.x & 7, qi = sub & 3, jj = sub >> 2;
-        for (int e = qw; e < ecount; e += kThreads / 8) {
-          const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
-          if (r0 == r1) continue;
-          const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
-          const int lx = ex + qi - 3;
-          const bool inx = lx >= 0 && lx < g.b[0] && bx * g.b[0] + lx < g.n[0];
-          for (uint32_t sl = r0; sl < r1; ++sl) {
-            const float4 r = __ldg(rec + sl);
-            float wx[4], wy[4], wz[4];
-            weights_all<4, M2>(s, r.x, wx);
-            weights_all<4, M2>(s, r.y, wy);
-            weights_all<4, M2>(s, r.z, wz);
-            const float w1s = pick(wx, qi) * S1;
-            float q[CP];
-            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
-#pragma unroll
-            for (int v = 0; v < CP / 4; ++v) {
-              const float4 t = __ldg(q4 + v);
-              q[4 * v] = t.x;
-              q[4 * v + 1] = t.y;
-              q[4 * v + 2] = t.z;
-              q[4 * v + 3] = t.w;
-            }
-            if (!inx) continue;
-#pragma unroll
-            for (int jp = 0; jp < 2; ++jp) {
-              const int ly = ey + 2 * jj + jp - 3;
-              if (ly < 0 || ly >= g.b[1] || by * g.b[1] + ly >= g.n[1]) continue;
-              const float wxy = w1s * pick(wy, 2 * jj + jp);
-#pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const int lz = ez + k - 3;
-                if (lz < 0 || lz >= g.b[2] || bz * g.b[2] + lz >= g.n[2]) continue;
-                const float w = wxy * wz[k];
-                const int node = (lz * g.b[1] + ly) * g.b[0] + lx;
-#pragma unroll
-                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * (int)g.bvol + node, w, q[c], LS);
-              }
-            }
-          }
-        }
-      } else {
-        for (int e = threadIdx.x; e < ecount; e += kThreads) {
-          const uint32_t r0 = ranges[2 * e], r1 = ranges[2 * e + 1];
-          if (r0 == r1) continue;
-          const int ex = e % g.e[0], ey = (e / g.e[0]) % g.e[1], ez = e / (g.e[0] * g.e[1]);
-          for (uint32_t sl = r0; sl < r1; ++sl) {
-            const float4 r = __ldg(rec + sl);
-            float wx[N2], wy[N2], wz[N2];
-            weights_all<N2, M2>(s, r.x, wx);
-            weights_all<N2, M2>(s, r.y, wy);
-            weights_all<N2, M2>(s, r.z, wz);
-            const float *q = qs + (int64_t)sl * CP;
-#pragma unroll 1
-            for (int k = 0; k < N2; ++k) {
-              const int lz = ez + k - (N2 - 1);
-              if (lz < 0 || lz >= g.b[2] || bz * g.b[2] + lz >= g.n[2]) continue;
-#pragma unroll 1
-              for (int j = 0; j < N2; ++j) {
-                const int ly = ey + j - (N2 - 1);
-                if (ly < 0 || ly >= g.b[1] || by * g.b[1] + ly >= g.n[1]) continue;
-#pragma unroll
-                for (int i = 0; i < N2; ++i) {
-                  const int lx = ex + i - (N2 - 1);
-                  if (lx < 0 || lx >= g.b[0] || bx * g.b[0] + lx >= g.n[0]) continue;
-                  const float w = wx[i] * wy[j] * wz[k] * S1;
-                  const int node = (lz * g.b[1] + ly) * g.b[0] + lx;
-                  for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * (int)g.bvol + node, w, __ldg(q + c), LS);
-                }
-              }
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-    // ordered write-back: every node of the brick is written once (in FP32: the value is
-    // hi * 2^-s1 + lo * 2^-(s1+k); both products are exact scalings)
-    const float to_value = exp2f((float)-s1), lo_value = exp2f((float)(-s1 - kbits));
-    for (int64_t i = threadIdx.x; i < g.bvol * CP; i += blockDim.x) {
-      const int64_t nl = i / CP;
-      const int c = (int)(i - nl * CP);
-      const int lx = (int)(nl % g.b[0]), ly = (int)((nl / g.b[0]) % g.b[1]), lz = (int)(nl / (g.b[0] * g.b[1]));
-      const int64_t x = bx * g.b[0] + lx, y = by * g.b[1] + ly, z = bz * g.b[2] + lz;
-      if (x >= g.n[0] || y >= g.n[1] || z >= g.n[2]) continue;
-      float *d = field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP + c;
-      const int64_t a = (int64_t)c * g.bvol + nl;
-      float v = finite ? fmaf((float)acc_hi[a], to_value, (float)acc_lo[a] * lo_value) : __int_as_float(0x7fc00000);
-      if (c >= g.ncomp) v = 0.0f;
-      *d = beta_zero ? v : __fadd_rn(__fmul_rn(beta, *d), v);
-    }
-  }
+  for (int64_t b = blockIdx.x; b < g.nbricks; b += gridDim.x)
+    scatter_brick32<N2, FIXED, CP>(g, coef, s.m2, b, cell_start, rec, qs, qmax, field, beta, beta_zero, smem_scatter,
+                                   warp_tot, status);
 }
 
 gbg_status check_field_bins(const gbg_field_s *f, const gbg_bins_s *b, const gbg_scheme *s) {
@@ -833,27 +965,29 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
   }
 }
 
-// Per-axis weight bound of a scheme: max over nodes of sum_r |c[q, r]| (|t| <= 1).
-double axis_bound(const gbg_scheme &sch) {
-  double best = 0.0;
-  for (int q = 0; q < sch.stencil_width; ++q) {
-    double s = 0.0;
-    for (int r = 0; r < sch.num_powers; ++r) s += std::fabs(sch.coefficients[q + sch.stencil_width * r]);
-    best = s > best ? s : best;
+// True when, on every axis, the region a brick's nodes gather from (half a stencil either
+// side) lies within the neighbouring bricks: full bricks and the last, partial one are at
+// least half a stencil wide, or the axis is a single brick.
+int32_t neighbour_skip_ok(const int32_t *b, const int64_t *nb, const int64_t *n, int width) {
+  for (int d = 0; d < 3; ++d) {
+    if (nb[d] == 1) continue;
+    const int64_t last = n[d] - (nb[d] - 1) * b[d];
+    if (b[d] < width / 2 || last < width / 2) return 0;
   }
-  return best;
+  return 1;
 }
 
-template <int N2, int M2>
+template <int N2, bool FIXED>
 gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, double beta,
                                  const unsigned *qmax_bits, int32_t *status, cudaStream_t st) {
   FixGeo g;
   for (int d = 0; d < 3; ++d) {
     g.b[d] = b->b[d];
-    g.nb[d] = b->nb[d];
-    g.n[d] = f->grid.n[d];
+    g.nb[d] = (int32_t)b->nb[d];
+    g.n[d] = (int32_t)f->grid.n[d];
     g.e[d] = b->b[d] + N2 - 1;
   }
+  g.neighbour_skip = neighbour_skip_ok(b->b, b->nb, f->grid.n, N2);
   g.nbricks = b->nbricks;
   g.bvol = b->bvol;
   g.px = f->px;
@@ -861,12 +995,12 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   g.halo = f->halo;
   g.cp = f->cp;
   g.ncomp = f->ncomp;
-  const double L = axis_bound(sch);
+  const double L = weight_bound(sch, std::ldexp(1.0, -16));
   g.l3 = L * L * L;
   const SchemeT<float, N2> s = make_scheme<float, N2>(sch);
-  const size_t smem = 2 * sizeof(int) * (size_t)g.bvol * f->cp +
-                      sizeof(uint32_t) * 2 * (size_t)g.e[0] * g.e[1] * g.e[2];
-  if (smem > 200 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared accumulators");
+  const size_t smem = scatter32_smem(g, f->cp);
+  if (smem > 200 * 1024 || (size_t)g.e[0] * g.e[1] * g.e[2] > 65535)
+    return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared accumulators");
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -879,14 +1013,387 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   };
-  if (f->cp == 4) return go(k_scatter_fixed<N2, M2, 4>);
-  return go(k_scatter_fixed<N2, M2, 12>);
+  if (f->cp == 4) return go(k_scatter_fixed<N2, FIXED, 4>);
+  return go(k_scatter_fixed<N2, FIXED, 12>);
+}
+
+// ------------------------------------------------------------ batched form
+//
+// One persistent launch for the gathers of every instance and one for the scatters.  The
+// work list holds (instance, brick) units, largest instances first; CTAs take units from
+// a device counter.  The gather keeps one TMA tile in flight ahead of the one it computes.
+
+struct BatchDev {
+  StagedGeo g;   // gather geometry (tile = brick + width - 1)
+  FixGeo fg;     // scatter geometry
+  const uint32_t *cell_start;
+  const float4 *rec;
+  const uint32_t *perm;
+  float *out;    // gather output or null
+  float *dest;   // scatter destination storage or null
+  const float *qs;
+  const unsigned *qmax_bits;
+  float coef[8 * 8];  // [q + n2*p], n2 == m2 <= 8
+  int32_t n2, cp;
+  uint32_t box_bytes;
+  float beta;
+  int32_t beta_zero;
+};
+
+constexpr int kBatchGatherThreads = 512;
+
+// Work unit u of a batch launch -> (instance, brick): the k-th instance in cost order,
+// idx[k], owns the units [off[k], off[k+1]) (off[0] = 0, u < off[n]).
+__device__ __forceinline__ uint2 batch_unit(uint32_t u, const uint32_t *__restrict__ off,
+                                            const uint32_t *__restrict__ idx, int n) {
+  int lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= u) lo = mid; else hi = mid;
+  }
+  return make_uint2(__ldg(idx + lo), u - __ldg(off + lo));
+}
+
+// The points of one brick, from its staged tile: a point per quarter-warp (width 4) or
+// per thread (other widths), as in the single-instance kernels.
+template <int N2, int CP>
+__device__ void batch_gather_points(const BatchDev *d, const float *tile, uint32_t s0, uint32_t s1) {
+  const StagedGeo &g = d->g;
+  if constexpr (N2 == 4) {
+    const int lane = threadIdx.x & 31, sub = lane & 7, qi = sub & 3, jj = sub >> 2;
+    const unsigned seg_mask = 0xFFu << (lane & ~7);
+    for (uint32_t sl = s0 + (threadIdx.x >> 3); sl < s1; sl += kBatchGatherThreads / 8) {
+      const float4 r = __ldg(d->rec + sl);
+      const int64_t p = __ldg(d->perm + sl);
+      const uint32_t loc = __float_as_uint(r.w);
+      const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
+      float wx[4], wy[4], w3[4];
+      weights_ptr<4>(d->coef, r.x, wx);
+      weights_ptr<4>(d->coef, r.y, wy);
+      weights_ptr<4>(d->coef, r.z, w3);
+      const float w1 = pick(wx, qi), w2a = pick(wy, 2 * jj), w2b = pick(wy, 2 * jj + 1);
+      float acc[CP];
+#pragma unroll
+      for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
+      const int node0 = (lz * g.w[1] + ly + 2 * jj) * g.w[0] + lx + qi;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp) {
+          const float w = w1 * (jp ? w2b : w2a) * w3[k];
+          const float4 *pv = reinterpret_cast<const float4 *>(tile + (node0 + (k * g.w[1] + jp) * g.w[0]) * CP);
+#pragma unroll
+          for (int q4 = 0; q4 < CP / 4; ++q4) {
+            const float4 v = pv[q4];
+            acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
+            acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
+            acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
+            acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
+          }
+        }
+      constexpr int H = CP / 2, Q = CP / 4;
+      const bool up2 = sub & 4, up1 = sub & 2;
+      float h[H];
+#pragma unroll
+      for (int v = 0; v < H; ++v) {
+        const float keep = up2 ? acc[H + v] : acc[v], give = up2 ? acc[v] : acc[H + v];
+        h[v] = keep + __shfl_xor_sync(seg_mask, give, 4, 8);
+      }
+      float qv[Q];
+#pragma unroll
+      for (int v = 0; v < Q; ++v) {
+        const float keep = up1 ? h[Q + v] : h[v], give = up1 ? h[v] : h[Q + v];
+        qv[v] = keep + __shfl_xor_sync(seg_mask, give, 2, 8);
+      }
+#pragma unroll
+      for (int v = 0; v < Q; ++v) qv[v] += __shfl_xor_sync(seg_mask, qv[v], 1, 8);
+      if ((sub & 1) == 0) {
+        const int cbase = (up2 ? H : 0) + (up1 ? Q : 0);
+#pragma unroll
+        for (int v = 0; v < Q; ++v)
+          if (cbase + v < g.ncomp) d->out[p + g.m * (cbase + v)] = qv[v];
+      }
+    }
+  } else {
+    for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += kBatchGatherThreads) {
+      const float4 r = __ldg(d->rec + sl);
+      const uint32_t loc = __float_as_uint(r.w);
+      const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
+      float w1[N2], w2[N2], w3[N2];
+      weights_ptr<N2>(d->coef, r.x, w1);
+      weights_ptr<N2>(d->coef, r.y, w2);
+      weights_ptr<N2>(d->coef, r.z, w3);
+      float acc[CP];
+#pragma unroll
+      for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
+#pragma unroll 1
+      for (int k = 0; k < N2; ++k) {
+        const float w3k = pick(w3, k);
+#pragma unroll
+        for (int j = 0; j < N2; ++j) {
+          const float wyz = w2[j] * w3k;
+          const float *row = tile + (((lz + k) * g.w[1] + ly + j) * g.w[0] + lx) * CP;
+#pragma unroll
+          for (int i = 0; i < N2; ++i) {
+            const float w = wyz * w1[i];
+            const float4 *pv = reinterpret_cast<const float4 *>(row + i * CP);
+#pragma unroll
+            for (int q4 = 0; q4 < CP / 4; ++q4) {
+              const float4 v = pv[q4];
+              acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
+              acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
+              acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
+              acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
+            }
+          }
+        }
+      }
+      const int64_t p = __ldg(d->perm + sl);
+#pragma unroll
+      for (int c = 0; c < CP; ++c)
+        if (c < g.ncomp) d->out[p + g.m * c] = acc[c];
+    }
+  }
+}
+
+__device__ __forceinline__ bool batch_issue(const BatchDev *items, const CUtensorMap *maps, uint2 u, void *dst,
+                                            uint64_t *bar) {
+  const BatchDev *d = items + u.x;
+  const int64_t b = u.y;
+  if (!d->out) return false;
+  if (__ldg(d->cell_start + (b + 1) * d->g.bvol) <= __ldg(d->cell_start + b * d->g.bvol)) return false;
+  int64_t bx, by, bz;
+  brick_coords(d->g, b, bx, by, bz);
+  mbar_expect_tx(bar, d->box_bytes);
+  tma_load_tile(dst, maps + u.x, 0, (int)(bx * d->g.b[0]) + d->g.box_off, (int)(by * d->g.b[1]) + d->g.box_off,
+                (int)(bz * d->g.b[2]) + d->g.box_off, bar);
+  return true;
+}
+
+__global__ void __launch_bounds__(kBatchGatherThreads, 1)
+    k_batch_gather(const BatchDev *__restrict__ items, const CUtensorMap *__restrict__ maps,
+                   const uint32_t *__restrict__ off, const uint32_t *__restrict__ idx, int n, uint32_t nwork,
+                   uint32_t *counter, uint32_t buf_bytes, int nbuf, int32_t *status) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nbuf * buf_bytes);
+  __shared__ uint32_t s_unit[2];
+  __shared__ int s_issued[2];
+  if (threadIdx.x == 0) {
+    mbar_init(bars, 1);
+    mbar_init(bars + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    const uint32_t u = atomicAdd(counter, 1u);
+    s_unit[0] = u;
+    s_issued[0] = u < nwork ? batch_issue(items, maps, batch_unit(u, off, idx, n), smem, bars) : 0;
+  }
+  __syncthreads();
+  uint32_t phase[2] = {0, 0};
+  int buf = 0;
+  bool failed = false;
+  while (true) {
+    const uint32_t u = s_unit[buf];
+    if (u >= nwork) break;
+    if (nbuf == 2 && threadIdx.x == 0) {
+      const uint32_t un = atomicAdd(counter, 1u);
+      s_unit[buf ^ 1] = un;
+      s_issued[buf ^ 1] =
+          un < nwork ? batch_issue(items, maps, batch_unit(un, off, idx, n), smem + (buf ^ 1) * buf_bytes, bars + (buf ^ 1))
+                     : 0;
+    }
+    if (s_issued[buf]) {
+      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
+        failed = true;
+        if (threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_TIMEOUT);
+        break;
+      }
+      phase[buf] ^= 1;
+      const uint2 wu = batch_unit(u, off, idx, n);
+      const BatchDev *d = items + wu.x;
+      const uint32_t s0 = __ldg(d->cell_start + (int64_t)wu.y * d->g.bvol);
+      const uint32_t s1 = __ldg(d->cell_start + ((int64_t)wu.y + 1) * d->g.bvol);
+      const float *tile = reinterpret_cast<const float *>(smem + buf * buf_bytes);
+      const int kind = d->n2 * 100 + d->cp;
+      switch (kind) {
+        case 404: batch_gather_points<4, 4>(d, tile, s0, s1); break;
+        case 412: batch_gather_points<4, 12>(d, tile, s0, s1); break;
+        case 604: batch_gather_points<6, 4>(d, tile, s0, s1); break;
+        case 612: batch_gather_points<6, 12>(d, tile, s0, s1); break;
+        case 204: batch_gather_points<2, 4>(d, tile, s0, s1); break;
+        case 212: batch_gather_points<2, 12>(d, tile, s0, s1); break;
+        case 804: batch_gather_points<8, 4>(d, tile, s0, s1); break;
+        default: batch_gather_points<8, 12>(d, tile, s0, s1); break;
+      }
+    }
+    __syncthreads();
+    if (nbuf == 1) {
+      if (threadIdx.x == 0) {
+        const uint32_t un = atomicAdd(counter, 1u);
+        s_unit[0] = un;
+        s_issued[0] = un < nwork ? batch_issue(items, maps, batch_unit(un, off, idx, n), smem, bars) : 0;
+      }
+      __syncthreads();
+    } else {
+      buf ^= 1;
+    }
+  }
+  if (failed)
+    for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
+}
+
+// The scatter of every brick of every instance: units taken from the device counter.
+__global__ void __launch_bounds__(kThreads, 2)
+    k_batch_scatter(const BatchDev *__restrict__ items, const uint32_t *__restrict__ off,
+                    const uint32_t *__restrict__ idx, int n, uint32_t nwork, uint32_t *counter, int32_t *status) {
+  extern __shared__ __align__(16) unsigned char bsmem[];
+  __shared__ uint32_t s_u;
+  __shared__ uint32_t warp_tot[32];
+  while (true) {
+    if (threadIdx.x == 0) s_u = atomicAdd(counter, 1u);
+    __syncthreads();
+    const uint32_t u = s_u;
+    __syncthreads();
+    if (u >= nwork) break;
+    const uint2 wu = batch_unit(u, off, idx, n);
+    const BatchDev *d = items + wu.x;
+    const float qmax = __uint_as_float(*d->qmax_bits);
+    const int kind = d->n2 * 100 + d->cp;
+#define GBG_BATCH_SCATTER(N2, CP)                                                                              \
+  scatter_brick32<N2, true, CP>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, qmax, d->dest, d->beta, \
+                                d->beta_zero, bsmem, warp_tot, status)
+    switch (kind) {
+      case 404: GBG_BATCH_SCATTER(4, 4); break;
+      case 412: GBG_BATCH_SCATTER(4, 12); break;
+      case 604: GBG_BATCH_SCATTER(6, 4); break;
+      case 612: GBG_BATCH_SCATTER(6, 12); break;
+      case 204: GBG_BATCH_SCATTER(2, 4); break;
+      case 212: GBG_BATCH_SCATTER(2, 12); break;
+      case 804: GBG_BATCH_SCATTER(8, 4); break;
+      default: GBG_BATCH_SCATTER(8, 12); break;
+    }
+#undef GBG_BATCH_SCATTER
+  }
+}
+
+// Flat index over every destination's points (quantity preparation): item i owns
+// [offsets[i], offsets[i+1]).  Each thread keeps a running max per item and flushes it
+// with one atomic when its item changes.
+__global__ void k_batch_qprep(const BatchDev *__restrict__ items, const float *const *__restrict__ qptrs,
+                              const int64_t *__restrict__ offsets, int32_t count, float *const *qs_out,
+                              const float *__restrict__ alphas, unsigned *const *qmax_out) {
+  const int64_t total = offsets[count];
+  unsigned mx = 0u;
+  int cur = -1;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = count;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) / 2;
+      if (offsets[mid] <= t) lo = mid; else hi = mid;
+    }
+    if (lo != cur) {
+      if (cur >= 0) atomicMax(qmax_out[cur], mx);
+      cur = lo;
+      mx = 0u;
+    }
+    const BatchDev *d = items + lo;
+    const int64_t s = t - offsets[lo];
+    const int64_t m = d->g.m;
+    const int64_t p = d->perm[s];
+    const int cp = d->cp, nc = d->g.ncomp;
+    for (int c = 0; c < cp; ++c) {
+      const float v = c < nc ? alphas[lo] * qptrs[lo][p + m * c] : 0.0f;
+      qs_out[lo][s * cp + c] = v;
+      const unsigned bits = __float_as_uint(fabsf(v));
+      mx = bits > mx ? bits : mx;
+    }
+  }
+  if (cur >= 0) atomicMax(qmax_out[cur], mx);
+}
+
+// Resets the batch's unit counters and the max|alpha q| word of every destination.
+__global__ void k_batch_reset(uint32_t *counters, unsigned *const *qmax_out, int32_t count) {
+  for (int i = threadIdx.x; i < count; i += blockDim.x)
+    if (qmax_out[i]) *qmax_out[i] = 0u;
+  if (threadIdx.x < 2) counters[threadIdx.x] = 0u;
 }
 
 }  // namespace
 }  // namespace gbg
 
 using namespace gbg;
+
+namespace gbg {
+
+// Geometry and byte count of new bins (no device memory is touched).
+gbg_status bins_plan(const gbg_grid &grid, int64_t max_points, const int32_t *brick, gbg_bins_s *b) {
+  if (max_points < 0 || max_points > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "point count outside 0..2^31-1");
+  cudaGetDevice(&b->device);
+  b->grid = grid;
+  b->max_points = max_points;
+  for (int d = 0; d < 3; ++d) {
+    if (brick && brick[d] != 0) b->b[d] = brick[d];
+    if (b->b[d] < 1 || b->b[d] > 64) return set_error(GBG_EARG, "brick edges must be 1..64 cells");
+    b->nb[d] = (grid.n[d] + b->b[d] - 1) / b->b[d];
+  }
+  b->bvol = (int64_t)b->b[0] * b->b[1] * b->b[2];
+  b->nbricks = b->nb[0] * b->nb[1] * b->nb[2];
+  b->nkeys = b->nbricks * b->bvol;
+  if (b->nkeys >= (int64_t(1) << 32) - 1) return set_error(GBG_EUNSUPPORTED, "bins: 2^32 or more cells");
+  Arena a;
+  bins_layout(a, b);
+  b->bytes = a.used + 256;
+  return GBG_OK;
+}
+
+// Carves the device block of planned bins into its arrays.
+void bins_carve(gbg_bins_s *b) {
+  Arena a;
+  a.base = static_cast<char *>(b->block);
+  bins_layout(a, b);
+}
+
+gbg_status field_info(gbg_field f, gbg_grid *grid, int32_t *ncomp, int32_t *max_width) {
+  if (!f) return set_error(GBG_EARG, "null field");
+  if (grid) *grid = f->grid;
+  if (ncomp) *ncomp = f->ncomp;
+  if (max_width) *max_width = f->max_width;
+  return GBG_OK;
+}
+
+size_t bins_bytes(const gbg_grid &grid, int64_t max_points, const int32_t *brick) {
+  gbg_bins_s b;
+  return bins_plan(grid, max_points, brick, &b) == GBG_OK ? b.bytes : 0;
+}
+
+gbg_status bins_create_async(const gbg_grid &grid, int64_t max_points, const int32_t *brick, cudaStream_t stream,
+                             gbg_bins *out, size_t *bytes) {
+  auto *b = new (std::nothrow) gbg_bins_s;
+  if (!b) return set_error(GBG_ENOMEM, "host allocation failed");
+  gbg_status st = bins_plan(grid, max_points, brick, b);
+  if (st) {
+    delete b;
+    return st;
+  }
+  if (cudaMallocAsync(&b->block, b->bytes, stream) != cudaSuccess) {
+    cudaGetLastError();
+    delete b;
+    return set_error(GBG_ENOMEM, "cudaMallocAsync of the bins failed");
+  }
+  bins_carve(b);
+  b->async = true;
+  if (bytes) *bytes = b->bytes;
+  *out = b;
+  return GBG_OK;
+}
+
+gbg_status bins_destroy_async(gbg_bins b, cudaStream_t stream) {
+  if (!b) return GBG_OK;
+  const cudaError_t e = b->async ? cudaFreeAsync(b->block, stream) : cudaFree(b->block);
+  delete b;
+  if (e != cudaSuccess) return set_error(GBG_ECUDA, std::string("freeing the bins: ") + cudaGetErrorString(e));
+  return GBG_OK;
+}
+
+}  // namespace gbg
 
 extern "C" {
 
@@ -968,57 +1475,19 @@ gbg_status gbg_field_export(gbg_field f, gbg_dtype dst_dtype, void *dst, void *s
 gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32_t *brick, gbg_bins *out) {
   clear_error();
   if (!grid || !out) return set_error(GBG_EARG, "null argument");
-  if (max_points < 0 || max_points > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "point count outside 0..2^31-1");
   auto *b = new (std::nothrow) gbg_bins_s;
   if (!b) return set_error(GBG_ENOMEM, "host allocation failed");
-  cudaGetDevice(&b->device);
-  b->grid = *grid;
-  b->max_points = max_points;
-  for (int d = 0; d < 3; ++d) {
-    if (brick) b->b[d] = brick[d];
-    if (b->b[d] < 1 || b->b[d] > 64) {
-      delete b;
-      return set_error(GBG_EARG, "brick edges must be 1..64 cells");
-    }
-    b->nb[d] = (grid->n[d] + b->b[d] - 1) / b->b[d];
-  }
-  b->bvol = (int64_t)b->b[0] * b->b[1] * b->b[2];
-  b->nbricks = b->nb[0] * b->nb[1] * b->nb[2];
-  b->nkeys = b->nbricks * b->bvol;
-  if (b->nkeys >= (int64_t(1) << 32) - 1) {
+  gbg_status st = bins_plan(*grid, max_points, brick, b);
+  if (st) {
     delete b;
-    return set_error(GBG_EUNSUPPORTED, "bins: 2^32 or more cells");
+    return st;
   }
-  const int64_t m = max_points > 0 ? max_points : 1;
-  Arena a;
-  a.take<uint32_t>(m);
-  a.take<uint32_t>(m);
-  a.take<uint32_t>(m);
-  a.take<uint32_t>((size_t)b->nkeys + 1);
-  a.take<float4>(m);
-  a.take<float4>(m);
-  a.take<char>(radix_sort_temp_bytes(m));
-  a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
-  a.take<float>((size_t)m * 12);
-  a.take<unsigned>(64);
-  b->bytes = a.used + 256;
   if (cudaMalloc(&b->block, b->bytes) != cudaSuccess) {
     cudaGetLastError();
     delete b;
     return set_error(GBG_ENOMEM, "cudaMalloc of the bins failed");
   }
-  a.base = static_cast<char *>(b->block);
-  a.used = 0;
-  b->keys = a.take<uint32_t>(m);
-  b->skeys = a.take<uint32_t>(m);
-  b->perm = a.take<uint32_t>(m);
-  b->cell_start = a.take<uint32_t>((size_t)b->nkeys + 1);
-  b->rec_user = a.take<float4>(m);
-  b->rec = a.take<float4>(m);
-  b->sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
-  b->scan_tmp = a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
-  b->qs = a.take<float>((size_t)m * 12);
-  b->qmax_bits = a.take<unsigned>(64);
+  bins_carve(b);
   cudaMemset(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1));
   *out = b;
   return GBG_OK;
@@ -1132,20 +1601,21 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
     GBG_CUDA_TRY(cudaGetLastError());
   }
   // With no points the push still runs: it writes beta * field (beta == 0 clears).
-  const int w = scheme->stencil_width, p = scheme->num_powers;
+  const int w = scheme->stencil_width;
+  const bool fixed = scheme->num_powers == w;
   gbg_status s;
   if (w == 2)
-    s = p == 2 ? launch_staged_scatter<2, 2>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-               : launch_staged_scatter<2, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<2, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+              : launch_staged_scatter<2, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   else if (w == 4)
-    s = p == 4 ? launch_staged_scatter<4, 4>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-               : launch_staged_scatter<4, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<4, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+              : launch_staged_scatter<4, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   else if (w == 6)
-    s = p == 6 ? launch_staged_scatter<6, 6>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-               : launch_staged_scatter<6, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<6, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+              : launch_staged_scatter<6, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   else
-    s = p == 8 ? launch_staged_scatter<8, 8>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-               : launch_staged_scatter<8, 0>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<8, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
+              : launch_staged_scatter<8, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   GBG_TRY(s);
   const int64_t total = f->px * f->py * f->pz;
   k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
@@ -1153,6 +1623,344 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ batched form: host
+
+struct gbg_batch_s {
+  int device = 0;
+  int32_t count = 0, ng = 0, ns = 0;  // instances; of them, with a gather / a scatter
+  gbg::BatchDev *items = nullptr;
+  CUtensorMap *maps = nullptr;
+  uint32_t *goff = nullptr, *gidx = nullptr, *soff = nullptr, *sidx = nullptr;
+  uint32_t ngwork = 0, nswork = 0;
+  uint32_t *counters = nullptr;
+  const float **qptrs = nullptr;
+  float **qs_out = nullptr;
+  unsigned **qmax_out = nullptr;
+  float *alphas = nullptr;
+  int64_t *qoff = nullptr;
+  int64_t total_q = 0;
+  uint32_t buf_bytes = 0;
+  int nbuf = 2;
+  size_t gather_smem = 0, scatter_smem = 0;
+  std::vector<gbg_field> dests;
+  void *block = nullptr;  // the device tables, one allocation
+  size_t bytes = 0;
+  bool async = false;     // block from cudaMallocAsync (serving loop)
+};
+
+namespace gbg {
+
+// Host side of a batch before its tables reach the device.
+struct BatchHost {
+  std::vector<BatchDev> items;
+  std::vector<CUtensorMap> maps;
+  std::vector<uint32_t> goff, gidx, soff, sidx;
+  std::vector<const float *> qptrs;
+  std::vector<float *> qs_out;
+  std::vector<unsigned *> qmax_out;
+  std::vector<float> alphas;
+  std::vector<int64_t> qoff;
+};
+
+// Byte offsets of a batch's device tables within its block.
+struct BatchLayout {
+  size_t items, maps, goff, gidx, soff, sidx, counters, qptrs, qs_out, qmax_out, alphas, qoff, bytes;
+};
+
+BatchLayout batch_layout(int32_t n) {
+  BatchLayout L;
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t off = (at + 255) & ~size_t(255);
+    at = off + bytes;
+    return off;
+  };
+  L.items = take(sizeof(BatchDev) * n);
+  L.maps = take(sizeof(CUtensorMap) * n);
+  L.goff = take(sizeof(uint32_t) * (n + 1));
+  L.gidx = take(sizeof(uint32_t) * n);
+  L.soff = take(sizeof(uint32_t) * (n + 1));
+  L.sidx = take(sizeof(uint32_t) * n);
+  L.counters = take(sizeof(uint32_t) * 64);
+  L.qptrs = take(sizeof(const float *) * n);
+  L.qs_out = take(sizeof(float *) * n);
+  L.qmax_out = take(sizeof(unsigned *) * n);
+  L.alphas = take(sizeof(float) * n);
+  L.qoff = take(sizeof(int64_t) * (n + 1));
+  L.bytes = (at + 255) & ~size_t(255);
+  return L;
+}
+
+// Checks the items and fills the host tables and the launch shapes of bt.
+gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *bt, BatchHost &h) {
+  if (!items || count < 1) return set_error(GBG_EARG, "batch: need at least one item");
+  cudaGetDevice(&bt->device);
+  bt->count = count;
+  h.items.resize(count);
+  h.maps.resize(count);
+  h.qptrs.assign(count, nullptr);
+  h.qs_out.assign(count, nullptr);
+  h.qmax_out.assign(count, nullptr);
+  h.alphas.assign(count, 1.0f);
+  h.qoff.assign(count + 1, 0);
+  std::vector<double> cost(count);
+  uint32_t buf_max = 0;
+  size_t scat_max = 0;
+  for (int32_t i = 0; i < count; ++i) {
+    const gbg_batch_item &it = items[i];
+    gbg_field_s *f = it.field;
+    gbg_bins_s *b = it.bins;
+    GBG_TRY(check_field_bins(f, b, &it.scheme));
+    const int w = it.scheme.stencil_width;
+    if (it.scheme.num_powers != w)
+      return set_error(GBG_EUNSUPPORTED, "batch: schemes must have num_powers == stencil_width");
+    if (it.dest && (it.dest->ncomp != f->ncomp || it.dest->grid.n[0] != f->grid.n[0] ||
+                    it.dest->grid.n[1] != f->grid.n[1] || it.dest->grid.n[2] != f->grid.n[2] ||
+                    it.dest->max_width < w || !it.q))
+      return set_error(GBG_EARG, "batch: the scatter destination must match the field and have quantities");
+    BatchDev &d = h.items[i];
+    d = BatchDev{};
+    d.g = staged_geo(f, b, w);
+    d.cell_start = b->cell_start;
+    d.rec = b->rec;
+    d.perm = b->perm;
+    d.out = it.out;
+    d.dest = it.dest ? it.dest->data : nullptr;
+    d.qs = b->qs;
+    d.qmax_bits = b->qmax_bits;
+    for (int k = 0; k < 64; ++k) d.coef[k] = 0.0f;
+    for (int q = 0; q < w; ++q)
+      for (int p = 0; p < w; ++p) d.coef[q + w * p] = (float)it.scheme.coefficients[q + w * p];
+    d.n2 = w;
+    d.cp = f->cp;
+    d.box_bytes = (uint32_t)((size_t)f->cp * 4 * d.g.w[0] * d.g.w[1] * d.g.w[2]);
+    d.beta = (float)it.beta;
+    d.beta_zero = it.beta == 0.0;
+    if (it.dest) {
+      gbg_field_s *ds = it.dest;
+      for (int k = 0; k < 3; ++k) {
+        d.fg.b[k] = b->b[k];
+        d.fg.nb[k] = (int32_t)b->nb[k];
+        d.fg.n[k] = (int32_t)ds->grid.n[k];
+        d.fg.e[k] = b->b[k] + w - 1;
+      }
+      d.fg.neighbour_skip = neighbour_skip_ok(b->b, b->nb, ds->grid.n, w);
+      d.fg.nbricks = b->nbricks;
+      d.fg.bvol = b->bvol;
+      d.fg.px = ds->px;
+      d.fg.py = ds->py;
+      d.fg.halo = ds->halo;
+      d.fg.cp = ds->cp;
+      d.fg.ncomp = ds->ncomp;
+      const double L = weight_bound(it.scheme, std::ldexp(1.0, -16));
+      d.fg.l3 = L * L * L;
+      scat_max = std::max(scat_max, scatter32_smem(d.fg, ds->cp));
+      if ((size_t)d.fg.e[0] * d.fg.e[1] * d.fg.e[2] > 65535)
+        return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");
+      h.qptrs[i] = it.q;
+      h.qs_out[i] = b->qs;
+      h.qmax_out[i] = b->qmax_bits;
+      h.alphas[i] = (float)it.alpha;
+      bt->dests.push_back(it.dest);
+      h.qoff[i + 1] = b->npoints;
+    }
+    if (it.out) {
+      CUtensorMap *m = nullptr;
+      GBG_TRY(tensor_map_for(f, w, b->b, &m));
+      h.maps[i] = *m;
+      buf_max = std::max(buf_max, (d.box_bytes + 1023u) & ~1023u);
+    } else {
+      std::memset(&h.maps[i], 0, sizeof(CUtensorMap));
+    }
+    cost[i] = (double)b->npoints * w * w * w * f->cp + (double)b->nbricks;
+  }
+  for (int32_t i = 0; i < count; ++i) h.qoff[i + 1] += h.qoff[i];
+  bt->total_q = h.qoff[count];
+  // units: every brick of every instance, largest instances first
+  std::vector<int32_t> order(count);
+  for (int32_t i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t c) { return cost[a] > cost[c]; });
+  uint64_t ng = 0, ns = 0;
+  h.goff.assign(1, 0);
+  h.soff.assign(1, 0);
+  for (int32_t i : order) {
+    const uint64_t nb = (uint64_t)items[i].bins->nbricks;
+    if (items[i].out) {
+      h.gidx.push_back((uint32_t)i);
+      ng += nb;
+      h.goff.push_back((uint32_t)ng);
+    }
+    if (items[i].dest) {
+      h.sidx.push_back((uint32_t)i);
+      ns += nb;
+      h.soff.push_back((uint32_t)ns);
+    }
+  }
+  if (ng >= 0xffffffffull || ns >= 0xffffffffull) return set_error(GBG_EUNSUPPORTED, "batch: 2^32 or more bricks");
+  bt->ng = (int32_t)h.gidx.size();
+  bt->ns = (int32_t)h.sidx.size();
+  h.goff.resize(count + 1, (uint32_t)ng);
+  h.gidx.resize(count, 0);
+  h.soff.resize(count + 1, (uint32_t)ns);
+  h.sidx.resize(count, 0);
+  bt->ngwork = (uint32_t)ng;
+  bt->nswork = (uint32_t)ns;
+  bt->buf_bytes = buf_max;
+  bt->nbuf = 2 * (size_t)buf_max + 64 <= 200 * 1024 ? 2 : 1;
+  bt->gather_smem = (size_t)bt->nbuf * buf_max + 64;
+  bt->scatter_smem = scat_max;
+  if (bt->gather_smem > 227 * 1024 || bt->scatter_smem > 200 * 1024)
+    return set_error(GBG_EUNSUPPORTED, "batch: a brick's tile does not fit in shared memory");
+  bt->bytes = batch_layout(count).bytes;
+  return GBG_OK;
+}
+
+// Points bt at its device block and writes the tables' image (the bytes the block must
+// hold) into host memory of bt->bytes bytes.
+void batch_fill(gbg_batch_s *bt, const BatchHost &h, char *image) {
+  const int32_t n = bt->count;
+  char *dev = static_cast<char *>(bt->block);
+  const BatchLayout L = batch_layout(n);
+  std::memset(image, 0, bt->bytes);
+  auto put = [&](auto *&dst, size_t off, const void *src, size_t bytes) {
+    if (bytes) std::memcpy(image + off, src, bytes);
+    dst = reinterpret_cast<std::remove_reference_t<decltype(dst)>>(dev + off);
+  };
+  put(bt->items, L.items, h.items.data(), sizeof(BatchDev) * n);
+  put(bt->maps, L.maps, h.maps.data(), sizeof(CUtensorMap) * n);
+  put(bt->goff, L.goff, h.goff.data(), sizeof(uint32_t) * (n + 1));
+  put(bt->gidx, L.gidx, h.gidx.data(), sizeof(uint32_t) * n);
+  put(bt->soff, L.soff, h.soff.data(), sizeof(uint32_t) * (n + 1));
+  put(bt->sidx, L.sidx, h.sidx.data(), sizeof(uint32_t) * n);
+  put(bt->counters, L.counters, nullptr, 0);
+  put(bt->qptrs, L.qptrs, h.qptrs.data(), sizeof(const float *) * n);
+  put(bt->qs_out, L.qs_out, h.qs_out.data(), sizeof(float *) * n);
+  put(bt->qmax_out, L.qmax_out, h.qmax_out.data(), sizeof(unsigned *) * n);
+  put(bt->alphas, L.alphas, h.alphas.data(), sizeof(float) * n);
+  put(bt->qoff, L.qoff, h.qoff.data(), sizeof(int64_t) * (n + 1));
+}
+
+gbg_status batch_create_async(const gbg_batch_item *items, int32_t count, cudaStream_t stream, void *pinned,
+                              size_t pinned_bytes, gbg_batch *out) {
+  auto *bt = new (std::nothrow) gbg_batch_s;
+  if (!bt) return set_error(GBG_ENOMEM, "host allocation failed");
+  BatchHost h;
+  gbg_status st = batch_plan(items, count, bt, h);
+  if (st == GBG_OK && bt->bytes > pinned_bytes) st = set_error(GBG_ENOMEM, "batch: staging buffer too small");
+  if (st) {
+    delete bt;
+    return st;
+  }
+  if (cudaMallocAsync(&bt->block, bt->bytes, stream) != cudaSuccess) {
+    cudaGetLastError();
+    delete bt;
+    return set_error(GBG_ENOMEM, "batch: cudaMallocAsync failed");
+  }
+  bt->async = true;
+  batch_fill(bt, h, static_cast<char *>(pinned));
+  const cudaError_t e = cudaMemcpyAsync(bt->block, pinned, bt->bytes, cudaMemcpyHostToDevice, stream);
+  if (e != cudaSuccess) {
+    cudaFreeAsync(bt->block, stream);
+    delete bt;
+    return set_error(GBG_ECUDA, std::string("batch: copy failed: ") + cudaGetErrorString(e));
+  }
+  *out = bt;
+  return GBG_OK;
+}
+
+size_t batch_table_bytes(int32_t count) { return batch_layout(count).bytes; }
+
+gbg_status batch_destroy_async(gbg_batch bt, cudaStream_t stream) {
+  if (!bt) return GBG_OK;
+  const cudaError_t e = bt->async ? cudaFreeAsync(bt->block, stream) : cudaFree(bt->block);
+  delete bt;
+  if (e != cudaSuccess) return set_error(GBG_ECUDA, std::string("freeing the batch: ") + cudaGetErrorString(e));
+  return GBG_OK;
+}
+
+}  // namespace gbg
+
+extern "C" {
+
+gbg_status gbg_batch_create(const gbg_batch_item *items, int32_t count, gbg_batch *out) {
+  clear_error();
+  if (!out) return set_error(GBG_EARG, "null argument");
+  auto *bt = new (std::nothrow) gbg_batch_s;
+  if (!bt) return set_error(GBG_ENOMEM, "host allocation failed");
+  BatchHost h;
+  gbg_status st = batch_plan(items, count, bt, h);
+  if (st) {
+    delete bt;
+    return st;
+  }
+  if (cudaMalloc(&bt->block, bt->bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete bt;
+    return set_error(GBG_ENOMEM, "batch: cudaMalloc failed");
+  }
+  std::vector<char> image(bt->bytes);
+  batch_fill(bt, h, image.data());
+  const cudaError_t e = cudaMemcpy(bt->block, image.data(), bt->bytes, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(bt->block);
+    delete bt;
+    return set_error(GBG_ECUDA, std::string("batch: copy failed: ") + cudaGetErrorString(e));
+  }
+  *out = bt;
+  return GBG_OK;
+}
+
+gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
+  clear_error();
+  if (!bt) return set_error(GBG_EARG, "null batch");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  k_batch_reset<<<1, 256, 0, st>>>(bt->counters, bt->qmax_out, bt->count);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device);
+  if (bt->nswork > 0 && bt->total_q > 0) {
+    k_batch_qprep<<<launch_blocks(bt->total_q, kThreads), kThreads, 0, st>>>(bt->items, bt->qptrs, bt->qoff, bt->count,
+                                                                            bt->qs_out, bt->alphas, bt->qmax_out);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+  }
+  if (bt->ngwork > 0) {
+    GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_gather, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bt->gather_smem));
+    const int blocks = (int)std::min<uint32_t>(bt->ngwork, (uint32_t)sms);
+    k_batch_gather<<<blocks, kBatchGatherThreads, bt->gather_smem, st>>>(
+        bt->items, bt->maps, bt->goff, bt->gidx, bt->ng, bt->ngwork, bt->counters, bt->buf_bytes, bt->nbuf,
+        device_status);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+  }
+  if (bt->nswork > 0) {
+    GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)bt->scatter_smem));
+    const int blocks = (int)std::min<uint32_t>(bt->nswork, (uint32_t)(2 * sms));
+    k_batch_scatter<<<blocks, kThreads, bt->scatter_smem, st>>>(bt->items, bt->soff, bt->sidx, bt->ns, bt->nswork,
+                                                                bt->counters + 1, device_status);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    for (gbg_field_s *f : bt->dests) {
+      const int64_t total = f->px * f->py * f->pz;
+      k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
+                                                                         f->grid.n[0], f->grid.n[1], f->grid.n[2]);
+      note_launch();
+    }
+    GBG_CUDA_TRY(cudaGetLastError());
+  }
+  return GBG_OK;
+}
+
+gbg_status gbg_batch_destroy(gbg_batch bt) {
+  clear_error();
+  return batch_destroy_async(bt, nullptr);
 }
 
 }  // extern "C"

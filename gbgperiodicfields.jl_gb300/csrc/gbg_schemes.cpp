@@ -125,6 +125,38 @@ bool lagrange(int n, gbg_scheme &out) {
 
 }  // namespace
 
+namespace gbg {
+
+// An upper bound of max over q and t in [0, 1] of |w_q(t)| for w_q(t) = sum_r c[q, r] t^r.
+// The power basis is converted to the Bernstein basis of the same degree; on [0, 1] a
+// polynomial lies in the convex hull of its Bernstein coefficients, so the largest
+// |b_k| bounds it.  For the spline schemes this is 1 (attained at the nodes), where the
+// sum of |c[q, r]| over-estimates by up to 10^5.  `horner_slack` times sum_r |c[q, r]|
+// is added for the rounding of the Horner evaluation in the working precision.
+double weight_bound(const gbg_scheme &sch, double horner_slack) {
+  const int n2 = sch.stencil_width, m = sch.num_powers, d = m - 1;
+  double best = 0.0;
+  for (int q = 0; q < n2; ++q) {
+    double abs_sum = 0.0;
+    for (int r = 0; r < m; ++r) abs_sum += std::fabs(sch.coefficients[q + n2 * r]);
+    double hull = 0.0;
+    for (int k = 0; k <= d; ++k) {
+      // b_k = sum_{i <= k} C(k, i) / C(d, i) a_i; the ratio is built as a running product
+      double b = 0.0, ratio = 1.0;  // ratio = C(k, i) / C(d, i)
+      for (int i = 0; i <= k; ++i) {
+        b += ratio * sch.coefficients[q + n2 * i];
+        if (i < k) ratio *= (double)(k - i) / (double)(d - i);
+      }
+      hull = std::fmax(hull, std::fabs(b));
+    }
+    // the conversion's own rounding is far below this slack
+    best = std::fmax(best, std::fmin(hull * (1.0 + 1e-12) + horner_slack * abs_sum, abs_sum));
+  }
+  return best;
+}
+
+}  // namespace gbg
+
 extern "C" {
 
 // Interpolation.jl:236-241 (_stencil_neighbours) + 244-258 (LalescuSpline).

@@ -112,3 +112,48 @@ def anterpolate_binned(field: ResidentField, bins: PointBins, scheme, q: torch.T
                                                   q.data_ptr(), float(alpha), float(beta), _stream()),
                "gbg_anterpolate_binned")
     return field
+
+
+class Batch:
+    """Many independent instances in one persistent gather launch and one persistent scatter
+    launch (gbg_batch_create / gbg_batch_run).  Each instance is a dict with keys field,
+    bins, scheme and optionally out (FP32 (M, ncomp)), dest (ResidentField), q (FP32
+    (M, ncomp)), alpha, beta.  The batch records each instance's point count and device
+    arrays at creation; rebuilding the bins with the same point count keeps it valid."""
+
+    def __init__(self, instances):
+        items = (_lib.BatchItemC * len(instances))()
+        self._keep = []
+        for i, inst in enumerate(instances):
+            it = items[i]
+            it.field = inst["field"].handle
+            it.bins = inst["bins"].handle
+            it.scheme = inst["scheme"].c()
+            out = inst.get("out")
+            it.out = out.data_ptr() if out is not None else None
+            dest = inst.get("dest")
+            it.dest = dest.handle if dest is not None else None
+            q = inst.get("q")
+            if q is not None:
+                q = colmajor(q)
+                self._keep.append(q)
+            it.q = q.data_ptr() if q is not None else None
+            it.alpha = float(inst.get("alpha", 1.0))
+            it.beta = float(inst.get("beta", 0.0))
+        self.instances = instances
+        h = ctypes.c_void_p()
+        _lib.check(_lib.load().gbg_batch_create(items, len(instances), ctypes.byref(h)), "gbg_batch_create")
+        self.handle = h
+
+    def run(self, status: torch.Tensor | None = None):
+        _lib.check(_lib.load().gbg_batch_run(self.handle, status.data_ptr() if status is not None else None,
+                                             _stream()), "gbg_batch_run")
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().gbg_batch_destroy(h)
+            except Exception:
+                pass
+            self.handle = None

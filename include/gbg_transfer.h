@@ -207,7 +207,8 @@ gbg_status gbg_field_export(gbg_field field, gbg_dtype dst_dtype, void *dst, voi
 gbg_status gbg_field_bytes(gbg_field field, size_t *bytes);
 
 /* Bins for up to max_points points on grid, grouped by bricks of brick[0] x brick[1] x
- * brick[2] cells (NULL selects 11 x 8 x 8; each edge 1..64).  Allocates on the current
+ * brick[2] cells (NULL selects 11 x 8 x 8, and an edge of 0 that edge's default; each
+ * edge 1..64).  Allocates on the current
  * device. */
 gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32_t *brick,
                            gbg_bins *out);
@@ -232,6 +233,112 @@ gbg_status gbg_interpolate_binned(gbg_field field, gbg_bins bins, const gbg_sche
 gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype q_dtype, const void *q, double alpha, double beta,
                                   void *stream);
+
+/* ------------------------------------------------------------ batched form
+ *
+ * Many independent instances of uneven sizes (fields of different grids and component
+ * counts, point sets of different sizes, mixed stencil widths) run as ONE persistent
+ * gather launch and ONE persistent scatter launch: every (instance, brick) is a unit of
+ * work that the CTAs take from a device counter, largest instances first.  The batch
+ * holds device copies of each instance's geometry, scheme and TMA descriptor, so
+ * gbg_batch_run issues only stream operations and can be captured in a CUDA graph
+ * together with the gbg_bins_build calls that precede it. */
+typedef struct gbg_batch_s *gbg_batch;
+typedef struct {
+  gbg_field field;    /* gathered from (FP32 resident storage) */
+  gbg_bins bins;      /* the instance's binned points */
+  gbg_scheme scheme;  /* stencil of 2, 4, 6 or 8 nodes with num_powers == stencil_width */
+  float *out;         /* gather output, (M, ncomp) in the points' order, or NULL */
+  gbg_field dest;     /* scatter destination (same grid and components as field), or NULL */
+  const float *q;     /* scatter quantities, (M, ncomp) in the points' order */
+  double alpha, beta; /* dest = alpha * W^T q + beta * dest */
+} gbg_batch_item;
+gbg_status gbg_batch_create(const gbg_batch_item *items, int32_t count, gbg_batch *out);
+/* Runs the batch on stream: the scatters' quantity preparation, one gather launch, one
+ * scatter launch, and the ghost refresh of every destination. */
+gbg_status gbg_batch_run(gbg_batch batch, int32_t *device_status, void *stream);
+gbg_status gbg_batch_destroy(gbg_batch batch);
+
+/* ------------------------------------------------------------------ serving loop
+ *
+ * No counterpart in the reference, which is a library called in-process with no request
+ * loop.  A server keeps resident fields on the device and runs a native progress thread
+ * over `slots` CUDA streams.  Requests -- a gather from, or a scatter into, a resident
+ * field at device-resident positions -- queue in arrival order.  Whenever a slot is free,
+ * the thread takes the longest run of queued requests from the head that (1) numbers at
+ * most max_batch, (2) fits, with the bins it needs, in the memory budget still free, and
+ * (3) touches no field twice in a way the batch kernels would race on (a second scatter
+ * into a field, or a gather from a field the run already scatters into), builds each
+ * request's bins on the slot's stream and runs the run as one batch (gbg_batch_run).
+ * Requests that arrive while others are on the device are admitted as slots and memory
+ * free up, and the runs of different slots overlap on the device.  Requests on the same
+ * field keep their arrival order -- a gather sees every earlier scatter into its field
+ * and no later one -- through stream events, without blocking the host.  The thread
+ * learns of completion by polling events; a run whose device work passes
+ * timeout_seconds is reported as GBG_ETIMEOUT, and its memory is held until the device
+ * has finished with it.  Fault injection (gbg_server_inject) acts on the host only.
+ * While requests on a field are queued or in flight, the caller makes no other call on
+ * that field. */
+typedef struct gbg_server_s *gbg_server;
+typedef struct {
+  int32_t slots;            /* runs in flight at once, one stream each, 1..64 */
+  int32_t max_batch;        /* requests per run, 1..256 */
+  int32_t brick[3];         /* bins' brick edges; 0 selects the default edge */
+  int32_t reserved;
+  size_t hbm_budget_bytes;  /* device memory the server may hold for requests; 0 = half the free memory */
+  double timeout_seconds;   /* deadline of one run's device work, > 0 */
+} gbg_server_config;
+
+#define GBG_REQ_INTERPOLATE 1
+#define GBG_REQ_ANTERPOLATE 2
+typedef struct {
+  int32_t kind;           /* GBG_REQ_INTERPOLATE or GBG_REQ_ANTERPOLATE */
+  gbg_dtype pos_dtype;    /* GBG_F32 or GBG_F64 positions */
+  gbg_field field;        /* gathered from (interpolate) or scattered into (anterpolate) */
+  gbg_scheme scheme;      /* 2, 4, 6 or 8 nodes with num_powers == stencil_width */
+  const void *positions;  /* device, (npoints, 3) column-major; kept alive until completion */
+  int64_t npoints;
+  float *out;             /* interpolate: device (npoints, ncomp) column-major FP32 */
+  const float *q;         /* anterpolate: device (npoints, ncomp) column-major FP32 */
+  double alpha, beta;     /* anterpolate: field = alpha * W^T q + beta * field */
+  void *ready_event;      /* a cudaEvent_t the run waits for before reading the request's
+                             arrays (recorded by the caller after producing them and not
+                             re-recorded until the request completes), or NULL when the
+                             arrays are ready at submission */
+} gbg_request;
+
+typedef struct {
+  int64_t submitted, completed, failed, queued, in_flight, runs;
+  int64_t points;                  /* points of the completed requests */
+  double p50_ms, p99_ms, mean_ms, max_ms;  /* submit -> observed completion */
+  double first_submit_s, last_done_s;      /* on the server's steady clock */
+  size_t hbm_in_use, hbm_peak, hbm_budget;
+} gbg_server_counters;
+
+gbg_status gbg_server_create(const gbg_server_config *config, gbg_server *out);
+/* Queues a request and returns its ticket.  A request whose bins alone exceed the
+ * budget is refused here (GBG_EBUSY); malformed requests return GBG_EARG. */
+gbg_status gbg_server_submit(gbg_server server, const gbg_request *request, int64_t *ticket);
+/* Waits up to timeout_seconds for a ticket.  Returns GBG_OK with the request's own
+ * status in *result (GBG_OK, GBG_ENONFINITE for a non-finite position, GBG_ETIMEOUT,
+ * GBG_ENOMEM, GBG_ECUDA), or GBG_ETIMEOUT if the request is still pending.  A ticket
+ * can be waited for once. */
+gbg_status gbg_server_wait(gbg_server server, int64_t ticket, double timeout_seconds, gbg_status *result);
+/* Waits up to timeout_seconds until nothing is queued or in flight. */
+gbg_status gbg_server_drain(gbg_server server, double timeout_seconds);
+/* Counters and latency percentiles since creation or the last reset (reset != 0 clears
+ * them after reading). */
+gbg_status gbg_server_stats(gbg_server server, int32_t reset, gbg_server_counters *out);
+#define GBG_FAULT_ALLOC 1    /* the next `count` request allocations fail (GBG_ENOMEM) */
+#define GBG_FAULT_DEADLINE 2 /* the next `count` runs get a deadline already passed (GBG_ETIMEOUT) */
+gbg_status gbg_server_inject(gbg_server server, int32_t fault, int32_t count);
+/* Drains (bounded by the timeout given at creation), stops the thread and frees. */
+gbg_status gbg_server_destroy(gbg_server server);
+/* The admission rule on its own, for planning: of n queued requests (kinds, fields as
+ * opaque ids, device bytes), how many from the head form the next run given free_bytes
+ * and max_batch.  0 means the head request waits for memory. */
+gbg_status gbg_server_plan(const int32_t *kinds, const uint64_t *fields, const size_t *bytes, int32_t n,
+                           size_t free_bytes, int32_t max_batch, int32_t *run_length);
 
 #ifdef __cplusplus
 }
