@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the precision, batched and served forms (reported beside the headline)")
     return ap.parse_args()
 
 
@@ -257,6 +259,14 @@ def run_gb300(args, rank, world):
 
     if not args.no_e2e:
         result["e2e"] = e2e_gb300(args, gbg, lib, grid, field, pos_h, q_h, dev, stream)
+    if not args.no_forms:
+        del field, pos, q, out, dep, ws_scatter, ws_order
+        torch.cuda.empty_cache()
+        launches1 = lib.gbg_kernel_launches()
+        result["precision_form"] = precision_form(gbg, lib, dev, peak)
+        result["batched_form"] = batched_form(gbg, dev)
+        result["served_form"] = served_form(gbg, dev)
+        result["forms_gpu_launches"] = int(lib.gbg_kernel_launches() - launches1)
     return result
 
 
@@ -307,6 +317,245 @@ def e2e_gb300(args, gbg, lib, grid, field_dev, pos_h, q_h, dev, stream):
     d2h = sum(t.numel() * 8 for t in out_h) + sum(t.numel() * 8 for t in dep_h)
     return {"value": 4 * M_POINTS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
+
+
+# ------------------------------------------------- precision / batched / served forms
+
+def _time_ms(fn, reps=3):
+    """Minimum over reps of CUDA-event time (warm-up call first)."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def _rel_errors(got, want):
+    """max and RMS of |got - want|, relative to max|want| and RMS(want)."""
+    import torch
+    d = (got.double() - want.double())
+    w = want.double()
+    return {"max_rel": float(d.abs().max() / w.abs().max().clamp_min(1e-300)),
+            "rms_rel": float(d.square().mean().sqrt() / w.square().mean().sqrt().clamp_min(1e-300))}
+
+
+def precision_form(gbg, lib, dev, peak):
+    """512^3 field of 3 + 9 components (velocity and its gradient tensor, stored as one
+    12-component resident FP32 field), 3.2e7 uniform points, cubic gather and scatter
+    through the resident form; errors against the FP64 drop-in path (itself pinned to the
+    oracle at <= 1e-13) and the speed-up over that FP64 path on the same inputs."""
+    import torch
+    from gbgperiodicfields_gb300 import resident
+    from gbgperiodicfields_gb300.workloads import spectral_field, uniform_points
+    n, C, M = (512, 512, 512), 12, 32_000_000
+    grid = gbg.Grid3D(n, (2 * np.pi,) * 3)
+    f64 = spectral_field(n, 3, kmax=64, seed=3, project=True, gradient=True, device=dev, dtype=torch.float64)
+    field = resident.ResidentField(grid, C, max_stencil_width=4).load(f64)
+    pos_r = torch.from_numpy(uniform_points(M, seed=4)).to(dev)
+    q64_r = gbg.colmajor(torch.randn((M, C), dtype=torch.float64, device=dev))
+    bins = resident.PointBins(grid, M)
+    out = gbg.empty_colmajor((M, C), torch.float32, dev)
+    dest = resident.ResidentField(grid, C, max_stencil_width=4)
+    scheme = gbg.CatmullRom
+    # points in arrival (random) order: every gathered value lands at a random row
+    q32_r = gbg.colmajor(q64_r.float())
+    random_order = {"bins": _time_ms(lambda: bins.build(pos_r)),
+                    "gather": _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out)),
+                    "scatter": _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32_r, 1.0, 0.0))}
+    # the particle state kept in binned order on the device (re-sorted once, as a
+    # particle code does when it moves its points), the configuration reported
+    perm = bins.order().long() - 1
+    pos = gbg.colmajor(pos_r[perm])
+    q64 = gbg.colmajor(q64_r[perm])
+    q32 = gbg.colmajor(q64.float())
+    del pos_r, q64_r, q32_r, perm
+    t_bins = _time_ms(lambda: bins.build(pos))
+    t_gather = _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out))
+    t_scatter = _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
+    # the FP64 drop-in on the same inputs: reference values and the speed comparison
+    gC = grid.c()
+    sh = torch.cuda.current_stream().cuda_stream
+    out64 = gbg.empty_colmajor((M, C), torch.float64, dev)
+    dep64 = gbg.empty_colmajor(n + (C,), torch.float64, dev)
+    order = torch.empty(M, dtype=torch.int32, device=dev)
+
+    def plain_step():
+        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M, 4, order.data_ptr(),
+                                                     None, 0, sh))
+        gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, C, f64.data_ptr(), pos.data_ptr(), M,
+                                           order.data_ptr(), scheme.c(), out64.data_ptr(), None, sh))
+        gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, C, dep64.data_ptr(), pos.data_ptr(), M,
+                                           q64.data_ptr(), None, scheme.c(), 1.0, 0.0, None, 0, None, sh))
+    t_plain = _time_ms(plain_step, reps=1)
+    err_g = _rel_errors(out, out64)
+    err_s = _rel_errors(dest.read(), dep64)
+    alg = algorithmic_bytes(M, C, int(np.prod(n)), 4)
+    step = t_bins + t_gather + t_scatter
+    res = {
+        "workload": "512^3 x (3+9) FP32 resident field (velocity + gradient, |k|<=64), 3.2e7 uniform points "
+                    "kept in binned order, cubic gather + scatter, bins rebuilt per step",
+        "value": 2 * M / (step / 1e3), "unit": UNIT,
+        "per_call_ms": {"bins": t_bins, "gather": t_gather, "scatter": t_scatter},
+        "random_order_ms": random_order,
+        "roofline": {
+            "gather": {"bound": "hbm", "achieved": alg["gather"] / (t_gather / 1e3) / 1e9, "peak": peak,
+                       "unit": "GB/s", "frac": alg["gather"] / (t_gather / 1e3) / 1e9 / peak,
+                       "algorithmic_bytes": alg["gather"]},
+            "scatter": {"bound": "hbm", "achieved": alg["scatter"] / (t_scatter / 1e3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": alg["scatter"] / (t_scatter / 1e3) / 1e9 / peak,
+                        "algorithmic_bytes": alg["scatter"]}},
+        "error_vs_fp64": {"gather": err_g, "scatter": err_s},
+        "plain_fp64_ms": t_plain, "speedup_vs_plain_fp64": t_plain / step,
+    }
+    del f64, field, dest, out64, dep64, q64, q32, pos, bins, out
+    torch.cuda.empty_cache()
+    return res
+
+
+def batched_form(gbg, dev):
+    """64 instances of uneven sizes (grids 32^3..256^3, 1/3/9 components, 1e3..1e6
+    points log-uniform, cubic or quintic) in one persistent gather launch and one
+    persistent scatter launch, the whole step (bins builds + batch) replayed from a CUDA
+    graph."""
+    import torch
+    from gbgperiodicfields_gb300 import autotune, resident
+    rng = np.random.default_rng(7)
+    insts = []
+    for _ in range(64):
+        nn = int(rng.choice([32, 64, 128, 256]))
+        C = int(rng.choice([1, 3, 9]))
+        M = int(np.exp(rng.uniform(np.log(1e3), np.log(1e6))))
+        scheme = gbg.CatmullRom if rng.random() < 0.5 else gbg.LalescuSpline(6)
+        grid = gbg.Grid3D((nn,) * 3, (2 * np.pi,) * 3)
+        field = resident.ResidentField(grid, C, max_stencil_width=6).load(
+            torch.randn((C, nn, nn, nn), device=dev).permute(3, 2, 1, 0))
+        dest = resident.ResidentField(grid, C, max_stencil_width=6)
+        pos = gbg.colmajor(torch.rand((M, 3), dtype=torch.float64, device=dev) * 2 * np.pi)
+        cfg = autotune.choose(grid.grid_size, C, scheme, M)
+        bins = autotune.apply(resident.PointBins(grid, M, brick=cfg["brick"]).build(pos), cfg)
+        insts.append(dict(field=field, dest=dest, bins=bins, scheme=scheme, pos=pos, M=M,
+                          out=gbg.empty_colmajor((M, C), torch.float32, dev),
+                          q=gbg.colmajor(torch.randn((M, C), device=dev))))
+    total = sum(i["M"] for i in insts)
+    batch = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"], dest=i["dest"],
+                                 q=i["q"]) for i in insts])
+
+    def step():
+        for i in insts:
+            i["bins"].build(i["pos"])
+        batch.run()
+
+    def seq():
+        for i in insts:
+            i["bins"].build(i["pos"])
+            resident.interpolate_binned(i["field"], i["bins"], i["scheme"], out=i["out"])
+            resident.anterpolate_binned(i["dest"], i["bins"], i["scheme"], i["q"])
+
+    t_seq = _time_ms(seq)
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        step()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        step()
+    t_graph = _time_ms(lambda: graph.replay())
+    res = {"workload": "64 instances: grids {32,64,128,256}^3, C in {1,3,9}, M log-uniform 1e3..1e6, "
+                       "cubic/quintic, FP32 resident, bricks from the autotuner; bins + one gather and one "
+                       "scatter launch, CUDA graph",
+           "points": int(total), "value": 2 * total / (t_graph / 1e3), "unit": UNIT,
+           "ms_per_step": t_graph, "sequential_ms": t_seq}
+    del insts, batch, graph
+    torch.cuda.empty_cache()
+    return res
+
+
+def served_form(gbg, dev, requests=240, seed=9):
+    """Poisson requests over 8 resident FP32 3-component fields of 128^3..512^3, request
+    sizes log-uniform in [1e4, 4e6] points, 70% gathers and 30% scatters (beta = 1 into
+    the field), at 80% of the capacity measured first with a full backlog."""
+    import torch
+    from gbgperiodicfields_gb300 import resident, serving
+    rng = np.random.default_rng(seed)
+    sizes = [128, 192, 256, 320, 384, 448, 512, 512]
+    fields, grids = [], []
+    for k, nn in enumerate(sizes):
+        grid = gbg.Grid3D((nn,) * 3, (2 * np.pi,) * 3)
+        grids.append(grid)
+        fields.append(resident.ResidentField(grid, 3, max_stencil_width=4).load(
+            torch.randn((3, nn, nn, nn), device=dev).permute(3, 2, 1, 0)))
+    # a pool of request inputs, made before the clock starts
+    pool = []
+    for _ in range(64):
+        M = int(np.exp(rng.uniform(np.log(1e4), np.log(4e6))))
+        pos = gbg.colmajor(torch.rand((M, 3), dtype=torch.float64, device=dev) * 2 * np.pi)
+        pool.append(dict(M=M, pos=pos, q=gbg.colmajor(torch.randn((M, 3), device=dev)),
+                         out=gbg.empty_colmajor((M, 3), torch.float32, dev)))
+    torch.cuda.synchronize()
+    scheme = gbg.CatmullRom
+    plan = [(int(rng.integers(0, 8)), int(rng.integers(0, len(pool))), rng.random() < 0.3) for _ in range(requests)]
+
+    def issue(server, r):
+        fi, pi, is_scatter = r
+        p = pool[pi]
+        if is_scatter:
+            return server.anterpolate(fields[fi], p["pos"], scheme, p["q"], 1.0, 1.0)
+        return server.interpolate(fields[fi], p["pos"], scheme, out=p["out"])
+
+    with serving.Server(slots=4, max_batch=8, timeout=60.0) as server:
+        # capacity: the whole plan as one backlog
+        for r in plan[:16]:
+            issue(server, r)
+        server.drain()
+        server.stats(reset=True)
+        t0 = time.perf_counter()
+        tickets = [issue(server, r) for r in plan]
+        server.drain()
+        t_cap = time.perf_counter() - t0
+        for t in tickets:
+            server.wait(t)
+        cap = server.stats(reset=True)
+        capacity = requests / t_cap
+        # open loop at 80% of capacity
+        rate = 0.8 * capacity
+        gaps = rng.exponential(1.0 / rate, requests)
+        t0 = time.perf_counter()
+        due = t0
+        tickets = []
+        for r, g in zip(plan, gaps):
+            due += g
+            while True:
+                now = time.perf_counter()
+                if now >= due:
+                    break
+                time.sleep(min(due - now, 0.0005))
+            tickets.append(issue(server, r))
+        server.drain()
+        wall = time.perf_counter() - t0
+        codes = [server.wait(t) for t in tickets]
+        st = server.stats()
+    pts = sum(pool[r[1]]["M"] for r in plan)
+    res = {"workload": "8 resident FP32 3-component fields (128^3..512^3), Poisson requests, M log-uniform "
+                       "1e4..4e6, 70% gather / 30% scatter (beta=1), cubic; 4 slots, runs of <= 8",
+           "requests": requests, "capacity_req_s": capacity, "capacity_points_s": pts / t_cap,
+           "offered_req_s": rate, "load": 0.8,
+           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"], "max_ms": st["max_ms"],
+           "throughput_req_s": requests / wall, "throughput_points_s": pts / wall,
+           "runs": st["runs"], "failed": int(sum(1 for c in codes if c != 0)),
+           "hbm_peak_bytes": int(st["hbm_peak"]),
+           "backlog_p50_ms": cap["p50_ms"], "backlog_p99_ms": cap["p99_ms"]}
+    del fields, pool
+    torch.cuda.empty_cache()
+    return res
 
 
 # ----------------------------------------------------------- CPU baseline

@@ -406,8 +406,11 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // to an int64 accumulator in shared memory.  Integer addition is associative, so the
 // result does not depend on which thread adds first, and no float atomics are used.  S is
 // chosen per brick from max|alpha q| (over all points) * l3 (bound on |w1 w2 w3|, from
-// the Bernstein form of the weights: 1 for the spline schemes) and the region's point
-// count so that no sum can overflow and every contribution is kept to 2^-50 of that bound.
+// the Bernstein form of the weights: 1 for the spline schemes) and the largest number of
+// points reaching one node (window sums of the cell counts) so that no node's sum can
+// overflow and every contribution is kept to 2^-50 of that bound.  The accumulators take
+// the raw bits of fma(w, q, magic); the write-back removes K * bits(magic) modulo 2^64,
+// K being the node's number of contributions.
 constexpr int kFlatChunk = 2048;
 
 template <typename T, int N2, bool FIXED>
@@ -427,6 +430,7 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *pslot = r0s + ecount;                                            // kFlatChunk: point slot
   uint32_t *pxyz = pslot + kFlatChunk;                                       // kFlatChunk: packed cell
   uint32_t *kx = pxyz + kFlatChunk, *ky = kx + E0, *kz = ky + E1;             // per-axis key tables
+  uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
   __shared__ uint32_t warp_tot[32];
   __shared__ T cs[N2 * GBG_MAX_POWERS];
   if (!FIXED) stage_coeffs(s, cs);
@@ -444,7 +448,6 @@ __global__ void __launch_bounds__(kThreads)
     const int bc[3] = {(int)(brick % nb0), (int)((brick / nb0) % nb1), (int)(brick / ((int64_t)nb0 * nb1))};
     const int vx = min(B0, n[0] - bc[0] * B0), vy = min(B1, n[1] - bc[1] * B1), vz = min(bg.b[2], n[2] - bc[2] * bg.b[2]);
     __syncthreads();
-    for (int i = threadIdx.x; i < bvol * ncomp; i += blockDim.x) acc[i] = 0ull;
     for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
       const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
       const int e = t - (d == 0 ? 0 : (d == 1 ? E0 : E0 + E1));
@@ -471,8 +474,51 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
     __syncthreads();
+    // coverage of every node (points whose stencil reaches it): window sums of the cell
+    // counts, over x and y into the accumulators as scratch, then over z
+    if (threadIdx.x == 0) kcnt[bvol] = 0u;
+    uint32_t *scratch = reinterpret_cast<uint32_t *>(acc);
+    if (E2 <= 2 * bg.b[2] * ncomp) {
+      for (int o = threadIdx.x; o < B0 * B1 * E2; o += blockDim.x) {
+        const int lx = o % B0, r = o / B0, ly = r % B1, ez = r / B1;
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < N2; ++j) {
+          const uint32_t *row = off + (ez * E1 + ly + j) * E0 + lx;
+#pragma unroll
+          for (int i = 0; i < N2; ++i) sum += row[i];
+        }
+        scratch[o] = sum;
+      }
+      __syncthreads();
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < N2; ++k) sum += scratch[nl + k * B0 * B1];
+        kcnt[nl] = sum;
+      }
+    } else {
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+        const int lx = nl % B0, ly = (nl / B0) % B1, lz = nl / (B0 * B1);
+        uint32_t sum = 0;
+        for (int k = 0; k < N2; ++k)
+          for (int j = 0; j < N2; ++j)
+            for (int i = 0; i < N2; ++i) sum += off[((lz + k) * E1 + ly + j) * E0 + lx + i];
+        kcnt[nl] = sum;
+      }
+    }
+    __syncthreads();
+    {
+      uint32_t mx = 0;
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) mx = max(mx, kcnt[nl]);
+      mx = __reduce_max_sync(0xffffffffu, mx);
+      if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
+    }
+    for (int i = threadIdx.x; i < bvol * ncomp; i += blockDim.x) acc[i] = 0ull;
+    __syncthreads();
+    const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
-    const double one = qmax * l3, bound = one * (double)count;
+    const double one = qmax * l3, bound = one * (double)kmax;
     const bool finite = isfinite(bound);
     if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
     int e1 = 0, es = 0;
@@ -481,7 +527,8 @@ __global__ void __launch_bounds__(kThreads)
     const int s1 = max(-1000, min(1000, min(50 - e1, 61 - es)));
     const double S = ldexp(1.0, s1);
     const double magic = 6755399441055744.0;  // 1.5 * 2^52
-    if (finite && count > 0 && one > 0.0) {
+    const bool accumulated = finite && count > 0 && one > 0.0;
+    if (accumulated) {
       for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk) {
         const uint32_t c1 = min(count, c0 + kFlatChunk);
         {
@@ -536,8 +583,7 @@ __global__ void __launch_bounds__(kThreads)
                 const double w = (double)w1[i] * wyz;
                 for (int c = 0; c < ncomp; ++c) {
                   const double h = fma(w, (double)__ldg(qv + c), magic);
-                  atomicAdd(acc + c * bvol + row + lx,
-                            (unsigned long long)(__double_as_longlong(h) - __double_as_longlong(magic)));
+                  atomicAdd(acc + c * bvol + row + lx, (unsigned long long)__double_as_longlong(h));
                 }
               }
             }
@@ -555,7 +601,10 @@ __global__ void __launch_bounds__(kThreads)
         if (lx < vx && ly < vy && lz < vz) {
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-          const T v = finite ? (T)((double)(long long)acc[c * bvol + nl] * to_value) : quiet_nan<T>();
+          // each add carried bits(magic) once: remove K * bits(magic), modulo 2^64
+          const unsigned long long bias = (unsigned long long)kcnt[nl] * (unsigned long long)__double_as_longlong(magic);
+          const T v = accumulated ? (T)((double)(long long)(acc[c * bvol + nl] - bias) * to_value)
+                                  : (finite ? T(0) : quiet_nan<T>());
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
         }
         lx += lsx;
@@ -701,7 +750,8 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   const size_t ecount = (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
   p.smem = (size_t)p.bg.bvol * ncomp * sizeof(unsigned long long) + 2 * sizeof(uint32_t) * ecount +
            2 * sizeof(uint32_t) * kFlatChunk +
-           sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1));
+           sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1)) +
+           sizeof(uint32_t) * (size_t)(p.bg.bvol + 1);
   (void)esize;
   if (ecount > 65535) wide_enough = false;
   p.bricked = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;

@@ -62,6 +62,7 @@ struct gbg_bins_s {
   void *block = nullptr;
   size_t bytes = 0;
   bool async = false;  // block from cudaMallocAsync (serving loop)
+  int32_t gather_threads = 0, scatter_threads = 0;  // 0: the defaults (gbg_bins_set_launch)
 };
 
 namespace gbg {
@@ -388,7 +389,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
   const int qi = sub & 3, jj = sub >> 2;
   const unsigned seg_mask = 0xFFu << (lane & ~7);
   const int qw = threadIdx.x >> 3;  // quarter-warp id within the CTA
-  const int nqw = kGatherThreads / 8;
+  const int nqw = (int)blockDim.x / 8;
   uint32_t phase[2] = {0, 0};
   bool failed = false;
 
@@ -531,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       phase[buf] ^= 1;
       const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
-      for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += kThreads) {
+      for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += blockDim.x) {
         const float4 r = __ldg(rec + sl);
         const uint32_t loc = __float_as_uint(r.w);
         const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
@@ -636,13 +637,16 @@ struct FixGeo {
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
-__device__ __forceinline__ void add_fixed(int *hi_acc, int *lo_acc, int idx, float w, float q, float lo_scale) {
+// The accumulators receive the raw bit patterns of h and l: each add carries the magic
+// number's bits once, and the write-back removes K * bits(magic) (modulo 2^32), K being the
+// node's number of contributions (its coverage count), so no subtraction runs per add.
+__device__ __forceinline__ void add_fixed(unsigned *hi_acc, unsigned *lo_acc, int idx, float w, float q,
+                                          float lo_scale) {
   const float h = fmaf(w, q, kMagic);
-  const float hi_f = h - kMagic;  // exact: an integer below 2^22
-  const float r = fmaf(w, q, -hi_f);
+  const float r = fmaf(w, q, -(h - kMagic));  // h - kMagic is exact: an integer below 2^21
   const float l = fmaf(r, lo_scale, kMagic);
-  atomicAdd(hi_acc + idx, __float_as_int(h) - kMagicBits);
-  atomicAdd(lo_acc + idx, __float_as_int(l) - kMagicBits);
+  atomicAdd(hi_acc + idx, __float_as_uint(h));
+  atomicAdd(lo_acc + idx, __float_as_uint(l));
 }
 
 // All N2 weights from coefficients in memory ([q + N2*p], M2 == N2 powers).
@@ -676,7 +680,7 @@ constexpr int kFlatChunk32 = 2048;
 size_t scatter32_smem(const FixGeo &g, int cp) {
   const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
   return 2 * sizeof(int) * (size_t)g.bvol * cp + 2 * sizeof(uint32_t) * ecount + 2 * sizeof(uint32_t) * kFlatChunk32 +
-         sizeof(uint32_t) * (size_t)(g.e[0] + g.e[1] + g.e[2]);
+         sizeof(uint32_t) * (size_t)(g.e[0] + g.e[1] + g.e[2]) + sizeof(uint32_t) * (size_t)(g.bvol + 1);
 }
 
 // The scatter of one brick: list the region's points, give each thread a point, and add
@@ -692,13 +696,14 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
   const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)g.bvol;
-  int *acc_hi = reinterpret_cast<int *>(smem);
-  int *acc_lo = acc_hi + bvol * CP;
+  unsigned *acc_hi = reinterpret_cast<unsigned *>(smem);
+  unsigned *acc_lo = acc_hi + bvol * CP;
   uint32_t *off = reinterpret_cast<uint32_t *>(acc_lo + bvol * CP);
   uint32_t *r0s = off + ecount;
   uint32_t *pslot = r0s + ecount;
   uint32_t *pxyz = pslot + kFlatChunk32;
   uint32_t *kx = pxyz + kFlatChunk32, *ky = kx + E0, *kz = ky + E1;
+  uint32_t *kcnt = kz + E2;  // bvol coverage counts, then their maximum
   constexpr int half = N2 / 2;
   const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]), bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
   // nodes of this brick inside the grid
@@ -720,9 +725,8 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
   if (!any && !beta_zero && beta == 1.0f) return;  // the brick keeps its values
   uint32_t count = 0;
   int s1 = 0, kbits = 0;
-  bool finite = true;
+  bool finite = true, accumulated = false;
   if (any) {
-    for (int i = threadIdx.x; i < 2 * bvol * CP; i += blockDim.x) acc_hi[i] = 0;
     // per-axis key tables of the region's cells (periodic wrap, then brick and local index)
     for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
       const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
@@ -752,17 +756,61 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
       }
     }
     __syncthreads();
+    // coverage of every node (points whose stencil reaches it): window sums of the cell
+    // counts, over x and y into acc_hi as scratch, then over z
+    const int B0 = g.b[0], B1 = g.b[1];
+    if (threadIdx.x == 0) kcnt[bvol] = 0u;
+    if (E2 <= g.b[2] * CP) {
+      for (int o = threadIdx.x; o < B0 * B1 * E2; o += blockDim.x) {
+        const int lx = o % B0, r = o / B0, ly = r % B1, ez = r / B1;
+        uint32_t sum = 0;
+#pragma unroll
+        for (int j = 0; j < N2; ++j) {
+          const uint32_t *row = off + (ez * E1 + ly + j) * E0 + lx;
+#pragma unroll
+          for (int i = 0; i < N2; ++i) sum += row[i];
+        }
+        acc_hi[o] = sum;
+      }
+      __syncthreads();
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < N2; ++k) sum += acc_hi[nl + k * B0 * B1];
+        kcnt[nl] = sum;
+      }
+    } else {
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
+        const int lx = nl % B0, ly = (nl / B0) % B1, lz = nl / (B0 * B1);
+        uint32_t sum = 0;
+        for (int k = 0; k < N2; ++k)
+          for (int j = 0; j < N2; ++j)
+            for (int i = 0; i < N2; ++i) sum += off[((lz + k) * E1 + ly + j) * E0 + lx + i];
+        kcnt[nl] = sum;
+      }
+    }
+    __syncthreads();
+    {
+      uint32_t mx = 0;
+      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) mx = max(mx, kcnt[nl]);
+      mx = __reduce_max_sync(0xffffffffu, mx);
+      if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
+    }
+    for (int i = threadIdx.x; i < 2 * bvol * CP; i += blockDim.x) acc_hi[i] = 0u;
+    __syncthreads();
+    const uint32_t kmax = kcnt[bvol];
     count = block_scan_counts(off, ecount, warp_tot);
-    const double one = (double)qmax * g.l3, bound = one * (double)count;
+    const double one = (double)qmax * g.l3, bound = one * (double)kmax;
     finite = isfinite(bound);
     if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
     int e1 = 0, es = 0;
     frexp(one, &e1);
     frexp(bound, &es);
     s1 = max(-120, min(120, min(20 - e1, 29 - es)));
-    kbits = min(21, 30 - (32 - __clz((int)max(count, 1u))));
+    kbits = min(21, 30 - (32 - __clz((int)max(kmax, 1u))));
     const float S1 = exp2f((float)s1), LS = exp2f((float)kbits);
-    if (finite && count > 0 && one > 0.0) {
+    accumulated = finite && count > 0 && one > 0.0;
+    if (accumulated) {
       for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk32) {
         const uint32_t c1 = min(count, c0 + kFlatChunk32);
         {
@@ -856,7 +904,12 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
             const int c = 4 * v4 + u;
             const int a = c * bvol + nl;
             float val = 0.0f;
-            if (any) val = finite ? fmaf((float)acc_hi[a], to_value, (float)acc_lo[a] * lo_value) : __int_as_float(0x7fc00000);
+            if (accumulated) {
+              const unsigned bias = kcnt[nl] * (unsigned)kMagicBits;  // modulo 2^32
+              val = fmaf((float)(int)(acc_hi[a] - bias), to_value, (float)(int)(acc_lo[a] - bias) * lo_value);
+            } else if (!finite) {
+              val = __int_as_float(0x7fc00000);
+            }
             v[u] = c < g.ncomp ? val : 0.0f;
           }
           if (beta_zero) {
@@ -945,11 +998,13 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms);
   int32_t *status = nullptr;
-  const int threads = N2 == 4 ? kGatherThreads : kThreads;
+  const int threads = b->gather_threads ? b->gather_threads : (N2 == 4 ? kGatherThreads : kThreads);
   auto go = [&](auto kernel) -> gbg_status {
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
     kernel<<<blocks, threads, smem, st>>>(*map, g, s, b->cell_start, b->rec, b->perm, out, status, nbuf, tile_bytes,
                                            box_bytes);
     note_launch();
@@ -1004,10 +1059,13 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * 2);
+  const int threads = b->scatter_threads ? b->scatter_threads : kThreads;
   auto go = [&](auto kernel) -> gbg_status {
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<blocks, kThreads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
+    kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
                                            beta == 0.0, status);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
@@ -1490,6 +1548,18 @@ gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32
   bins_carve(b);
   cudaMemset(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1));
   *out = b;
+  return GBG_OK;
+}
+
+gbg_status gbg_bins_set_launch(gbg_bins b, int32_t gather_threads, int32_t scatter_threads) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  if (gather_threads != 0 && gather_threads != 128 && gather_threads != 256 && gather_threads != 512)
+    return set_error(GBG_EARG, "gather_threads must be 0, 128, 256 or 512");
+  if (scatter_threads != 0 && scatter_threads != 64 && scatter_threads != 128 && scatter_threads != 256)
+    return set_error(GBG_EARG, "scatter_threads must be 0, 64, 128 or 256");
+  b->gather_threads = gather_threads;
+  b->scatter_threads = scatter_threads;
   return GBG_OK;
 }
 

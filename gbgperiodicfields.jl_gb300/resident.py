@@ -91,6 +91,13 @@ class PointBins:
                                               _stream()), "gbg_bins_build")
         return self
 
+    def set_launch(self, gather_threads: int = 0, scatter_threads: int = 0):
+        """Threads per CTA of the binned gather and scatter (0 = default)."""
+        _lib.check(_lib.load().gbg_bins_set_launch(self.handle, int(gather_threads), int(scatter_threads)),
+                   "gbg_bins_set_launch")
+        self.gather_threads, self.scatter_threads = int(gather_threads), int(scatter_threads)
+        return self
+
     def order(self) -> torch.Tensor:
         o = torch.empty(self.npoints, dtype=torch.int32, device="cuda")
         _lib.check(_lib.load().gbg_bins_order(self.handle, o.data_ptr(), _stream()), "gbg_bins_order")

@@ -213,6 +213,11 @@ gbg_status gbg_field_bytes(gbg_field field, size_t *bytes);
 gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32_t *brick,
                            gbg_bins *out);
 gbg_status gbg_bins_destroy(gbg_bins bins);
+/* Threads per CTA of the binned gather (0 = default, 128, 256 or 512) and scatter
+ * (0 = default, 64, 128 or 256) launched on these bins: the autotuner's knobs beside
+ * the brick edges.  Each CTA works through whole bricks; the grid is sized from the
+ * occupancy the choice allows.  No counterpart in the reference. */
+gbg_status gbg_bins_set_launch(gbg_bins bins, int32_t gather_threads, int32_t scatter_threads);
 /* Bins the points: each position is wrapped periodically and split into a cell index
  * and a fractional offset in the positions' own precision (FP64 positions keep FP64
  * for this step), then the points are stably sorted by brick and cell on the device.

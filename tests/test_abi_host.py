@@ -138,3 +138,18 @@ def test_c_abi_checks_before_launch(gbg):
     # keys, sorted keys, permutation, a 32-byte record and 3 quantities per point, at least
     assert nbytes.value > 1000 * (3 * 4 + 32 + 3 * 8)
     assert lib.gbg_point_traversal_order_workspace_size(grid, 1000, 0, ctypes.byref(nbytes)) == gbg._lib.GBG_EARG
+
+
+def test_autotune_heuristic_and_cache_keys(gbg, tmp_path, monkeypatch):
+    from gbgperiodicfields_gb300 import autotune
+    monkeypatch.setenv("GBG_TUNE_CACHE", str(tmp_path / "t.json"))
+    big = autotune.heuristic((256, 256, 256), 3, gbg.CatmullRom, 10**6)
+    assert big["brick"] == list(autotune.DEFAULT_BRICK) and big["source"] == "heuristic"
+    small = autotune.heuristic((32, 32, 32), 3, gbg.CatmullRom, 10**6)
+    nb = np.prod([-(-32 // e) for e in small["brick"]])
+    assert nb >= 2 * 152 or small["brick"] == list(min(autotune.BRICKS, key=np.prod))
+    k1 = autotune.key((64, 64, 64), 3, gbg.CatmullRom, 64 ** 3)
+    k2 = autotune.key((64, 64, 64), 3, gbg.LalescuSpline(6), 64 ** 3)
+    k3 = autotune.key((64, 64, 64), 3, gbg.CatmullRom, 8 * 64 ** 3)
+    assert len({k1, k2, k3}) == 3
+    assert autotune.choose((64, 64, 64), 3, gbg.CatmullRom, 64 ** 3)["source"] == "heuristic"

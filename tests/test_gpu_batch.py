@@ -95,3 +95,41 @@ def test_batch_step_in_cuda_graph(gbg, oracle, dev):
     for i, o, d in zip(insts, ref_out, ref_dest):
         assert torch.equal(i["out"], o)
         assert torch.equal(i["dest"].read(), d)
+
+
+def test_autotune_persists_and_keeps_results(gbg, oracle, dev, tmp_path, monkeypatch):
+    """The tuner's choice (brick, threads per CTA) changes the launch shape only: results
+    stay within the precision form's tolerance of the default configuration, and the
+    choice is cached per problem class."""
+    from gbgperiodicfields_gb300 import autotune, resident
+    monkeypatch.setenv("GBG_TUNE_CACHE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(21)
+    grid = gbg.Grid3D((40, 36, 32), (TWO_PI,) * 3)
+    g = oracle.grid_dict(grid.grid_size, grid.domain_size, grid.origin)
+    M, C = 30000, 3
+    pos = np.asfortranarray(TWO_PI * rng.random((M, 3)))
+    pos_t = torch.from_numpy(pos).cuda()
+    res = autotune.tune(grid, C, gbg.CatmullRom, pos_t, bricks=((11, 8, 8), (7, 4, 4)),
+                        gather_threads=(256, 512), scatter_threads=(128, 256), reps=1)
+    assert len(res["trials"]) == 2 and res["brick"] in ([11, 8, 8], [7, 4, 4])
+    chosen = autotune.choose(grid.grid_size, C, gbg.CatmullRom, M)
+    assert chosen["source"] == "cache" and chosen["brick"] == res["brick"]
+    f = np.asfortranarray(rng.standard_normal(grid.grid_size + (C,)))
+    q = np.asfortranarray(rng.standard_normal((M, C)))
+    field = resident.ResidentField(grid, C, max_stencil_width=4).load(torch.from_numpy(f).cuda())
+    bins = autotune.apply(resident.PointBins(grid, M, brick=chosen["brick"]).build(pos_t), chosen)
+    got = resident.interpolate_binned(field, bins, gbg.CatmullRom).cpu().numpy()
+    assert relerr(got, oracle.gather(g, f, pos, gbg.CatmullRom.coefficients)) <= 1e-5
+    dest = resident.ResidentField(grid, C, max_stencil_width=4)
+    resident.anterpolate_binned(dest, bins, gbg.CatmullRom, torch.from_numpy(q).float().cuda())
+    want = oracle.scatter(g, np.zeros(grid.grid_size + (C,), order="F"), pos, q, gbg.CatmullRom.coefficients)
+    assert relerr(dest.read().cpu().numpy(), want) <= 1e-5
+    # every thread choice gives the same bits for the scatter (integer accumulation)
+    ref = dest.read()
+    for gt, st in ((128, 64), (512, 256), (256, 128)):
+        bins.set_launch(gt, st)
+        d2 = resident.ResidentField(grid, C, max_stencil_width=4)
+        resident.anterpolate_binned(d2, bins, gbg.CatmullRom, torch.from_numpy(q).float().cuda())
+        assert torch.equal(d2.read(), ref)
+        assert torch.equal(resident.interpolate_binned(field, bins, gbg.CatmullRom),
+                           torch.from_numpy(got).cuda())
