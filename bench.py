@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the precision, batched and served forms (reported beside the headline)")
+    ap.add_argument("--case", choices=sorted(PROFILE_CASES),
+                    help="run one small fixed case twice and exit (the inputs of the ncu captures in profiles/)")
     return ap.parse_args()
 
 
@@ -620,8 +622,61 @@ def run_reference(args, rank, world):
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+# ------------------------------------------------------- profiling cases
+
+def case_resident(n=256, C=12, M=4_000_000):
+    """256^3 x 12 FP32 resident field (0.85 GB), 4e6 uniform points in binned order,
+    cubic gather and scatter, twice."""
+    import torch
+    from __graft_entry__ import load_package
+    gbg = load_package()
+    from gbgperiodicfields_gb300 import resident
+    from gbgperiodicfields_gb300.workloads import uniform_points
+    dev = torch.device("cuda:0")
+    grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3)
+    field = resident.ResidentField(grid, C, max_stencil_width=4).load(
+        torch.randn((C, n, n, n), device=dev).permute(3, 2, 1, 0))
+    pos = torch.from_numpy(uniform_points(M, seed=2)).to(dev)
+    bins = resident.PointBins(grid, M).build(pos)
+    pos = gbg.colmajor(pos[bins.order().long() - 1])
+    bins.build(pos)
+    out = gbg.empty_colmajor((M, C), torch.float32, dev)
+    q = gbg.colmajor(torch.randn((M, C), dtype=torch.float32, device=dev))
+    for _ in range(2):
+        resident.interpolate_binned(field, bins, gbg.CatmullRom, out=out)
+        resident.anterpolate_binned(field, bins, gbg.CatmullRom, q)
+    torch.cuda.synchronize()
+
+
+def case_plain(n=256, M=4_000_000):
+    """256^3 x 3 FP64 field (403 MB, above L2), 4e6 clustered points, quintic
+    (LalescuSpline(6)) scatter and gather through the drop-in API, twice."""
+    import torch
+    from __graft_entry__ import load_package
+    gbg = load_package()
+    from gbgperiodicfields_gb300.workloads import clustered_points
+    dev = torch.device("cuda:0")
+    grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3)
+    pts = gbg.PointSet(torch.from_numpy(clustered_points(M, seed=3)).to(dev))
+    q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=torch.float64, device=dev)))
+    f = gbg.VectorFieldPhysical(gbg.colmajor(torch.randn((n, n, n, 3), dtype=torch.float64, device=dev)), grid)
+    order = gbg.point_traversal_order(grid, pts)
+    s = gbg.LalescuSpline(6)
+    for _ in range(2):
+        gbg.anterpolate_(f, pts, q, s, 1.0, 0.0)
+        gbg.interpolate(f, pts, s, traversal=order)
+    torch.cuda.synchronize()
+
+
+PROFILE_CASES = {"resident_256c12_4e6": case_resident, "plain_256c3_4e6_quintic": case_plain}
+
+
 def main():
     args = parse()
+    if args.case:
+        PROFILE_CASES[args.case]()
+        print(json.dumps({"case": args.case, "ok": True}))
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:

@@ -10,9 +10,9 @@ from ._lib import ArgumentError, DimensionMismatch, GBGError, InexactError
 from .api import (AbstractFieldPhysical, AbstractPointValues, Grid3D, LagrangeSpline, LalescuSpline,
                   PointSet, PointTraversalOrder, PointTraversalOrderScratch, ScalarFieldPhysical,
                   ScalarPointValues, TensorFieldPhysical, TensorPointValues, VectorFieldPhysical,
-                  VectorPointValues, anterpolate, anterpolate_, colmajor, empty_colmajor, field_data,
-                  field_grid, interpolate, interpolate_, npoints, point_positions,
-                  point_traversal_order, point_traversal_order_, point_values, sample_field,
+                  VectorPointValues, anterpolate, anterpolate_, colmajor, displace_, empty_colmajor,
+                  field_data, field_grid, interpolate, interpolate_, npoints, point_positions,
+                  point_traversal_order, point_traversal_order_, point_values, sample_field, wrap_,
                   zeros_colmajor)
 
 

@@ -133,6 +133,10 @@ SIGNATURES = {
     "gbg_bins_create": (_I32, [_GP, _I64, ctypes.POINTER(_I32), ctypes.POINTER(_P)]),
     "gbg_bins_destroy": (_I32, [_P]),
     "gbg_bins_set_launch": (_I32, [_P, _I32, _I32]),
+    "gbg_points_displace": (_I32, [_GP, _I32, _P, _P, _I64, _I32, ctypes.POINTER(_D), ctypes.POINTER(_P), _P]),
+    "gbg_bins_build_displaced": (_I32, [_P, _I32, _P, _P, _I64, _I32, ctypes.POINTER(_D), ctypes.POINTER(_P),
+                                        _I32, _P, _P]),
+    "gbg_bins_permute": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "gbg_bins_build": (_I32, [_P, _I32, _P, _I64, _P, _P]),
     "gbg_bins_order": (_I32, [_P, _P, _P]),
     "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P]),

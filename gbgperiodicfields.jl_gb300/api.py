@@ -578,3 +578,78 @@ def anterpolate(grid: Grid3D, points: PointSet, quantities: AbstractPointValues,
     R = quantities.tensor_order
     data = empty_colmajor(tuple(grid.grid_size) + (3,) * R, grid.dtype, quantities.data.device)
     return anterpolate_(AbstractFieldPhysical(data, grid, R), points, quantities, scheme, traversal=traversal)
+
+
+# ------------------------------------------------------------ displacement
+
+
+def _displace_terms(destination: PointSet, terms):
+    """Points.jl:1286-1307: every section matches the point set's count, precision and
+    array family; coefficients are real."""
+    secs, coefs = [], []
+    for term in terms:
+        if not (isinstance(term, tuple) and len(term) == 2 and isinstance(term[1], AbstractPointValues)
+                and term[1].tensor_order == 1):
+            raise ArgumentError("a displacement term is a (coefficient, VectorPointValues) tuple")
+        c, v = term
+        if isinstance(c, complex) or not isinstance(c, (int, float)) or isinstance(c, bool):
+            raise ArgumentError(f"a displacement coefficient must be real, got {type(c).__name__}")
+        _check_npoints_match(destination, v)
+        if v.data.dtype != destination.dtype:
+            raise ArgumentError(f"a displacement section's scalar type {v.data.dtype} does not match the point "
+                                f"set's {destination.dtype}; displacement does not convert between precisions")
+        if v.data.device != destination.device:
+            raise ArgumentError("a displacement section must live in the point set's array family")
+        secs.append(v.data)
+        coefs.append(float(c))
+    return secs, coefs
+
+
+def displace_(destination: PointSet, *args) -> PointSet:
+    """displace! (Points.jl:1382-1440).  Forms, as in the reference:
+
+        displace_(destination, source, (c1, v1), (c2, v2), ...)
+        displace_(destination, source, grid, (c1, v1), ...)
+        displace_(points, (c1, v1), ...)
+        displace_(points, grid, (c1, v1), ...)
+
+    Each coordinate becomes source + c1*v1 + c2*v2 + ... (products and sums rounded in the
+    positions' type, left to right); with a grid the result is wrapped into
+    [origin, origin + domain).  Returns destination."""
+    args = list(args)
+    source = destination
+    if args and isinstance(args[0], PointSet):
+        source = args.pop(0)
+    grid = None
+    if args and isinstance(args[0], Grid3D):
+        grid = args.pop(0)
+    _check_npoints_match(destination, source)
+    if source.dtype != destination.dtype:
+        raise ArgumentError(f"point-set scalar types differ: {destination.dtype} and {source.dtype}; "
+                            "displacement does not convert between precisions")
+    if source.device != destination.device:
+        raise ArgumentError("point sets must live in the same array family")
+    if grid is not None and grid.dtype != destination.dtype:
+        raise ArgumentError(f"the domain's element type {grid.dtype} does not match the point set's "
+                            f"{destination.dtype}; displacement does not convert between precisions")
+    secs, coefs = _displace_terms(destination, args)
+    _require_cuda(destination.positions, "displace!")
+    m = destination.npoints
+    if m == 0:
+        return destination
+    lib = _lib.load()
+    import ctypes
+    carr = (ctypes.c_double * max(1, len(coefs)))(*coefs)
+    parr = (ctypes.c_void_p * max(1, len(secs)))(*[v.data_ptr() for v in secs])
+    with torch.cuda.device(destination.device):
+        stream = torch.cuda.current_stream()
+        _lib.check(lib.gbg_points_displace(grid.c() if grid is not None else None, _DTYPE_CODE[destination.dtype],
+                                           destination.positions.data_ptr(), source.positions.data_ptr(), m,
+                                           len(secs), carr, parr, stream.cuda_stream), "displace!")
+        stream.synchronize()
+    return destination
+
+
+def wrap_(points: PointSet, grid: Grid3D) -> PointSet:
+    """wrap! (Points.jl:1481-1490): every coordinate reduced to [origin, origin + domain)."""
+    return displace_(points, grid)

@@ -401,7 +401,8 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 
 // The default scatter (deterministic, FP64-grade).  A CTA owns one brick of nodes.  It
 // lists the points of every cell whose stencil reaches the brick (the extended region),
-// gives each thread a point, and adds every contribution w*alpha*q, scaled by a power of
+// gives each warp a point (its lanes cover the point's nodes inside the brick), and adds
+// every contribution w*alpha*q, scaled by a power of
 // two S and rounded once to an integer with the FP64 "magic number" 1.5*2^52 (one FMA),
 // to an int64 accumulator in shared memory.  Integer addition is associative, so the
 // result does not depend on which thread adds first, and no float atomics are used.  S is
@@ -433,7 +434,9 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
   __shared__ uint32_t warp_tot[32];
   __shared__ T cs[N2 * GBG_MAX_POWERS];
-  if (!FIXED) stage_coeffs(s, cs);
+  stage_coeffs(s, cs);
+  const int m2 = FIXED ? N2 : s.m2;
+  const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5, nwarps = (int)blockDim.x >> 5;
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
   const int n[3] = {(int)g.nx, (int)g.ny, (int)g.nz};
@@ -549,41 +552,91 @@ __global__ void __launch_bounds__(kThreads)
           }
         }
         __syncthreads();
-        for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
-          const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
-          const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-          const RecT<T> r = rec[sl];
-          T w1[N2], w2[N2], w3[N2];
-          if constexpr (FIXED) {
-            axis_weights_m<T, N2, N2>(s, r.t[0], w1);
-            axis_weights_m<T, N2, N2>(s, r.t[1], w2);
-            axis_weights_m<T, N2, N2>(s, r.t[2], w3);
-          } else {
-            axis_weights_dyn(cs, N2, s.m2, r.t[0], w1);
-            axis_weights_dyn(cs, N2, s.m2, r.t[1], w2);
-            axis_weights_dyn(cs, N2, s.m2, r.t[2], w3);
+        if constexpr (N2 <= 4) {
+          // stencils of up to 64 nodes: a thread per point
+          for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
+            const RecT<T> r = rec[sl];
+            T w1[N2], w2[N2], w3[N2];
+            if constexpr (FIXED) {
+              axis_weights_m<T, N2, N2>(s, r.t[0], w1);
+              axis_weights_m<T, N2, N2>(s, r.t[1], w2);
+              axis_weights_m<T, N2, N2>(s, r.t[2], w3);
+            } else {
+              axis_weights_dyn(cs, N2, s.m2, r.t[0], w1);
+              axis_weights_dyn(cs, N2, s.m2, r.t[1], w2);
+              axis_weights_dyn(cs, N2, s.m2, r.t[2], w3);
+            }
+            const T *qv = qs + (int64_t)sl * ncomp;
+            const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
+            const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
+            const int lxb = ex - (N2 - 1);
+  #pragma unroll 1
+            for (int k = kz0; k < kz1; ++k) {
+              const int lz = ez + k - (N2 - 1);
+              const double wz = (double)pick_t(w3, k) * S;
+  #pragma unroll 1
+              for (int j = ky0; j < ky1; ++j) {
+                const int ly = ey + j - (N2 - 1);
+                const double wyz = (double)pick_t(w2, j) * wz;
+                const int row = (lz * B1 + ly) * B0;
+  #pragma unroll
+                for (int i = 0; i < N2; ++i) {
+                  const int lx = lxb + i;
+                  if (lx < 0 || lx >= vx) continue;
+                  const double w = (double)w1[i] * wyz;
+                  for (int c = 0; c < ncomp; ++c) {
+                    const double h = fma(w, (double)__ldg(qv + c), magic);
+                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)__double_as_longlong(h));
+                  }
+                }
+              }
+            }
           }
-          const T *qv = qs + (int64_t)sl * ncomp;
-          const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
-          const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
-          const int lxb = ex - (N2 - 1);
-#pragma unroll 1
-          for (int k = kz0; k < kz1; ++k) {
-            const int lz = ez + k - (N2 - 1);
-            const double wz = (double)pick_t(w3, k) * S;
-#pragma unroll 1
-            for (int j = ky0; j < ky1; ++j) {
-              const int ly = ey + j - (N2 - 1);
-              const double wyz = (double)pick_t(w2, j) * wz;
-              const int row = (lz * B1 + ly) * B0;
-#pragma unroll
-              for (int i = 0; i < N2; ++i) {
-                const int lx = lxb + i;
-                if (lx < 0 || lx >= vx) continue;
-                const double w = (double)w1[i] * wyz;
+        } else {
+          // a warp per point: its lanes cover the nodes of the point's stencil that lie in
+          // the brick (the sub-box i0..i1 x j0..j1 x k0..k1), so every lane of every atomic
+          // does work; lanes 0..3*N2-1 evaluate one axis weight each, and each node's three
+          // weights arrive by shuffle.  The weight products are formed in the same order as
+          // in the gather (wz * S first, then wy, then wx).
+          for (uint32_t t = c0 + warp; t < c1; t += nwarps) {
+            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
+            const int i0 = max(0, N2 - 1 - ex), i1 = min(N2, vx + N2 - 1 - ex);
+            const int j0 = max(0, N2 - 1 - ey), j1 = min(N2, vy + N2 - 1 - ey);
+            const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
+            const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
+            if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
+            const RecT<T> r = rec[sl];
+            T wl = T(0);
+            if (lane < 3 * N2) {
+              const int a = lane / N2, q = lane - a * N2;
+              const T tt = a == 0 ? r.t[0] : (a == 1 ? r.t[1] : r.t[2]);
+              wl = cs[q + N2 * (m2 - 1)];
+              for (int p = m2 - 2; p >= 0; --p) wl = add_rn(mul_rn(wl, tt), cs[q + N2 * p]);
+            }
+            const T *qv = qs + (int64_t)sl * ncomp;
+            const int count = nx * ny * nz;
+            // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
+            const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
+            const int node0 = ((ez - (N2 - 1)) * B1 + ey - (N2 - 1)) * B0 + ex - (N2 - 1);
+            for (int base = 0; base < count; base += 32) {
+              const int idx = base + lane;
+              const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
+              const int kk = (int)(((uint32_t)r1 * rny) >> 16), jj = r1 - kk * ny;
+              const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
+              const T wxi = __shfl_sync(0xffffffffu, wl, i);
+              const T wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
+              const T wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
+              if (idx < count) {
+                const double wz = (double)wzk * S;
+                const double wyz = (double)wyj * wz;
+                const double w = (double)wxi * wyz;
+                const int node = node0 + (k * B1 + j) * B0 + i;
                 for (int c = 0; c < ncomp; ++c) {
                   const double h = fma(w, (double)__ldg(qv + c), magic);
-                  atomicAdd(acc + c * bvol + row + lx, (unsigned long long)__double_as_longlong(h));
+                  atomicAdd(acc + c * bvol + node, (unsigned long long)__double_as_longlong(h));
                 }
               }
             }

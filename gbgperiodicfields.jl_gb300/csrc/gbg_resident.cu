@@ -220,10 +220,71 @@ __device__ __forceinline__ bool split32(float x, float o, float d, int64_t n, in
   return ok;
 }
 
+// ------------------------------------------------------------ displacement
+//
+// Points.jl:1217-1231, 1382-1490 -- displace!(dst, src, [grid,] (c_1, v_1), ...): per
+// coordinate dst = ((src + c_1 v_1) + c_2 v_2) + ..., every product and sum rounded in the
+// positions' type (the reference's broadcast fuses no multiply-add), then, on the torus,
+// _wrap_coordinate (Points.jl:1245-1249).
+
+template <typename T>
+struct DisplaceArgs {
+  const T *src;
+  T *dst;
+  const T *sec[GBG_MAX_TERMS];
+  T coef[GBG_MAX_TERMS];
+  int32_t nterms, wrap;
+  T extent[3], origin[3];
+};
+
+// Julia's floating-point mod (rem, then the sign moved toward the divisor).
+template <typename T>
+__device__ __forceinline__ T jl_mod(T x, T y) {
+  const T r = fmod(x, y);
+  if (r == T(0)) return copysign(r, y);
+  if ((r > T(0)) != (y > T(0))) return r + y;
+  return r;
+}
+
+// The excluded endpoint is folded by an equality test, so a non-finite coordinate stays
+// non-finite (an infinity becomes NaN, mod's own image of it).
+template <typename T>
+__device__ __forceinline__ T wrap_coordinate(T x, T extent, T origin) {
+  T off = jl_mod(x - origin, extent);
+  off = off == extent ? T(0) : off;
+  return off + origin;
+}
+
+template <typename T>
+__device__ __forceinline__ T displaced(const DisplaceArgs<T> &a, int64_t i, int d) {
+  T x = a.src[i];
+  for (int j = 0; j < a.nterms; ++j) x = add_rn(x, mul_rn(a.coef[j], a.sec[j][i]));
+  return a.wrap ? wrap_coordinate(x, a.extent[d], a.origin[d]) : x;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_displace(DisplaceArgs<T> a, int64_t m) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < 3 * m; i += (int64_t)gridDim.x * blockDim.x)
+    a.dst[i] = displaced(a, i, (int)(i / m));
+}
+
+// dst[s + m*c] = src[perm[s] + m*c]: an (m, ncols) column-major array in binned order.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
+    k_permute(const T *__restrict__ src, T *__restrict__ dst, const uint32_t *__restrict__ perm, int64_t m, int ncols) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m * ncols; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = i / m, s = i - c * m;
+    dst[i] = src[__ldg(perm + s) + m * c];
+  }
+}
+
+// Keys, counts and per-point records of the bins; with DISP the positions are first
+// displaced (and wrapped) from `disp`, written to disp.dst, and binned in the same pass.
+template <typename T, bool DISP = false>
+__global__ void __launch_bounds__(kThreads)
     k_bin_keys(BinGeom g, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
-               uint32_t *__restrict__ counts, float4 *__restrict__ rec_user, int32_t *status) {
+               uint32_t *__restrict__ counts, float4 *__restrict__ rec_user, int32_t *status,
+               DisplaceArgs<T> disp = {}) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t c[3];
@@ -231,10 +292,17 @@ __global__ void __launch_bounds__(kThreads)
     bool ok = true;
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
+      T x;
+      if constexpr (DISP) {
+        x = displaced(disp, p + m * d, d);
+        disp.dst[p + m * d] = x;
+      } else {
+        x = pos[p + m * d];
+      }
       if constexpr (sizeof(T) == 8)
-        ok &= split64((double)pos[p + m * d], g.scale[d], g.shift[d], g.n[d], c[d], t[d]);
+        ok &= split64((double)x, g.scale[d], g.shift[d], g.n[d], c[d], t[d]);
       else
-        ok &= split32((float)pos[p + m * d], g.o32[d], g.d32[d], g.n[d], c[d], t[d]);
+        ok &= split32((float)x, g.o32[d], g.d32[d], g.n[d], c[d], t[d]);
     }
     if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
     const int64_t bx = c[0] / g.b[0], by = c[1] / g.b[1], bz = c[2] / g.b[2];
@@ -683,8 +751,9 @@ size_t scatter32_smem(const FixGeo &g, int cp) {
          sizeof(uint32_t) * (size_t)(g.e[0] + g.e[1] + g.e[2]) + sizeof(uint32_t) * (size_t)(g.bvol + 1);
 }
 
-// The scatter of one brick: list the region's points, give each thread a point, and add
-// its contributions to the brick's fixed-point accumulators; then write every node once.
+// The scatter of one brick: list the region's points, give each warp a point (its lanes
+// cover the point's nodes in the brick), and add its contributions to the brick's
+// fixed-point accumulators; then write every node once.
 // All index arithmetic is 32-bit and division-free inside the loops: the region's cell
 // keys come from three per-axis tables (key = kx[ex] + ky[ey] + kz[ez]) and each thread
 // steps its (ex, ey, ez) incrementally.
@@ -832,50 +901,105 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
           }
         }
         __syncthreads();
-        for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
-          const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
-          const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-          const float4 r = __ldg(rec + sl);
-          float wx[N2], wy[N2], wz[N2];
-          if constexpr (FIXED) {
-            weights_ptr<N2>(coef, r.x, wx);
-            weights_ptr<N2>(coef, r.y, wy);
-            weights_ptr<N2>(coef, r.z, wz);
-          } else {
-            weights_rt<N2>(coef, m2, r.x, wx);
-            weights_rt<N2>(coef, m2, r.y, wy);
-            weights_rt<N2>(coef, m2, r.z, wz);
+        if constexpr (N2 <= 4) {
+          // stencils of up to 64 nodes: a thread per point
+          for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
+            const float4 r = __ldg(rec + sl);
+            float wx[N2], wy[N2], wz[N2];
+            if constexpr (FIXED) {
+              weights_ptr<N2>(coef, r.x, wx);
+              weights_ptr<N2>(coef, r.y, wy);
+              weights_ptr<N2>(coef, r.z, wz);
+            } else {
+              weights_rt<N2>(coef, m2, r.x, wx);
+              weights_rt<N2>(coef, m2, r.y, wy);
+              weights_rt<N2>(coef, m2, r.z, wz);
+            }
+            float q[CP];
+            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+  #pragma unroll
+            for (int v = 0; v < CP / 4; ++v) {
+              const float4 tq = __ldg(q4 + v);
+              q[4 * v] = tq.x;
+              q[4 * v + 1] = tq.y;
+              q[4 * v + 2] = tq.z;
+              q[4 * v + 3] = tq.w;
+            }
+            // node l = e + k - (N2 - 1) along each axis; the k that land inside the brick
+            const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
+            const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
+            const int lx0 = ex - (N2 - 1);
+  #pragma unroll 1
+            for (int k = kz0; k < kz1; ++k) {
+              const int lz = ez + k - (N2 - 1);
+              const float wzk = pick(wz, k) * S1;
+  #pragma unroll 1
+              for (int j = ky0; j < ky1; ++j) {
+                const int ly = ey + j - (N2 - 1);
+                const float wyz = pick(wy, j) * wzk;
+                const int row = (lz * g.b[1] + ly) * g.b[0];
+  #pragma unroll
+                for (int i = 0; i < N2; ++i) {
+                  const int lx = lx0 + i;
+                  if (lx < 0 || lx >= vx) continue;
+                  const float w = wx[i] * wyz;
+  #pragma unroll
+                  for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + row + lx, w, q[c], LS);
+                }
+              }
+            }
           }
-          float q[CP];
-          const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
-#pragma unroll
-          for (int v = 0; v < CP / 4; ++v) {
-            const float4 tq = __ldg(q4 + v);
-            q[4 * v] = tq.x;
-            q[4 * v + 1] = tq.y;
-            q[4 * v + 2] = tq.z;
-            q[4 * v + 3] = tq.w;
-          }
-          // node l = e + k - (N2 - 1) along each axis; the k that land inside the brick
-          const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
-          const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
-          const int lx0 = ex - (N2 - 1);
-#pragma unroll 1
-          for (int k = kz0; k < kz1; ++k) {
-            const int lz = ez + k - (N2 - 1);
-            const float wzk = pick(wz, k) * S1;
-#pragma unroll 1
-            for (int j = ky0; j < ky1; ++j) {
-              const int ly = ey + j - (N2 - 1);
-              const float wyz = pick(wy, j) * wzk;
-              const int row = (lz * g.b[1] + ly) * g.b[0];
-#pragma unroll
-              for (int i = 0; i < N2; ++i) {
-                const int lx = lx0 + i;
-                if (lx < 0 || lx >= vx) continue;
-                const float w = wx[i] * wyz;
-#pragma unroll
-                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + row + lx, w, q[c], LS);
+        } else {
+          // a warp per point: its lanes cover the point's nodes inside the brick (the sub-box
+          // i0..i1 x j0..j1 x k0..k1); lanes 0..3*N2-1 evaluate one axis weight each and each
+          // node's three weights arrive by shuffle (product order wz*S1, *wy, *wx)
+          const int lane = (int)threadIdx.x & 31;
+          for (uint32_t t = c0 + (threadIdx.x >> 5); t < c1; t += (blockDim.x >> 5)) {
+            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
+            const int i0 = max(0, N2 - 1 - ex), i1 = min(N2, vx + N2 - 1 - ex);
+            const int j0 = max(0, N2 - 1 - ey), j1 = min(N2, vy + N2 - 1 - ey);
+            const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
+            const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
+            if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
+            const float4 r = __ldg(rec + sl);
+            float wl = 0.0f;
+            if (lane < 3 * N2) {
+              const int a = lane / N2, qn = lane - a * N2;
+              const float tt = a == 0 ? r.x : (a == 1 ? r.y : r.z);
+              const int mm = FIXED ? N2 : m2;
+              wl = coef[qn + N2 * (mm - 1)];
+              for (int p = mm - 2; p >= 0; --p) wl = fmaf(wl, tt, coef[qn + N2 * p]);
+            }
+            float q[CP];
+            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+  #pragma unroll
+            for (int v = 0; v < CP / 4; ++v) {
+              const float4 tq = __ldg(q4 + v);
+              q[4 * v] = tq.x;
+              q[4 * v + 1] = tq.y;
+              q[4 * v + 2] = tq.z;
+              q[4 * v + 3] = tq.w;
+            }
+            const int count = nx * ny * nz;
+            // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
+            const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
+            const int node0 = ((ez - (N2 - 1)) * B1 + ey - (N2 - 1)) * B0 + ex - (N2 - 1);
+            for (int base = 0; base < count; base += 32) {
+              const int idx = base + lane;
+              const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
+              const int kk = (int)(((uint32_t)r1 * rny) >> 16), jj = r1 - kk * ny;
+              const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
+              const float wxi = __shfl_sync(0xffffffffu, wl, i);
+              const float wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
+              const float wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
+              if (idx < count) {
+                const float w = wxi * (wyj * (wzk * S1));
+                const int node = node0 + (k * B1 + j) * B0 + i;
+  #pragma unroll
+                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + node, w, q[c], LS);
               }
             }
           }
@@ -1571,14 +1695,40 @@ gbg_status gbg_bins_destroy(gbg_bins b) {
   return GBG_OK;
 }
 
-gbg_status gbg_bins_build(gbg_bins b, gbg_dtype pos_dtype, const void *positions, int64_t npoints,
-                          int32_t *device_status, void *stream) {
-  clear_error();
-  if (!b) return set_error(GBG_EARG, "null bins");
-  if (npoints < 0 || npoints > b->max_points) return set_error(GBG_EDIM, "more points than the bins hold");
-  if (pos_dtype != GBG_F32 && pos_dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
-  if (npoints > 0 && !positions) return set_error(GBG_EARG, "null positions");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
+}  // extern "C"
+
+namespace gbg {
+namespace {
+
+// Fills the displacement arguments (C ABI terms converted to the positions' type).
+template <typename T>
+gbg_status make_displace(DisplaceArgs<T> &a, const gbg_grid *grid, T *dst, const T *src, int32_t nterms,
+                         const double *coefficients, const void *const *sections) {
+  if (nterms < 0 || nterms > GBG_MAX_TERMS)
+    return set_error(GBG_EUNSUPPORTED, "displacement: 0.." + std::to_string(GBG_MAX_TERMS) + " terms per call");
+  if (nterms > 0 && (!coefficients || !sections)) return set_error(GBG_EARG, "null displacement terms");
+  a = DisplaceArgs<T>{};
+  a.src = src;
+  a.dst = dst;
+  a.nterms = nterms;
+  for (int j = 0; j < nterms; ++j) {
+    if (!sections[j]) return set_error(GBG_EARG, "null displacement section");
+    a.sec[j] = static_cast<const T *>(sections[j]);
+    a.coef[j] = T(coefficients[j]);
+  }
+  a.wrap = grid != nullptr;
+  for (int d = 0; d < 3; ++d) {
+    a.extent[d] = grid ? T(grid->domain[d]) : T(1);
+    a.origin[d] = grid ? T(grid->origin[d]) : T(0);
+    if (grid && !(a.extent[d] > T(0) && isfinite((double)a.extent[d]) && isfinite((double)a.origin[d])))
+      return set_error(GBG_EARG, "displacement: the domain must be finite and positive");
+  }
+  return GBG_OK;
+}
+
+template <typename T>
+gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, int32_t *device_status,
+                           cudaStream_t st, const DisplaceArgs<T> *disp) {
   b->npoints = npoints;
   GBG_CUDA_TRY(cudaMemsetAsync(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1), st));
   if (npoints == 0) return GBG_OK;
@@ -1595,12 +1745,12 @@ gbg_status gbg_bins_build(gbg_bins b, gbg_dtype pos_dtype, const void *positions
   }
   g.bvol = b->bvol;
   const int blocks = launch_blocks(npoints, kThreads);
-  if (pos_dtype == GBG_F64)
-    k_bin_keys<double><<<blocks, kThreads, 0, st>>>(g, static_cast<const double *>(positions), npoints, b->keys,
-                                                    b->cell_start, b->rec_user, device_status);
+  if (disp)
+    k_bin_keys<T, true><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->rec_user,
+                                                     device_status, *disp);
   else
-    k_bin_keys<float><<<blocks, kThreads, 0, st>>>(g, static_cast<const float *>(positions), npoints, b->keys,
-                                                   b->cell_start, b->rec_user, device_status);
+    k_bin_keys<T, false><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->rec_user,
+                                                      device_status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   int bits = 0;
@@ -1611,6 +1761,86 @@ gbg_status gbg_bins_build(gbg_bins b, gbg_dtype pos_dtype, const void *positions
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
+}
+
+}  // namespace
+}  // namespace gbg
+
+extern "C" {
+
+gbg_status gbg_points_displace(const gbg_grid *grid, gbg_dtype dtype, void *dst, const void *src, int64_t npoints,
+                               int32_t nterms, const double *coefficients, const void *const *sections,
+                               void *stream) {
+  clear_error();
+  if (dtype != GBG_F32 && dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
+  if (npoints < 0) return set_error(GBG_EDIM, "negative point count");
+  if (npoints > 0 && (!dst || !src)) return set_error(GBG_EARG, "null positions");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto go = [&](auto *tag) -> gbg_status {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    DisplaceArgs<T> a;
+    GBG_TRY(make_displace<T>(a, grid, static_cast<T *>(dst), static_cast<const T *>(src), nterms, coefficients,
+                             sections));
+    if (npoints == 0) return GBG_OK;
+    k_displace<T><<<launch_blocks(3 * npoints, kThreads), kThreads, 0, st>>>(a, npoints);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+  };
+  return dtype == GBG_F64 ? go((double *)nullptr) : go((float *)nullptr);
+}
+
+gbg_status gbg_bins_build_displaced(gbg_bins b, gbg_dtype dtype, void *dst, const void *src, int64_t npoints,
+                                    int32_t nterms, const double *coefficients, const void *const *sections,
+                                    int32_t wrap, int32_t *device_status, void *stream) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  if (npoints < 0 || npoints > b->max_points) return set_error(GBG_EDIM, "more points than the bins hold");
+  if (dtype != GBG_F32 && dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
+  if (npoints > 0 && (!dst || !src)) return set_error(GBG_EARG, "null positions");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  auto go = [&](auto *tag) -> gbg_status {
+    using T = std::remove_pointer_t<decltype(tag)>;
+    DisplaceArgs<T> a;
+    GBG_TRY(make_displace<T>(a, wrap ? &b->grid : nullptr, static_cast<T *>(dst), static_cast<const T *>(src), nterms,
+                             coefficients, sections));
+    return bins_build_impl<T>(b, static_cast<const T *>(dst), npoints, device_status, st, &a);
+  };
+  return dtype == GBG_F64 ? go((double *)nullptr) : go((float *)nullptr);
+}
+
+gbg_status gbg_bins_permute(gbg_bins b, gbg_dtype dtype, int32_t ncols, const void *src, void *dst, void *stream) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  if (dtype != GBG_F32 && dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
+  if (ncols < 1) return set_error(GBG_EARG, "ncols must be positive");
+  if (b->npoints == 0) return GBG_OK;
+  if (!src || !dst || src == dst) return set_error(GBG_EARG, "permute needs distinct source and destination");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int64_t m = b->npoints;
+  const int blocks = launch_blocks(m * ncols, kThreads);
+  if (dtype == GBG_F64)
+    k_permute<double><<<blocks, kThreads, 0, st>>>(static_cast<const double *>(src), static_cast<double *>(dst), b->perm,
+                                                   m, ncols);
+  else
+    k_permute<float><<<blocks, kThreads, 0, st>>>(static_cast<const float *>(src), static_cast<float *>(dst), b->perm,
+                                                  m, ncols);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
+gbg_status gbg_bins_build(gbg_bins b, gbg_dtype pos_dtype, const void *positions, int64_t npoints,
+                          int32_t *device_status, void *stream) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  if (npoints < 0 || npoints > b->max_points) return set_error(GBG_EDIM, "more points than the bins hold");
+  if (pos_dtype != GBG_F32 && pos_dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
+  if (npoints > 0 && !positions) return set_error(GBG_EARG, "null positions");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (pos_dtype == GBG_F64)
+    return bins_build_impl<double>(b, static_cast<const double *>(positions), npoints, device_status, st, nullptr);
+  return bins_build_impl<float>(b, static_cast<const float *>(positions), npoints, device_status, st, nullptr);
 }
 
 gbg_status gbg_bins_order(gbg_bins b, int32_t *order, void *stream) {

@@ -98,6 +98,38 @@ class PointBins:
         self.gather_threads, self.scatter_threads = int(gather_threads), int(scatter_threads)
         return self
 
+    def build_displaced(self, dst: torch.Tensor, src: torch.Tensor, terms=(), wrap: bool = True,
+                        status: torch.Tensor | None = None):
+        """Move the points (dst = src + sum c_j v_j, wrapped onto the grid's box when wrap)
+        and bin the moved points in the same pass (gbg_bins_build_displaced).  dst may be
+        src; terms are (coefficient, (M, 3) tensor) pairs of the positions' dtype."""
+        import ctypes
+        src = colmajor(src)
+        if not dst.is_cuda or dst.dtype != src.dtype or tuple(dst.shape) != tuple(src.shape):
+            raise _lib.ArgumentError("dst must be a CUDA tensor shaped and typed like src")
+        secs = [colmajor(v) for _, v in terms]
+        if any(v.dtype != src.dtype or tuple(v.shape) != tuple(src.shape) for v in secs):
+            raise _lib.ArgumentError("displacement sections must be (M, 3) tensors of the positions' dtype")
+        carr = (ctypes.c_double * max(1, len(secs)))(*[float(c) for c, _ in terms])
+        parr = (ctypes.c_void_p * max(1, len(secs)))(*[v.data_ptr() for v in secs])
+        self.npoints = int(src.shape[0])
+        self.status = status
+        self._keep = secs
+        _lib.check(_lib.load().gbg_bins_build_displaced(
+            self.handle, _DTYPE_CODE[src.dtype], dst.data_ptr(), src.data_ptr(), self.npoints, len(secs), carr, parr,
+            int(bool(wrap)), status.data_ptr() if status is not None else None, _stream()), "gbg_bins_build_displaced")
+        return self
+
+    def permute(self, src: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """An (M, ncols) array copied into the bins' sorted order (gbg_bins_permute)."""
+        src = colmajor(src)
+        two = src if src.dim() == 2 else src.reshape(src.shape[0], -1)
+        if out is None:
+            out = empty_colmajor(tuple(src.shape), src.dtype, src.device)
+        _lib.check(_lib.load().gbg_bins_permute(self.handle, _DTYPE_CODE[src.dtype], int(two.shape[1]), src.data_ptr(),
+                                                out.data_ptr(), _stream()), "gbg_bins_permute")
+        return out
+
     def order(self) -> torch.Tensor:
         o = torch.empty(self.npoints, dtype=torch.int32, device="cuda")
         _lib.check(_lib.load().gbg_bins_order(self.handle, o.data_ptr(), _stream()), "gbg_bins_order")

@@ -213,6 +213,30 @@ gbg_status gbg_field_bytes(gbg_field field, size_t *bytes);
 gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32_t *brick,
                            gbg_bins *out);
 gbg_status gbg_bins_destroy(gbg_bins bins);
+/* ---------------------------------------------------------- displacement
+ * Points.jl:1382-1440 (displace!) and 1481-1490 (wrap!): per coordinate
+ * dst = ((src + c_1 v_1) + c_2 v_2) + ... in the positions' type, every product and sum
+ * rounded separately as the reference's broadcast does, then, with a grid (or wrap != 0),
+ * reduced to [origin, origin + domain) by _wrap_coordinate (Points.jl:1245-1249: the
+ * excluded endpoint folded to the origin, non-finite coordinates left non-finite).
+ * Positions and the nterms sections are device (M, 3) column-major arrays of dtype; the
+ * coefficients are host doubles converted to dtype; dst may equal src.  nterms = 0 with a
+ * grid is wrap!. */
+#define GBG_MAX_TERMS 32
+gbg_status gbg_points_displace(const gbg_grid *grid /* NULL: no wrap */, gbg_dtype dtype, void *dst, const void *src,
+                               int64_t npoints, int32_t nterms, const double *coefficients,
+                               const void *const *sections, void *stream);
+/* The displacement fused with the bins build: the moved (and, with wrap != 0, wrapped)
+ * positions are written to dst and binned in the same pass over the points, which keeps a
+ * particle loop's points binned from step to step without a second read of the positions. */
+gbg_status gbg_bins_build_displaced(gbg_bins bins, gbg_dtype dtype, void *dst, const void *src, int64_t npoints,
+                                    int32_t nterms, const double *coefficients, const void *const *sections,
+                                    int32_t wrap, int32_t *device_status, void *stream);
+/* Copies an (M, ncols) column-major array into the bins' sorted order
+ * (dst[s + M*c] = src[perm[s] + M*c]); applied to the positions and every per-point array
+ * it keeps the particle state in binned order.  src and dst must differ. */
+gbg_status gbg_bins_permute(gbg_bins bins, gbg_dtype dtype, int32_t ncols, const void *src, void *dst,
+                            void *stream);
 /* Threads per CTA of the binned gather (0 = default, 128, 256 or 512) and scatter
  * (0 = default, 64, 128 or 256) launched on these bins: the autotuner's knobs beside
  * the brick edges.  Each CTA works through whole bricks; the grid is sized from the

@@ -485,3 +485,33 @@ float gbgo_wrap_coordinate_f32(float coordinate, float extent, float origin) {
   offset = (offset == extent) ? 0.0f : offset;
   return offset + origin;
 }
+
+/* Points.jl:1217-1231, 1382-1440 -- displace!(dst, src, [grid,] (c_1, v_1), ..., (c_K, v_K)):
+ * per coordinate dst = (((src + c_1 v_1) + c_2 v_2) + ...), each product and sum rounded
+ * in the positions' type (Julia's broadcast fuses no multiply-add; coefficients converted
+ * to that type first), then, with wrap, _wrap_coordinate with the axis's extent and origin.
+ * All arrays (M, 3) column-major; dst may be src. */
+void gbgo_displace_f64(double *dst, const double *src, int64_t m, int32_t nterms, const double *coefficients,
+                       const double *const *sections, int32_t wrap, const double *extent, const double *origin) {
+  for (int a = 0; a < 3; ++a)
+    for (int64_t p = 0; p < m; ++p) {
+      double x = src[p + m * a];
+      for (int32_t j = 0; j < nterms; ++j) {
+        const double prod = coefficients[j] * sections[j][p + m * a];
+        x = x + prod;
+      }
+      dst[p + m * a] = wrap ? gbgo_wrap_coordinate_f64(x, extent[a], origin[a]) : x;
+    }
+}
+void gbgo_displace_f32(float *dst, const float *src, int64_t m, int32_t nterms, const double *coefficients,
+                       const float *const *sections, int32_t wrap, const double *extent, const double *origin) {
+  for (int a = 0; a < 3; ++a)
+    for (int64_t p = 0; p < m; ++p) {
+      float x = src[p + m * a];
+      for (int32_t j = 0; j < nterms; ++j) {
+        const float prod = (float)coefficients[j] * sections[j][p + m * a];
+        x = x + prod;
+      }
+      dst[p + m * a] = wrap ? gbgo_wrap_coordinate_f32(x, (float)extent[a], (float)origin[a]) : x;
+    }
+}

@@ -121,6 +121,10 @@ int gbgo_traversal_order_f32(const int64_t *grid_n, const double *domain, const 
 /* Points.jl:1245-1249 -- periodic wrap of one coordinate. */
 double gbgo_wrap_coordinate_f64(double coordinate, double extent, double origin);
 float gbgo_wrap_coordinate_f32(float coordinate, float extent, float origin);
+void gbgo_displace_f64(double *dst, const double *src, int64_t m, int32_t nterms, const double *coefficients,
+                       const double *const *sections, int32_t wrap, const double *extent, const double *origin);
+void gbgo_displace_f32(float *dst, const float *src, int64_t m, int32_t nterms, const double *coefficients,
+                       const float *const *sections, int32_t wrap, const double *extent, const double *origin);
 
 /* Interpolation.jl:1000 + 1025-1027 -- the periodic walk: fills idx[0..width) with
  * mod(base - neighbourhood + t, extent) by the reference's wrapped-start + step rule. */

@@ -65,6 +65,10 @@ def lib():
         L.gbgo_wrap_coordinate_f64.restype = ctypes.c_double
         L.gbgo_wrap_coordinate_f32.argtypes = [ctypes.c_float] * 3
         L.gbgo_wrap_coordinate_f32.restype = ctypes.c_float
+        for suf, vp in (("f64", _dp), ("f32", _fp)):
+            fn = getattr(L, f"gbgo_displace_{suf}")
+            fn.argtypes = [vp, vp, ctypes.c_int64, ctypes.c_int32, _dp, ctypes.POINTER(vp), ctypes.c_int32, _dp, _dp]
+            fn.restype = None
         L.gbgo_walk.argtypes = [ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, _i64p]
         L.gbgo_walk.restype = None
         for suf, vp in (("f64", _dp), ("f32", _fp)):
@@ -234,6 +238,25 @@ def wrap_coordinate(coordinate, extent, origin, dtype=np.float64):
     if np.dtype(dtype) == np.float64:
         return lib().gbgo_wrap_coordinate_f64(coordinate, extent, origin)
     return lib().gbgo_wrap_coordinate_f32(coordinate, extent, origin)
+
+
+def displace(src, terms, grid=None):
+    """Points.jl displace!: src (M,3) plus sum_j c_j * v_j in order, wrapped when a grid dict
+    (with 'domain' and 'origin') is given.  Returns a new (M,3) column-major array."""
+    src = np.asfortranarray(src)
+    dt = src.dtype
+    m = src.shape[0]
+    dst = np.zeros_like(src, order="F")
+    secs = [np.asfortranarray(v, dtype=dt) for _, v in terms]
+    coefs = np.array([float(c) for c, _ in terms] or [0.0], dtype=np.float64)
+    ctype = ctypes.c_double if dt == np.float64 else ctypes.c_float
+    arr = (ctypes.POINTER(ctype) * max(1, len(secs)))(*[_ptr(v, ctype) for v in secs])
+    ext = np.array(grid["domain"] if grid else (1.0, 1.0, 1.0), dtype=np.float64)
+    org = np.array(grid["origin"] if grid else (0.0, 0.0, 0.0), dtype=np.float64)
+    fn = lib().gbgo_displace_f64 if dt == np.float64 else lib().gbgo_displace_f32
+    fn(_ptr(dst, ctype), _ptr(src, ctype), m, len(secs), _ptr(coefs, ctypes.c_double), arr,
+       1 if grid else 0, _ptr(ext, ctypes.c_double), _ptr(org, ctypes.c_double))
+    return dst
 
 
 def walk(base: int, neighbourhood: int, extent: int, width: int) -> np.ndarray:

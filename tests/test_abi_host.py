@@ -153,3 +153,32 @@ def test_autotune_heuristic_and_cache_keys(gbg, tmp_path, monkeypatch):
     k3 = autotune.key((64, 64, 64), 3, gbg.CatmullRom, 8 * 64 ** 3)
     assert len({k1, k2, k3}) == 3
     assert autotune.choose((64, 64, 64), 3, gbg.CatmullRom, 64 ** 3)["source"] == "heuristic"
+
+
+def test_displacement_refusals(gbg):
+    """test/displacement.jl:149-157: mixed precision and mismatched counts are refused
+    before any launch; the C ABI bounds the term count."""
+    M = 7
+    pts = gbg.PointSet(torch.rand((M, 3), dtype=torch.float64))
+    with pytest.raises(gbg.ArgumentError):
+        gbg.displace_(pts, (1.0, gbg.VectorPointValues(torch.rand((M, 3), dtype=torch.float32))))
+    with pytest.raises(gbg.DimensionMismatch):
+        gbg.displace_(pts, (1.0, gbg.VectorPointValues(torch.rand((M + 1, 3), dtype=torch.float64))))
+    with pytest.raises(gbg.DimensionMismatch):
+        gbg.displace_(pts, gbg.PointSet(torch.rand((M + 1, 3), dtype=torch.float64)))
+    g32 = gbg.Grid3D((8, 12, 16), (TWO_PI, 2 * TWO_PI, 3 * TWO_PI), dtype=torch.float32)
+    with pytest.raises(gbg.ArgumentError):
+        gbg.wrap_(pts, g32)
+    with pytest.raises(gbg.ArgumentError):
+        gbg.displace_(pts, (1j, gbg.VectorPointValues(torch.rand((M, 3), dtype=torch.float64))))
+    with pytest.raises(gbg.ArgumentError):  # host arrays: no CPU path
+        gbg.displace_(pts, (1.0, gbg.VectorPointValues(torch.rand((M, 3), dtype=torch.float64))))
+    lib = gbg._lib.load()
+    coefs = (ctypes.c_double * 33)()
+    secs = (ctypes.c_void_p * 33)(*([1] * 33))
+    assert lib.gbg_points_displace(None, 2, 1, 1, 10, 33, coefs, secs, None) == gbg._lib.GBG_EUNSUPPORTED
+    assert lib.gbg_points_displace(None, 2, 1, 1, 10, 1, coefs, None, None) == gbg._lib.GBG_EARG
+    bad = gbg.Grid3D((8, 8, 8), (TWO_PI,) * 3).c()
+    bad.domain[1] = -1.0
+    assert lib.gbg_points_displace(bad, 2, 1, 1, 10, 0, None, None, None) == gbg._lib.GBG_EARG
+    assert lib.gbg_points_displace(None, 2, 1, 1, 0, 0, None, None, None) == gbg._lib.GBG_OK
