@@ -325,12 +325,6 @@ struct BrickGeo {
 };
 
 template <typename T>
-struct alignas(16) RecT {
-  T t[3];
-  uint32_t loc;
-};
-
-template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_brick_keys(GridT<T> g, BrickGeo bg, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
                  uint32_t *__restrict__ counts, int32_t *status) {
@@ -354,12 +348,14 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-template <typename T>
+// Per point in sorted order: the three axes' stencil weights (w[axis*N2 + q], the
+// reference's Horner and roundings, evaluated once per point rather than once per brick
+// that the point reaches) and alpha*q; max|alpha q| for the fixed-point scale.
+template <typename T, int N2, int M2>
 __global__ void __launch_bounds__(kThreads)
-    k_brick_prep(GridT<T> g, BrickGeo bg, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
-                 int64_t m, const uint32_t *__restrict__ perm, T alpha, RecT<T> *__restrict__ rec,
+    k_brick_prep(GridT<T> g, SchemeT<T, N2> sch, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
+                 int64_t m, const uint32_t *__restrict__ perm, T alpha, T *__restrict__ wts,
                  T *__restrict__ qs, unsigned long long *__restrict__ qmax_bits) {
-  const int64_t n[3] = {g.nx, g.ny, g.nz};
   unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
@@ -367,14 +363,14 @@ __global__ void __launch_bounds__(kThreads)
     int64_t b[3];
     T t[3];
     const bool ok = locate3(g, pos, p, m, b, t);
-    int64_t local = 0;
+    T *wp = wts + sl * (3 * N2);
 #pragma unroll
-    for (int d = 2; d >= 0; --d) local = local * bg.b[d] + imod(b[d], n[d]) % bg.b[d];
-    RecT<T> r;
+    for (int d = 0; d < 3; ++d) {
+      T w[N2];
+      axis_weights_m<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) r.t[d] = ok ? t[d] : quiet_nan<T>();
-    r.loc = (uint32_t)local;
-    rec[sl] = r;
+      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = w[k];
+    }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
       qs[sl * ncomp + c] = v;
@@ -414,10 +410,10 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // K being the node's number of contributions.
 constexpr int kFlatChunk = 2048;
 
-template <typename T, int N2, bool FIXED>
+template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
-    k_scatter_fixed64(GridT<T> g, BrickGeo bg, SchemeT<T, N2> s, int ncomp,
-                      const uint32_t *__restrict__ cell_start, const RecT<T> *__restrict__ rec,
+    k_scatter_fixed64(GridT<T> g, BrickGeo bg, int ncomp,
+                      const uint32_t *__restrict__ cell_start, const T *__restrict__ wts,
                       const T *__restrict__ qs, const unsigned long long *__restrict__ qmax_bits, double l3,
                       T *__restrict__ field, T beta, int beta_zero, int32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -433,9 +429,6 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *kx = pxyz + kFlatChunk, *ky = kx + E0, *kz = ky + E1;             // per-axis key tables
   uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
   __shared__ uint32_t warp_tot[32];
-  __shared__ T cs[N2 * GBG_MAX_POWERS];
-  stage_coeffs(s, cs);
-  const int m2 = FIXED ? N2 : s.m2;
   const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5, nwarps = (int)blockDim.x >> 5;
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
@@ -552,21 +545,18 @@ __global__ void __launch_bounds__(kThreads)
           }
         }
         __syncthreads();
-        if constexpr (N2 <= 4) {
-          // stencils of up to 64 nodes: a thread per point
+        if constexpr (N2 <= 2) {
+          // two-node stencils: a thread per point
           for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
             const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
             const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-            const RecT<T> r = rec[sl];
+            const T *wp = wts + (int64_t)sl * (3 * N2);
             T w1[N2], w2[N2], w3[N2];
-            if constexpr (FIXED) {
-              axis_weights_m<T, N2, N2>(s, r.t[0], w1);
-              axis_weights_m<T, N2, N2>(s, r.t[1], w2);
-              axis_weights_m<T, N2, N2>(s, r.t[2], w3);
-            } else {
-              axis_weights_dyn(cs, N2, s.m2, r.t[0], w1);
-              axis_weights_dyn(cs, N2, s.m2, r.t[1], w2);
-              axis_weights_dyn(cs, N2, s.m2, r.t[2], w3);
+#pragma unroll
+            for (int k = 0; k < N2; ++k) {
+              w1[k] = wp[k];
+              w2[k] = wp[N2 + k];
+              w3[k] = wp[2 * N2 + k];
             }
             const T *qv = qs + (int64_t)sl * ncomp;
             const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
@@ -597,7 +587,7 @@ __global__ void __launch_bounds__(kThreads)
         } else {
           // a warp per point: its lanes cover the nodes of the point's stencil that lie in
           // the brick (the sub-box i0..i1 x j0..j1 x k0..k1), so every lane of every atomic
-          // does work; lanes 0..3*N2-1 evaluate one axis weight each, and each node's three
+          // does work; lanes 0..3*N2-1 load one axis weight each, and each node's three
           // weights arrive by shuffle.  The weight products are formed in the same order as
           // in the gather (wz * S first, then wy, then wx).
           for (uint32_t t = c0 + warp; t < c1; t += nwarps) {
@@ -608,14 +598,9 @@ __global__ void __launch_bounds__(kThreads)
             const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
             const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
             if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-            const RecT<T> r = rec[sl];
-            T wl = T(0);
-            if (lane < 3 * N2) {
-              const int a = lane / N2, q = lane - a * N2;
-              const T tt = a == 0 ? r.t[0] : (a == 1 ? r.t[1] : r.t[2]);
-              wl = cs[q + N2 * (m2 - 1)];
-              for (int p = m2 - 2; p >= 0; --p) wl = add_rn(mul_rn(wl, tt), cs[q + N2 * p]);
-            }
+            const T wl = lane < 3 * N2 ? wts[(int64_t)sl * (3 * N2) + lane] : T(0);
+            // the z weights carry the brick's scale S (a power of two: exact), once per point
+            const double wd = lane >= 2 * N2 && lane < 3 * N2 ? (double)wl * S : (double)wl;
             const T *qv = qs + (int64_t)sl * ncomp;
             const int count = nx * ny * nz;
             // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
@@ -626,13 +611,12 @@ __global__ void __launch_bounds__(kThreads)
               const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
               const int kk = (int)(((uint32_t)r1 * rny) >> 16), jj = r1 - kk * ny;
               const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
-              const T wxi = __shfl_sync(0xffffffffu, wl, i);
-              const T wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
-              const T wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
+              const double wxi = __shfl_sync(0xffffffffu, wd, i);
+              const double wyj = __shfl_sync(0xffffffffu, wd, N2 + j);
+              const double wzs = __shfl_sync(0xffffffffu, wd, 2 * N2 + k);  // wz * S
               if (idx < count) {
-                const double wz = (double)wzk * S;
-                const double wyz = (double)wyj * wz;
-                const double w = (double)wxi * wyz;
+                const double wyz = wyj * wzs;
+                const double w = wxi * wyz;
                 const int node = node0 + (k * B1 + j) * B0 + i;
                 for (int c = 0; c < ncomp; ++c) {
                   const double h = fma(w, (double)__ldg(qv + c), magic);
@@ -828,7 +812,7 @@ ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncom
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  const size_t rec_bytes = P.bricked ? (esize == 8 ? sizeof(RecT<double>) : sizeof(RecT<float>)) : 3 * n2 * esize;
+  const size_t rec_bytes = 3 * (size_t)n2 * esize;  // the three axes' weights per point
   L.rec = a.take<char>((size_t)m * rec_bytes);
   L.qs = a.take<char>((size_t)m * ncomp * esize);
   L.qmax_bits = a.take<unsigned long long>(4);
@@ -843,9 +827,14 @@ int bits_for(uint64_t max_value) {
 
 template <typename T, int N2, bool FIXED>
 gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_scheme &sch, int ncomp,
-                          const ScatterLayout &L, T *field, double beta, int32_t *status, cudaStream_t st) {
+                          const T *x, const T *q, int64_t m, double alpha, const ScatterLayout &L, T *field,
+                          double beta, int32_t *status, cudaStream_t st) {
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
-  auto kernel = k_scatter_fixed64<T, N2, FIXED>;
+  k_brick_prep<T, N2, FIXED ? N2 : 0><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
+      g, s, ncomp, x, q, m, L.perm, T(alpha), static_cast<T *>(L.rec), static_cast<T *>(L.qs), L.qmax_bits);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  auto kernel = k_scatter_fixed64<T, N2>;
   GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
   const int64_t nbricks = P.bg.nb[0] * P.bg.nb[1] * P.bg.nb[2];
   int dev = 0, sms = 1, per_sm = 1;
@@ -854,7 +843,7 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, P.smem);
   const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
   const double L3 = std::pow(weight_bound(sch, std::ldexp(1.0, -40)), 3);
-  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, s, ncomp, L.counts, static_cast<const RecT<T> *>(L.rec),
+  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, ncomp, L.counts, static_cast<const T *>(L.rec),
                                            static_cast<const T *>(L.qs), L.qmax_bits, L3, field, T(beta),
                                            beta == 0.0, status);
   note_launch();
@@ -877,21 +866,17 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
     GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
     GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
     GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
-    k_brick_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, ncomp, x, static_cast<const T *>(q), m,
-                                                                     L.perm, T(alpha), static_cast<RecT<T> *>(L.rec),
-                                                                     static_cast<T *>(L.qs), L.qmax_bits);
-    note_launch();
-    GBG_CUDA_TRY(cudaGetLastError());
+    const T *qq = static_cast<const T *>(q);
     const int w = sch.stencil_width;
     const bool fixed = sch.num_powers == w;
-    if (w == 2) return fixed ? launch_bricked<T, 2, true>(g, P, sch, ncomp, L, f, beta, status, st)
-                             : launch_bricked<T, 2, false>(g, P, sch, ncomp, L, f, beta, status, st);
-    if (w == 4) return fixed ? launch_bricked<T, 4, true>(g, P, sch, ncomp, L, f, beta, status, st)
-                             : launch_bricked<T, 4, false>(g, P, sch, ncomp, L, f, beta, status, st);
-    if (w == 6) return fixed ? launch_bricked<T, 6, true>(g, P, sch, ncomp, L, f, beta, status, st)
-                             : launch_bricked<T, 6, false>(g, P, sch, ncomp, L, f, beta, status, st);
-    return fixed ? launch_bricked<T, 8, true>(g, P, sch, ncomp, L, f, beta, status, st)
-                 : launch_bricked<T, 8, false>(g, P, sch, ncomp, L, f, beta, status, st);
+#define GBG_BRICKED(W)                                                                               \
+  return fixed ? launch_bricked<T, W, true>(g, P, sch, ncomp, x, qq, m, alpha, L, f, beta, status, st) \
+               : launch_bricked<T, W, false>(g, P, sch, ncomp, x, qq, m, alpha, L, f, beta, status, st)
+    if (w == 2) GBG_BRICKED(2);
+    if (w == 4) GBG_BRICKED(4);
+    if (w == 6) GBG_BRICKED(6);
+    GBG_BRICKED(8);
+#undef GBG_BRICKED
   }
   const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
   const int64_t ncells = g.npf;

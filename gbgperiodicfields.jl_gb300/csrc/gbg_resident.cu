@@ -972,6 +972,7 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
               const int mm = FIXED ? N2 : m2;
               wl = coef[qn + N2 * (mm - 1)];
               for (int p = mm - 2; p >= 0; --p) wl = fmaf(wl, tt, coef[qn + N2 * p]);
+              if (a == 2) wl *= S1;  // the z weights carry the brick's scale (a power of two)
             }
             float q[CP];
             const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
@@ -994,9 +995,9 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
               const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
               const float wxi = __shfl_sync(0xffffffffu, wl, i);
               const float wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
-              const float wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
+              const float wzs = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);  // wz * S1
               if (idx < count) {
-                const float w = wxi * (wyj * (wzk * S1));
+                const float w = wxi * (wyj * wzs);
                 const int node = node0 + (k * B1 + j) * B0 + i;
   #pragma unroll
                 for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + node, w, q[c], LS);
@@ -1116,15 +1117,26 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
   // the copy's exact byte count (what the mbarrier expects) and the buffer stride
   const uint32_t box_bytes = (uint32_t)((size_t)f->cp * 4 * g.w[0] * g.w[1] * g.w[2]);
   const uint32_t tile_bytes = (box_bytes + 1023u) & ~1023u;
-  const int nbuf = (2 * (size_t)tile_bytes + 64 <= 200 * 1024) ? 2 : 1;
-  const size_t smem = (size_t)nbuf * tile_bytes + 64;
-  if (smem > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick halo tile does not fit in shared memory");
+  if ((size_t)tile_bytes + 64 > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick halo tile does not fit in shared memory");
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int32_t *status = nullptr;
   const int threads = b->gather_threads ? b->gather_threads : (N2 == 4 ? kGatherThreads : kThreads);
   auto go = [&](auto kernel) -> gbg_status {
+    // Double-buffer the tile when that leaves as many CTAs per SM as a single buffer
+    // would; otherwise (a large tile whose registers allow two CTAs) keep one buffer per
+    // CTA and let the second CTA overlap the first one's copy.
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, kernel);
+    const size_t smem_sm = 228 * 1024;
+    const int by_regs = std::max(1, 65536 / std::max(1, fa.numRegs * threads));
+    auto ctas = [&](int nb) {
+      const size_t sm = (size_t)nb * tile_bytes + 64 + 1024;  // + the block's static/reserved share
+      return std::min<int>(by_regs, (int)(smem_sm / sm));
+    };
+    const int nbuf = (2 * (size_t)tile_bytes + 64 <= 200 * 1024 && ctas(2) >= ctas(1)) ? 2 : 1;
+    const size_t smem = (size_t)nbuf * tile_bytes + 64;
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
