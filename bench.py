@@ -135,6 +135,35 @@ def peaks():
     return 6800.0, "fallback"
 
 
+# The main kernel of each timed call of the headline step.
+KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 3>", "gather_quintic": "k_gather_plain<double, 6, 3>",
+                "scatter_cubic": "k_scatter_fixed64<double, 4>", "scatter_quintic": "k_scatter_fixed64<double, 6>"}
+
+# DRAM bytes (read + write) per launch of those kernels on this workload, from one ncu capture
+# of dram__bytes_read.sum + dram__bytes_write.sum (one pass) on the full-size step.
+NCU_TRAFFIC: dict = {}
+
+
+def fp64_peak_tflops() -> float:
+    """FP64 throughput of this GPU, measured: the best of a few cuBLAS DGEMMs."""
+    import torch
+    n = 8192
+    a = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    b = torch.randn((n, n), dtype=torch.float64, device="cuda")
+    torch.mm(a, b)
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.mm(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    del a, b
+    return best
+
+
 def algorithmic_bytes(m: int, ncomp: int, n: int, s: int, beta_nonzero=False) -> dict:
     """Compulsory traffic per call: every input read once, every output written once."""
     gather = m * (3 * s + ncomp * s) + n * ncomp * s
@@ -180,27 +209,41 @@ def run_gb300(args, rank, world):
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
 
-    # per-call CUDA events on the launching stream
+    # per-call CUDA events on the launching stream, and per call the main kernel alone
+    # (gbg_set_kernel_timing_events: events recorded by the library around that kernel)
     timings = {"order": [], "gather_cubic": [], "scatter_cubic": [], "gather_quintic": [], "scatter_quintic": []}
+    kernel_times = {k: [] for k in timings if k != "order"}
+
+    def timed(kev, fn):
+        gbg._lib.check(lib.gbg_set_kernel_timing_events(kev[0].cuda_event, kev[1].cuda_event))
+        try:
+            fn()
+        finally:
+            lib.gbg_set_kernel_timing_events(None, None)
 
     def step(record):
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+        kev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for k in kernel_times}
+        for a, b in kev.values():  # the handles exist once recorded
+            a.record(stream)
+            b.record(stream)
         ev[0].record(stream)
         gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M_POINTS, 4,
                                                      order.data_ptr(), ws_order.data_ptr(), ws_order.numel(), sh))
         ev[1].record(stream)
         k = 2
         for name, s in (("cubic", cubic), ("quintic", quintic)):
-            gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, NCOMP, field.data_ptr(), pos.data_ptr(), M_POINTS,
-                                               order.data_ptr(), s.c(), out.data_ptr(), status.data_ptr(), sh))
+            timed(kev["gather_" + name], lambda: gbg._lib.check(lib.gbg_interpolate(
+                gC, gbg._lib.GBG_F64, NCOMP, field.data_ptr(), pos.data_ptr(), M_POINTS, order.data_ptr(), s.c(),
+                out.data_ptr(), status.data_ptr(), sh)))
             ev[k].record(stream)
-            gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, NCOMP, dep.data_ptr(), pos.data_ptr(), M_POINTS,
-                                               q.data_ptr(), None, s.c(), 1.0, 0.0, ws_scatter.data_ptr(),
-                                               ws_scatter.numel(), status.data_ptr(), sh))
+            timed(kev["scatter_" + name], lambda: gbg._lib.check(lib.gbg_anterpolate(
+                gC, gbg._lib.GBG_F64, NCOMP, dep.data_ptr(), pos.data_ptr(), M_POINTS, q.data_ptr(), None, s.c(),
+                1.0, 0.0, ws_scatter.data_ptr(), ws_scatter.numel(), status.data_ptr(), sh)))
             ev[k + 1].record(stream)
             k += 2
         if record is not None:
-            record.append(ev)
+            record.append((ev, kev))
 
     for _ in range(args.warmup):
         step(None)
@@ -222,10 +265,12 @@ def run_gb300(args, rank, world):
     clk = clocks.stop()
     launches = lib.gbg_kernel_launches() - launches0
     ms_total = start.elapsed_time(end)
-    for ev in evs:
+    for ev, kev in evs:
         names = list(timings)
         for i, nm in enumerate(names):
             timings[nm].append(ev[i].elapsed_time(ev[i + 1]))
+        for nm, (a, b) in kev.items():
+            kernel_times[nm].append(a.elapsed_time(b))
     if int(status.item()) != 0:
         raise RuntimeError(f"device status {int(status.item())}")
 
@@ -236,13 +281,20 @@ def run_gb300(args, rank, world):
     evals_per_step = 4 * M_POINTS
     value = world * evals_per_step * args.steps / (ms_total / 1e3)
 
-    # roofline of the dominant call (by measured time) against the HBM copy peak
+    # roofline of the dominant kernel (by its own event-timed duration): algorithmic bytes
+    # per launch against the HBM copy peak, and algorithmic FP64 flops (2 * width^3 * C per
+    # point) against the FP64 peak measured here with a cuBLAS DGEMM
     avg = {k: float(np.mean(v)) for k, v in timings.items()}
+    kavg = {k: float(np.mean(v)) for k, v in kernel_times.items()}
     peak, peak_kind = peaks()
     ab = algorithmic_bytes(M_POINTS, NCOMP, int(np.prod(N_GRID)), 8)
-    dominant = max(avg, key=avg.get)
-    dom_bytes = ab["scatter"] if dominant.startswith("scatter") else (ab["gather"] if dominant.startswith("gather") else M_POINTS * 28)
-    achieved = dom_bytes / (avg[dominant] / 1e3) / 1e9
+    dominant = max(kavg, key=kavg.get)
+    dom_bytes = ab["scatter"] if dominant.startswith("scatter") else ab["gather"]
+    achieved = dom_bytes / (kavg[dominant] / 1e3) / 1e9
+    width = 6 if dominant.endswith("quintic") else 4
+    dom_flops = 2 * width ** 3 * NCOMP * M_POINTS
+    fp64_peak = fp64_peak_tflops()
+    fp64_achieved = dom_flops / (kavg[dominant] / 1e3) / 1e12
 
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -252,9 +304,13 @@ def run_gb300(args, rank, world):
                    "schemes": ["CatmullRom", "LalescuSpline(6)"], "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (field 403 MB)"},
         "per_call_ms": avg,
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": None, "algorithmic_bytes": dom_bytes},
+        "kernel_ms": kavg,
+        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dominant], "call": dominant, "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": NCU_TRAFFIC.get(dominant), "algorithmic_bytes": dom_bytes,
+                     "fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                              "frac": fp64_achieved / fp64_peak, "algorithmic_flops": dom_flops,
+                              "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
@@ -339,6 +395,25 @@ def _time_ms(fn, reps=3):
     return best
 
 
+def _kernel_ms(lib, fn, reps=3):
+    """Minimum over reps of the library's main kernel alone (timing events recorded by the
+    library around it, on its stream)."""
+    import torch
+    best = float("inf")
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        b.record()
+        lib.gbg_set_kernel_timing_events(a.cuda_event, b.cuda_event)
+        try:
+            fn()
+        finally:
+            lib.gbg_set_kernel_timing_events(None, None)
+        torch.cuda.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
 def _rel_errors(got, want):
     """max and RMS of |got - want|, relative to max|want| and RMS(want)."""
     import torch
@@ -381,6 +456,8 @@ def precision_form(gbg, lib, dev, peak):
     t_bins = _time_ms(lambda: bins.build(pos))
     t_gather = _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out))
     t_scatter = _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
+    k_gather = _kernel_ms(lib, lambda: resident.interpolate_binned(field, bins, scheme, out=out))
+    k_scatter = _kernel_ms(lib, lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
     # the FP64 drop-in on the same inputs: reference values and the speed comparison
     gC = grid.c()
     sh = torch.cuda.current_stream().cuda_stream
@@ -405,13 +482,16 @@ def precision_form(gbg, lib, dev, peak):
                     "kept in binned order, cubic gather + scatter, bins rebuilt per step",
         "value": 2 * M / (step / 1e3), "unit": UNIT,
         "per_call_ms": {"bins": t_bins, "gather": t_gather, "scatter": t_scatter},
+        "kernel_ms": {"gather": k_gather, "scatter": k_scatter},
         "random_order_ms": random_order,
         "roofline": {
-            "gather": {"bound": "hbm", "achieved": alg["gather"] / (t_gather / 1e3) / 1e9, "peak": peak,
-                       "unit": "GB/s", "frac": alg["gather"] / (t_gather / 1e3) / 1e9 / peak,
+            "gather": {"bound": "hbm", "kernel": "k_gather_staged4<4, 12, float>",
+                       "achieved": alg["gather"] / (k_gather / 1e3) / 1e9, "peak": peak,
+                       "unit": "GB/s", "frac": alg["gather"] / (k_gather / 1e3) / 1e9 / peak,
                        "algorithmic_bytes": alg["gather"]},
-            "scatter": {"bound": "hbm", "achieved": alg["scatter"] / (t_scatter / 1e3) / 1e9, "peak": peak,
-                        "unit": "GB/s", "frac": alg["scatter"] / (t_scatter / 1e3) / 1e9 / peak,
+            "scatter": {"bound": "hbm", "kernel": "k_scatter_fixed<4, 1, 12>",
+                        "achieved": alg["scatter"] / (k_scatter / 1e3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "frac": alg["scatter"] / (k_scatter / 1e3) / 1e9 / peak,
                         "algorithmic_bytes": alg["scatter"]}},
         "error_vs_fp64": {"gather": err_g, "scatter": err_s},
         "plain_fp64_ms": t_plain, "speedup_vs_plain_fp64": t_plain / step,

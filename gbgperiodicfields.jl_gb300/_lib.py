@@ -113,6 +113,7 @@ SIGNATURES = {
     "gbg_status_string": (ctypes.c_char_p, [_I32]),
     "gbg_last_error": (ctypes.c_char_p, []),
     "gbg_kernel_launches": (ctypes.c_uint64, []),
+    "gbg_set_kernel_timing_events": (_I32, [_P, _P]),
     "gbg_scheme_lalescu": (_I32, [_I32, _I32, _SP]),
     "gbg_scheme_lagrange": (_I32, [_I32, _SP]),
     "gbg_scheme_custom": (_I32, [_I32, _I32, ctypes.POINTER(_D), _SP]),

@@ -9,6 +9,16 @@ namespace gbg {
 namespace {
 thread_local std::string g_last_error;
 std::atomic<uint64_t> g_launches{0};
+// Measurement hook: events recorded around the main kernel of a transfer call.
+thread_local cudaEvent_t g_main_start = nullptr, g_main_stop = nullptr;
+}
+
+void mark_main_start(cudaStream_t st) {
+  if (g_main_start) cudaEventRecord(g_main_start, st);
+}
+
+void mark_main_stop(cudaStream_t st) {
+  if (g_main_stop) cudaEventRecord(g_main_stop, st);
 }
 
 gbg_status set_error(gbg_status status, const std::string &message) {
@@ -83,5 +93,14 @@ const char *gbg_status_string(gbg_status status) {
 const char *gbg_last_error(void) { return gbg::g_last_error.c_str(); }
 
 uint64_t gbg_kernel_launches(void) { return gbg::g_launches.load(std::memory_order_relaxed); }
+
+gbg_status gbg_set_kernel_timing_events(void *start_event, void *stop_event) {
+  gbg::clear_error();
+  if ((start_event == nullptr) != (stop_event == nullptr))
+    return gbg::set_error(GBG_EARG, "give both events or neither");
+  gbg::g_main_start = static_cast<cudaEvent_t>(start_event);
+  gbg::g_main_stop = static_cast<cudaEvent_t>(stop_event);
+  return GBG_OK;
+}
 
 }  // extern "C"

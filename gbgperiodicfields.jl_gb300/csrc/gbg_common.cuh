@@ -21,6 +21,11 @@ void clear_error();
 // Counts kernel launches (gbg_kernel_launches); called next to every <<<...>>>.
 void note_launch(int n = 1);
 
+// Record the calling thread's timing events (gbg_set_kernel_timing_events), if any, just
+// before and just after the main kernel of a transfer, on that kernel's stream.
+void mark_main_start(cudaStream_t st);
+void mark_main_stop(cudaStream_t st);
+
 #define GBG_CUDA_TRY(expr)                                                                  \
   do {                                                                                      \
     cudaError_t _e = (expr);                                                                \

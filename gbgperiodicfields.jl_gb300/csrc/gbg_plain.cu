@@ -350,11 +350,12 @@ __global__ void __launch_bounds__(kThreads)
 
 // Per point in sorted order: the three axes' stencil weights (w[axis*N2 + q], the
 // reference's Horner and roundings, evaluated once per point rather than once per brick
-// that the point reaches) and alpha*q; max|alpha q| for the fixed-point scale.
+// that the point reaches) as 64-bit fixed point w * 2^wexp, and alpha*q; max|alpha q|
+// for the quantities' fixed-point scale.
 template <typename T, int N2, int M2>
 __global__ void __launch_bounds__(kThreads)
     k_brick_prep(GridT<T> g, SchemeT<T, N2> sch, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
-                 int64_t m, const uint32_t *__restrict__ perm, T alpha, T *__restrict__ wts,
+                 int64_t m, const uint32_t *__restrict__ perm, T alpha, int wexp, long long *__restrict__ wts,
                  T *__restrict__ qs, unsigned long long *__restrict__ qmax_bits) {
   unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
@@ -363,13 +364,14 @@ __global__ void __launch_bounds__(kThreads)
     int64_t b[3];
     T t[3];
     const bool ok = locate3(g, pos, p, m, b, t);
-    T *wp = wts + sl * (3 * N2);
+    long long *wp = wts + sl * (3 * N2);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T w[N2];
       axis_weights_m<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
+      // exact: a double times a power of two, then a 53-bit integer (|w| < 2^(62-wexp))
 #pragma unroll
-      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = w[k];
+      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = ok ? __double2ll_rn(ldexp((double)w[k], wexp)) : 0ll;
     }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
@@ -386,6 +388,20 @@ __global__ void __launch_bounds__(kThreads)
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
+// alpha*q as 64-bit fixed point q * 2^(62 - e), max|alpha q| < 2^e (one scale for all
+// points, known once the preparation pass has reduced the maximum).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_quantities_fixed(const T *__restrict__ qs, int64_t n, const unsigned long long *__restrict__ qmax_bits,
+                       long long *__restrict__ qi) {
+  const double qmax = __longlong_as_double((long long)*qmax_bits);
+  int e = 0;
+  frexp(qmax, &e);
+  const bool finite = isfinite(qmax);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    qi[i] = finite ? __double2ll_rn(ldexp((double)qs[i], 62 - e)) : 0ll;
+}
+
 template <int N, typename T>
 __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
   T v = w[0];
@@ -398,23 +414,24 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // The default scatter (deterministic, FP64-grade).  A CTA owns one brick of nodes.  It
 // lists the points of every cell whose stencil reaches the brick (the extended region),
 // gives each warp a point (its lanes cover the point's nodes inside the brick), and adds
-// every contribution w*alpha*q, scaled by a power of
-// two S and rounded once to an integer with the FP64 "magic number" 1.5*2^52 (one FMA),
-// to an int64 accumulator in shared memory.  Integer addition is associative, so the
-// result does not depend on which thread adds first, and no float atomics are used.  S is
-// chosen per brick from max|alpha q| (over all points) * l3 (bound on |w1 w2 w3|, from
-// the Bernstein form of the weights: 1 for the spline schemes) and the largest number of
-// points reaching one node (window sums of the cell counts) so that no node's sum can
-// overflow and every contribution is kept to 2^-50 of that bound.  The accumulators take
-// the raw bits of fma(w, q, magic); the write-back removes K * bits(magic) modulo 2^64,
-// K being the node's number of contributions.
+// every contribution w1*w2*w3*alpha*q to an int64 accumulator in shared memory.
+//
+// The arithmetic is integer: GB300's FP64 rate is 1/58 of its FP32 rate, while 64-bit
+// integer products run on the integer pipes.  The weights are 64-bit fixed point
+// w * 2^P (P = 62 - lb, |w| <= 2^lb from the scheme's Bernstein bound) and the
+// quantities q * 2^Q (Q = 62 - e, max|alpha q| < 2^e), both converted once per point;
+// each contribution is the high half of three signed 64 x 64-bit products,
+// hi(hi(hi(wy, wz), wx), q) = w1 w2 w3 q * 2^(3P + Q - 192) (truncated, relative error
+// ~2^-56), shifted right by sh bits so that the brick's largest node coverage K_max cannot
+// overflow (sh = max(0, bits(K_max) - 6)).  Integer addition is associative, so the result
+// does not depend on which thread adds first, and no float atomics are used.
 constexpr int kFlatChunk = 2048;
 
 template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
     k_scatter_fixed64(GridT<T> g, BrickGeo bg, int ncomp,
-                      const uint32_t *__restrict__ cell_start, const T *__restrict__ wts,
-                      const T *__restrict__ qs, const unsigned long long *__restrict__ qmax_bits, double l3,
+                      const uint32_t *__restrict__ cell_start, const long long *__restrict__ wts,
+                      const long long *__restrict__ qi, const unsigned long long *__restrict__ qmax_bits, int wexp,
                       T *__restrict__ field, T beta, int beta_zero, int32_t *status) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int half = N2 / 2;
@@ -514,16 +531,14 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
     const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
-    const double one = qmax * l3, bound = one * (double)kmax;
-    const bool finite = isfinite(bound);
+    const bool finite = isfinite(qmax);
     if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
-    int e1 = 0, es = 0;
-    frexp(one, &e1);
-    frexp(bound, &es);
-    const int s1 = max(-1000, min(1000, min(50 - e1, 61 - es)));
-    const double S = ldexp(1.0, s1);
-    const double magic = 6755399441055744.0;  // 1.5 * 2^52
-    const bool accumulated = finite && count > 0 && one > 0.0;
+    int eq = 0;
+    frexp(qmax, &eq);
+    const int sh = max(0, (32 - __clz((int)kmax)) - 6);
+    // value = acc * 2^-(3P + Q - 192 - sh), P = wexp, Q = 62 - eq
+    const int vexp = 3 * wexp + (62 - eq) - 192 - sh;
+    const bool accumulated = finite && count > 0 && qmax > 0.0;
     if (accumulated) {
       for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk) {
         const uint32_t c1 = min(count, c0 + kFlatChunk);
@@ -550,36 +565,34 @@ __global__ void __launch_bounds__(kThreads)
           for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
             const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
             const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-            const T *wp = wts + (int64_t)sl * (3 * N2);
-            T w1[N2], w2[N2], w3[N2];
+            const long long *wp = wts + (int64_t)sl * (3 * N2);
+            long long w1[N2], w2[N2], w3[N2];
 #pragma unroll
             for (int k = 0; k < N2; ++k) {
               w1[k] = wp[k];
               w2[k] = wp[N2 + k];
               w3[k] = wp[2 * N2 + k];
             }
-            const T *qv = qs + (int64_t)sl * ncomp;
+            const long long *qv = qi + (int64_t)sl * ncomp;
             const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
             const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
             const int lxb = ex - (N2 - 1);
   #pragma unroll 1
             for (int k = kz0; k < kz1; ++k) {
               const int lz = ez + k - (N2 - 1);
-              const double wz = (double)pick_t(w3, k) * S;
+              const long long wz = pick_t(w3, k);
   #pragma unroll 1
               for (int j = ky0; j < ky1; ++j) {
                 const int ly = ey + j - (N2 - 1);
-                const double wyz = (double)pick_t(w2, j) * wz;
+                const long long wyz = __mul64hi(pick_t(w2, j), wz);
                 const int row = (lz * B1 + ly) * B0;
   #pragma unroll
                 for (int i = 0; i < N2; ++i) {
                   const int lx = lxb + i;
                   if (lx < 0 || lx >= vx) continue;
-                  const double w = (double)w1[i] * wyz;
-                  for (int c = 0; c < ncomp; ++c) {
-                    const double h = fma(w, (double)__ldg(qv + c), magic);
-                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)__double_as_longlong(h));
-                  }
+                  const long long w = __mul64hi(w1[i], wyz);
+                  for (int c = 0; c < ncomp; ++c)
+                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)(__mul64hi(w, __ldg(qv + c)) >> sh));
                 }
               }
             }
@@ -598,10 +611,8 @@ __global__ void __launch_bounds__(kThreads)
             const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
             const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
             if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-            const T wl = lane < 3 * N2 ? wts[(int64_t)sl * (3 * N2) + lane] : T(0);
-            // the z weights carry the brick's scale S (a power of two: exact), once per point
-            const double wd = lane >= 2 * N2 && lane < 3 * N2 ? (double)wl * S : (double)wl;
-            const T *qv = qs + (int64_t)sl * ncomp;
+            const long long wl = lane < 3 * N2 ? __ldg(wts + (int64_t)sl * (3 * N2) + lane) : 0ll;
+            const long long *qv = qi + (int64_t)sl * ncomp;
             const int count = nx * ny * nz;
             // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
             const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
@@ -611,17 +622,14 @@ __global__ void __launch_bounds__(kThreads)
               const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
               const int kk = (int)(((uint32_t)r1 * rny) >> 16), jj = r1 - kk * ny;
               const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
-              const double wxi = __shfl_sync(0xffffffffu, wd, i);
-              const double wyj = __shfl_sync(0xffffffffu, wd, N2 + j);
-              const double wzs = __shfl_sync(0xffffffffu, wd, 2 * N2 + k);  // wz * S
+              const long long wxi = __shfl_sync(0xffffffffu, wl, i);
+              const long long wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
+              const long long wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
               if (idx < count) {
-                const double wyz = wyj * wzs;
-                const double w = wxi * wyz;
+                const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
                 const int node = node0 + (k * B1 + j) * B0 + i;
-                for (int c = 0; c < ncomp; ++c) {
-                  const double h = fma(w, (double)__ldg(qv + c), magic);
-                  atomicAdd(acc + c * bvol + node, (unsigned long long)__double_as_longlong(h));
-                }
+                for (int c = 0; c < ncomp; ++c)
+                  atomicAdd(acc + c * bvol + node, (unsigned long long)(__mul64hi(w, __ldg(qv + c)) >> sh));
               }
             }
           }
@@ -631,16 +639,13 @@ __global__ void __launch_bounds__(kThreads)
     }
     __syncthreads();
     // write-back in the reference layout: node fastest, so a warp writes a contiguous row
-    const double to_value = ldexp(1.0, -s1);
     for (int c = 0; c < ncomp; ++c) {
       int lx = lx0, ly = ly0, lz = lz0;
       for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
         if (lx < vx && ly < vy && lz < vz) {
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-          // each add carried bits(magic) once: remove K * bits(magic), modulo 2^64
-          const unsigned long long bias = (unsigned long long)kcnt[nl] * (unsigned long long)__double_as_longlong(magic);
-          const T v = accumulated ? (T)((double)(long long)(acc[c * bvol + nl] - bias) * to_value)
+          const T v = accumulated ? (T)ldexp((double)(long long)acc[c * bvol + nl], -vexp)
                                   : (finite ? T(0) : quiet_nan<T>());
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
         }
@@ -731,11 +736,13 @@ gbg_status launch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncomp,
   const T *f = static_cast<const T *>(field);
   const T *x = static_cast<const T *>(pos);
   T *o = static_cast<T *>(out);
+  mark_main_start(st);
   switch (chunk_for(ncomp)) {
     case 9: k_gather_plain<T, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
     case 3: k_gather_plain<T, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
     default: k_gather_plain<T, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
   }
+  mark_main_stop(st);
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
 }
@@ -801,6 +808,7 @@ struct ScatterLayout {
   void *sort_tmp;
   uint32_t *scan_tmp;
   void *rec, *qs;
+  long long *qi;  // alpha*q in 64-bit fixed point (brick scatter)
   unsigned long long *qmax_bits;
 };
 
@@ -812,9 +820,11 @@ ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncom
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  const size_t rec_bytes = 3 * (size_t)n2 * esize;  // the three axes' weights per point
+  // the three axes' weights per point (64-bit fixed point for the brick scatter)
+  const size_t rec_bytes = 3 * (size_t)n2 * (P.bricked ? sizeof(long long) : esize);
   L.rec = a.take<char>((size_t)m * rec_bytes);
   L.qs = a.take<char>((size_t)m * ncomp * esize);
+  L.qi = P.bricked ? a.take<long long>((size_t)m * ncomp) : nullptr;
   L.qmax_bits = a.take<unsigned long long>(4);
   return L;
 }
@@ -830,8 +840,18 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
                           const T *x, const T *q, int64_t m, double alpha, const ScatterLayout &L, T *field,
                           double beta, int32_t *status, cudaStream_t st) {
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
+  // weights as w * 2^wexp with |w| <= 2^lb (the Bernstein bound with evaluation slack)
+  const double wbound = weight_bound(sch, std::ldexp(1.0, -40));
+  int lb = 0;
+  while (std::ldexp(1.0, lb) < wbound && lb < 60) ++lb;
+  const int wexp = 62 - lb;
   k_brick_prep<T, N2, FIXED ? N2 : 0><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
-      g, s, ncomp, x, q, m, L.perm, T(alpha), static_cast<T *>(L.rec), static_cast<T *>(L.qs), L.qmax_bits);
+      g, s, ncomp, x, q, m, L.perm, T(alpha), wexp, static_cast<long long *>(L.rec), static_cast<T *>(L.qs),
+      L.qmax_bits);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  k_quantities_fixed<T><<<launch_blocks(m * ncomp, kThreads), kThreads, 0, st>>>(
+      static_cast<const T *>(L.qs), m * ncomp, L.qmax_bits, L.qi);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   auto kernel = k_scatter_fixed64<T, N2>;
@@ -842,10 +862,10 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, P.smem);
   const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
-  const double L3 = std::pow(weight_bound(sch, std::ldexp(1.0, -40)), 3);
-  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, ncomp, L.counts, static_cast<const T *>(L.rec),
-                                           static_cast<const T *>(L.qs), L.qmax_bits, L3, field, T(beta),
-                                           beta == 0.0, status);
+  mark_main_start(st);
+  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, ncomp, L.counts, static_cast<const long long *>(L.rec), L.qi,
+                                           L.qmax_bits, wexp, field, T(beta), beta == 0.0, status);
+  mark_main_stop(st);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;

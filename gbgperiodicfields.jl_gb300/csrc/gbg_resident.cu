@@ -1141,8 +1141,10 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
+    mark_main_start(st);
     kernel<<<blocks, threads, smem, st>>>(*map, g, s, b->cell_start, b->rec, b->perm, out, status, nbuf, tile_bytes,
                                            box_bytes);
+    mark_main_stop(st);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
@@ -1201,8 +1203,10 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
+    mark_main_start(st);
     kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
                                            beta == 0.0, status);
+    mark_main_stop(st);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;

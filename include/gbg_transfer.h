@@ -93,6 +93,12 @@ const char *gbg_status_string(gbg_status status);
 const char *gbg_last_error(void);
 /* Number of kernels this library has launched in this process (all threads). */
 uint64_t gbg_kernel_launches(void);
+/* Measurement hook (no counterpart in the reference): with two CUDA events (cudaEvent_t,
+ * created with timing), every later transfer call from this host thread records the first
+ * just before and the second just after its main kernel (the gather kernel, or the brick
+ * accumulation kernel of a scatter), on the call's stream, so that a benchmark can time
+ * that kernel alone.  NULL, NULL switches it off. */
+gbg_status gbg_set_kernel_timing_events(void *start_event, void *stop_event);
 
 /* ---------------------------------------------------------------- schemes */
 
