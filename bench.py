@@ -140,8 +140,10 @@ KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 3>", "gather_quintic"
                 "scatter_cubic": "k_scatter_fixed64<double, 4>", "scatter_quintic": "k_scatter_fixed64<double, 6>"}
 
 # DRAM bytes (read + write) per launch of those kernels on this workload, from one ncu capture
-# of dram__bytes_read.sum + dram__bytes_write.sum (one pass) on the full-size step.
-NCU_TRAFFIC: dict = {}
+# of dram__bytes_read.sum + dram__bytes_write.sum (one pass) on the full-size step (the timed
+# step's launches; the warm-up step's agree to 0.1%).
+NCU_TRAFFIC = {"gather_cubic": 5857477376, "scatter_cubic": 2846136576,
+               "gather_quintic": 6050684928, "scatter_quintic": 5662607872}
 
 
 def fp64_peak_tflops() -> float:
@@ -453,6 +455,10 @@ def precision_form(gbg, lib, dev, peak):
     q64 = gbg.colmajor(q64_r[perm])
     q32 = gbg.colmajor(q64.float())
     del pos_r, q64_r, q32_r, perm
+    # the autotuner picks the bin brick and the threads per CTA for this problem
+    from gbgperiodicfields_gb300 import autotune
+    tuned = autotune.tune(grid, C, scheme, pos, bricks=((11, 8, 8), (7, 8, 8), (15, 8, 8)), reps=1, persist=False)
+    bins = autotune.apply(resident.PointBins(grid, M, brick=tuned["brick"]).build(pos), tuned)
     t_bins = _time_ms(lambda: bins.build(pos))
     t_gather = _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out))
     t_scatter = _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
@@ -483,6 +489,7 @@ def precision_form(gbg, lib, dev, peak):
         "value": 2 * M / (step / 1e3), "unit": UNIT,
         "per_call_ms": {"bins": t_bins, "gather": t_gather, "scatter": t_scatter},
         "kernel_ms": {"gather": k_gather, "scatter": k_scatter},
+        "tuned": {k: tuned[k] for k in ("brick", "gather_threads", "scatter_threads")},
         "random_order_ms": random_order,
         "roofline": {
             "gather": {"bound": "hbm", "kernel": "k_gather_staged4<4, 12, float>",

@@ -155,6 +155,18 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Fixed-point exponent P of the scatter's weights, w * 2^P: |w| <= L (the scheme's
+// Bernstein bound with evaluation slack) <= 1.5 * 2^lb, P = 62 - lb.  Then
+// |w * 2^P| < 1.5 * 2^62, a product of three weights' high halves stays below
+// 3.375 * 2^58, a contribution below 3.375 * 2^56, and a node's sum, shifted by
+// bits(K_max) - 5, below 2^63.
+int fixed_weight_exp(const gbg_scheme &sch) {
+  const double L = weight_bound(sch, std::ldexp(1.0, -40));
+  int lb = 0;
+  while (1.5 * std::ldexp(1.0, lb) < L && lb < 60) ++lb;
+  return 62 - lb;
+}
+
 // Run-time width (stencils of 10..16 nodes): nothing unrolled.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
@@ -423,7 +435,7 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // each contribution is the high half of three signed 64 x 64-bit products,
 // hi(hi(hi(wy, wz), wx), q) = w1 w2 w3 q * 2^(3P + Q - 192) (truncated, relative error
 // ~2^-56), shifted right by sh bits so that the brick's largest node coverage K_max cannot
-// overflow (sh = max(0, bits(K_max) - 6)).  Integer addition is associative, so the result
+// overflow (sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
 // does not depend on which thread adds first, and no float atomics are used.
 constexpr int kFlatChunk = 2048;
 
@@ -535,7 +547,8 @@ __global__ void __launch_bounds__(kThreads)
     if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
     int eq = 0;
     frexp(qmax, &eq);
-    const int sh = max(0, (32 - __clz((int)kmax)) - 6);
+    const int sh = max(0, (32 - __clz((int)kmax)) - 5);
+    const long long half = sh > 0 ? (1ll << (sh - 1)) : 0ll;  // the shift rounds to nearest
     // value = acc * 2^-(3P + Q - 192 - sh), P = wexp, Q = 62 - eq
     const int vexp = 3 * wexp + (62 - eq) - 192 - sh;
     const bool accumulated = finite && count > 0 && qmax > 0.0;
@@ -592,7 +605,7 @@ __global__ void __launch_bounds__(kThreads)
                   if (lx < 0 || lx >= vx) continue;
                   const long long w = __mul64hi(w1[i], wyz);
                   for (int c = 0; c < ncomp; ++c)
-                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)(__mul64hi(w, __ldg(qv + c)) >> sh));
+                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
                 }
               }
             }
@@ -629,7 +642,7 @@ __global__ void __launch_bounds__(kThreads)
                 const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
                 const int node = node0 + (k * B1 + j) * B0 + i;
                 for (int c = 0; c < ncomp; ++c)
-                  atomicAdd(acc + c * bvol + node, (unsigned long long)(__mul64hi(w, __ldg(qv + c)) >> sh));
+                  atomicAdd(acc + c * bvol + node, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
               }
             }
           }
@@ -840,11 +853,7 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
                           const T *x, const T *q, int64_t m, double alpha, const ScatterLayout &L, T *field,
                           double beta, int32_t *status, cudaStream_t st) {
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
-  // weights as w * 2^wexp with |w| <= 2^lb (the Bernstein bound with evaluation slack)
-  const double wbound = weight_bound(sch, std::ldexp(1.0, -40));
-  int lb = 0;
-  while (std::ldexp(1.0, lb) < wbound && lb < 60) ++lb;
-  const int wexp = 62 - lb;
+  const int wexp = fixed_weight_exp(sch);
   k_brick_prep<T, N2, FIXED ? N2 : 0><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
       g, s, ncomp, x, q, m, L.perm, T(alpha), wexp, static_cast<long long *>(L.rec), static_cast<T *>(L.qs),
       L.qmax_bits);
