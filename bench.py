@@ -136,7 +136,7 @@ def peaks():
 
 
 # The main kernel of each timed call of the headline step.
-KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 3>", "gather_quintic": "k_gather_plain<double, 6, 3>",
+KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 4, 3>", "gather_quintic": "k_gather_plain<double, 6, 6, 3>",
                 "scatter_cubic": "k_scatter_fixed64<double, 4>", "scatter_quintic": "k_scatter_fixed64<double, 6>"}
 
 # DRAM bytes (read + write) per launch of those kernels on this workload, from one ncu capture
@@ -276,10 +276,7 @@ def run_gb300(args, rank, world):
     if int(status.item()) != 0:
         raise RuntimeError(f"device status {int(status.item())}")
 
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
+    ms_total = reduce_max(ms_total, world, dev)
     evals_per_step = 4 * M_POINTS
     value = world * evals_per_step * args.steps / (ms_total / 1e3)
 
@@ -645,6 +642,17 @@ def served_form(gbg, dev, requests=240, seed=9):
     del fields, pool
     torch.cuda.empty_cache()
     return res
+
+
+def reduce_max(value: float, world: int, device) -> float:
+    """The largest value over the ranks (the whole job's time is its slowest replica's)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 # ----------------------------------------------------------- CPU baseline

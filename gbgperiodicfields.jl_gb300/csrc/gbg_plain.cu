@@ -5,8 +5,8 @@
 //   gbg_point_traversal_order   point_traversal_order   Interpolation.jl:816-833, 636-684
 //   gbg_validate_traversal      PointTraversalOrder     Interpolation.jl:560-589
 //
-// The gather is one thread per work item, as in the reference, with the stencil weight
-// of each node formed once and applied to every component of the chunk.  The scatter is
+// The gather is one thread per work item, as in the reference, contracting the x
+// direction first for every component of the chunk.  The scatter is
 // not the reference's atomic push: points are sorted by brick and cell with a stable
 // device radix sort, and each brick's nodes are accumulated in shared memory as int64
 // fixed-point sums (or, for a stencil wider than the grid, every node pulls its
@@ -98,9 +98,36 @@ __device__ __forceinline__ bool visit(const int32_t *__restrict__ trav, int64_t 
 
 // ---------------------------------------------------------------- gather
 
+// Horner with fused multiply-adds (one rounding per step instead of the reference's two;
+// the weights differ by at most an ulp or so, far inside the transfer's 1e-13 bar).
+// M2 > 0: that many powers at compile time; M2 == 0: the scheme's own count.
+template <typename T, int N2, int M2>
+__device__ __forceinline__ void axis_weights_fma(const SchemeT<T, N2> &s, T t, T (&w)[N2]) {
+  if constexpr (M2 > 0) {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = s.c[q + N2 * (M2 - 1)];
+#pragma unroll
+    for (int p = M2 - 2; p >= 0; --p)
+#pragma unroll
+      for (int q = 0; q < N2; ++q) w[q] = fma_rn(w[q], t, s.c[q + N2 * p]);
+  } else {
+#pragma unroll
+    for (int q = 0; q < N2; ++q) w[q] = T(0);
+#pragma unroll
+    for (int p = GBG_MAX_POWERS - 1; p >= 0; --p) {
+      if (p < s.m2) {
+#pragma unroll
+        for (int q = 0; q < N2; ++q) w[q] = fma_rn(w[q], t, s.c[q + N2 * p]);
+      }
+    }
+  }
+}
+
 // Compile-time width N2: the (j, i) stencil plane is unrolled, z advances by the
-// reference's running walk.
-template <typename T, int N2, int CC>
+// reference's running walk.  The x direction is contracted first, per (j, k) and
+// component, s = sum_i w1[i] f, then acc += (w2[j] w3[k]) s: 22 FP64 operations per
+// (j, k) at width 6 and 3 components instead of 25 -- this kernel is FP64-pipe-bound.
+template <typename T, int N2, int M2, int CC>
 __global__ void __launch_bounds__(kThreads)
     k_gather_plain(GridT<T> g, SchemeT<T, N2> s, int ncomp, const T *__restrict__ field,
                    const T *__restrict__ pos, int64_t m, const int32_t *__restrict__ trav,
@@ -115,9 +142,9 @@ __global__ void __launch_bounds__(kThreads)
     const bool ok = locate3(g, pos, p, m, b, t);
     if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
     T w1[N2], w2[N2], w3[N2];
-    axis_weights<T, N2>(s, t[0], w1);
-    axis_weights<T, N2>(s, t[1], w2);
-    axis_weights<T, N2>(s, t[2], w3);
+    axis_weights_fma<T, N2, M2>(s, t[0], w1);
+    axis_weights_fma<T, N2, M2>(s, t[1], w2);
+    axis_weights_fma<T, N2, M2>(s, t[2], w3);
     int64_t ix[N2], iy[N2];
     walk_offsets<N2>(b[0], g.nx, 1, ix);
     walk_offsets<N2>(b[1], g.ny, g.nx, iy);
@@ -139,13 +166,17 @@ __global__ void __launch_bounds__(kThreads)
         for (int j = 0; j < N2; ++j) {
           const T wyz = mul_rn(w2[j], w3k);
           const T *row = plane + iy[j];
+          T sx[CC];
 #pragma unroll
-          for (int i = 0; i < N2; ++i) {
-            const T wv = mul_rn(wyz, w1[i]);
+          for (int c = 0; c < CC; ++c) sx[c] = mul_rn(w1[0], __ldg(row + ix[0] + g.npf * c));
+#pragma unroll
+          for (int i = 1; i < N2; ++i) {
             const T *f = row + ix[i];
 #pragma unroll
-            for (int c = 0; c < CC; ++c) acc[c] = fma_rn(wv, __ldg(f + g.npf * c), acc[c]);
+            for (int c = 0; c < CC; ++c) sx[c] = fma_rn(w1[i], __ldg(f + g.npf * c), sx[c]);
           }
+#pragma unroll
+          for (int c = 0; c < CC; ++c) acc[c] = fma_rn(wyz, sx[c], acc[c]);
         }
         node_z = step_up(node_z, g.nz);
       }
@@ -750,11 +781,16 @@ gbg_status launch_gather(const gbg_grid &grid, const gbg_scheme &sch, int ncomp,
   const T *x = static_cast<const T *>(pos);
   T *o = static_cast<T *>(out);
   mark_main_start(st);
-  switch (chunk_for(ncomp)) {
-    case 9: k_gather_plain<T, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
-    case 3: k_gather_plain<T, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
-    default: k_gather_plain<T, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); note_launch(); break;
+  const bool full = sch.num_powers == N2;  // num_powers == width: compile-time Horner
+  switch (chunk_for(ncomp) * 2 + (full ? 1 : 0)) {
+    case 19: k_gather_plain<T, N2, N2, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 18: k_gather_plain<T, N2, 0, 9><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 7: k_gather_plain<T, N2, N2, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 6: k_gather_plain<T, N2, 0, 3><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    case 3: k_gather_plain<T, N2, N2, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
+    default: k_gather_plain<T, N2, 0, 1><<<blocks, kThreads, 0, st>>>(g, s, ncomp, f, x, m, trav, o, status); break;
   }
+  note_launch();
   mark_main_stop(st);
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
