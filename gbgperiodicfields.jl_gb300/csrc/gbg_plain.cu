@@ -367,11 +367,17 @@ struct BrickGeo {
   int64_t bvol;
 };
 
-template <typename T>
+// One pass over the points in their own order: the locate, the brick-major key and the
+// cell count, the three axes' stencil weights (the reference's Horner with fused
+// multiply-adds, once per point) as 64-bit fixed point w * 2^wexp, and max|alpha q|.
+template <typename T, int N2, int M2>
 __global__ void __launch_bounds__(kThreads)
-    k_brick_keys(GridT<T> g, BrickGeo bg, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
-                 uint32_t *__restrict__ counts, int32_t *status) {
+    k_brick_keys(GridT<T> g, BrickGeo bg, SchemeT<T, N2> sch, const T *__restrict__ pos, int64_t m,
+                 uint32_t *__restrict__ keys, uint32_t *__restrict__ counts, int wexp, long long *__restrict__ worig,
+                 const T *__restrict__ q, int ncomp, T alpha, unsigned long long *__restrict__ qmax_bits,
+                 int32_t *status) {
   const int64_t n[3] = {g.nx, g.ny, g.nz};
+  unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t b[3];
@@ -388,37 +394,17 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t key = (uint32_t)(brick * bg.bvol + local);
     keys[p] = key;
     atomicAdd(counts + key, 1u);
-  }
-}
-
-// Per point in sorted order: the three axes' stencil weights (w[axis*N2 + q], the
-// reference's Horner and roundings, evaluated once per point rather than once per brick
-// that the point reaches) as 64-bit fixed point w * 2^wexp, and alpha*q; max|alpha q|
-// for the quantities' fixed-point scale.
-template <typename T, int N2, int M2>
-__global__ void __launch_bounds__(kThreads)
-    k_brick_prep(GridT<T> g, SchemeT<T, N2> sch, int ncomp, const T *__restrict__ pos, const T *__restrict__ q,
-                 int64_t m, const uint32_t *__restrict__ perm, T alpha, int wexp, long long *__restrict__ wts,
-                 T *__restrict__ qs, unsigned long long *__restrict__ qmax_bits) {
-  unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
-  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
-       sl += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = perm[sl];
-    int64_t b[3];
-    T t[3];
-    const bool ok = locate3(g, pos, p, m, b, t);
-    long long *wp = wts + sl * (3 * N2);
+    long long *wp = worig + p * (3 * N2);
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
       T w[N2];
-      axis_weights_m<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
-      // exact: a double times a power of two, then a 53-bit integer (|w| < 2^(62-wexp))
+      axis_weights_fma<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
+      // exact: a double times a power of two, then a 53-bit integer
 #pragma unroll
       for (int k = 0; k < N2; ++k) wp[d * N2 + k] = ok ? __double2ll_rn(ldexp((double)w[k], wexp)) : 0ll;
     }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
-      qs[sl * ncomp + c] = v;
       const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs((double)v));
       mx = bits > mx ? bits : mx;
     }
@@ -431,18 +417,29 @@ __global__ void __launch_bounds__(kThreads)
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
-// alpha*q as 64-bit fixed point q * 2^(62 - e), max|alpha q| < 2^e (one scale for all
-// points, known once the preparation pass has reduced the maximum).
-template <typename T>
+// Into sorted order: each slot's weights, and alpha*q as 64-bit fixed point
+// q * 2^(62 - e) with max|alpha q| < 2^e (one scale for all points).
+template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
-    k_quantities_fixed(const T *__restrict__ qs, int64_t n, const unsigned long long *__restrict__ qmax_bits,
-                       long long *__restrict__ qi) {
+    k_brick_order(const uint32_t *__restrict__ perm, int64_t m, const long long *__restrict__ worig,
+                  long long *__restrict__ wts, const T *__restrict__ q, int ncomp, T alpha,
+                  const unsigned long long *__restrict__ qmax_bits, long long *__restrict__ qi) {
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   int e = 0;
   frexp(qmax, &e);
   const bool finite = isfinite(qmax);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    qi[i] = finite ? __double2ll_rn(ldexp((double)qs[i], 62 - e)) : 0ll;
+  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
+       sl += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t p = perm[sl];
+    const long long *src = worig + p * (3 * N2);
+    long long *dst = wts + sl * (3 * N2);
+#pragma unroll
+    for (int k = 0; k < 3 * N2; ++k) dst[k] = __ldg(src + k);
+    for (int c = 0; c < ncomp; ++c) {
+      const T v = mul_rn(alpha, q[p + m * c]);
+      qi[sl * ncomp + c] = finite ? __double2ll_rn(ldexp((double)v, 62 - e)) : 0ll;
+    }
+  }
 }
 
 template <int N, typename T>
@@ -869,10 +866,11 @@ ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncom
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  // the three axes' weights per point (64-bit fixed point for the brick scatter)
+  // the three axes' weights per point (64-bit fixed point for the brick scatter, whose
+  // qs region holds them in the points' own order before they are sorted)
   const size_t rec_bytes = 3 * (size_t)n2 * (P.bricked ? sizeof(long long) : esize);
   L.rec = a.take<char>((size_t)m * rec_bytes);
-  L.qs = a.take<char>((size_t)m * ncomp * esize);
+  L.qs = a.take<char>((size_t)m * (P.bricked ? rec_bytes : ncomp * esize));
   L.qi = P.bricked ? a.take<long long>((size_t)m * ncomp) : nullptr;
   L.qmax_bits = a.take<unsigned long long>(4);
   return L;
@@ -890,13 +888,18 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
                           double beta, int32_t *status, cudaStream_t st) {
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
   const int wexp = fixed_weight_exp(sch);
-  k_brick_prep<T, N2, FIXED ? N2 : 0><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
-      g, s, ncomp, x, q, m, L.perm, T(alpha), wexp, static_cast<long long *>(L.rec), static_cast<T *>(L.qs),
-      L.qmax_bits);
+  const int blocks_m = launch_blocks(m, kThreads);
+  GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
+  k_brick_keys<T, N2, FIXED ? N2 : 0><<<blocks_m, kThreads, 0, st>>>(
+      g, P.bg, s, x, m, L.keys, L.counts, wexp, static_cast<long long *>(L.qs), q, ncomp, T(alpha), L.qmax_bits,
+      status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
-  k_quantities_fixed<T><<<launch_blocks(m * ncomp, kThreads), kThreads, 0, st>>>(
-      static_cast<const T *>(L.qs), m * ncomp, L.qmax_bits, L.qi);
+  GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
+  GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
+  k_brick_order<T, N2><<<blocks_m, kThreads, 0, st>>>(L.perm, m, static_cast<const long long *>(L.qs),
+                                                     static_cast<long long *>(L.rec), q, ncomp, T(alpha),
+                                                     L.qmax_bits, L.qi);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   auto kernel = k_scatter_fixed64<T, N2>;
@@ -925,12 +928,6 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   T *f = static_cast<T *>(field);
   GBG_CUDA_TRY(cudaMemsetAsync(L.counts, 0, sizeof(uint32_t) * (size_t)(P.nkeys + 1), st));
   if (P.bricked) {
-    k_brick_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, status);
-    note_launch();
-    GBG_CUDA_TRY(cudaGetLastError());
-    GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
-    GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
-    GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
     const T *qq = static_cast<const T *>(q);
     const int w = sch.stencil_width;
     const bool fixed = sch.num_powers == w;

@@ -133,8 +133,9 @@ gbg_status gbg_interpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
 /* anterpolate! -- Interpolation.jl:1299-1323 (kernel 1063-1106, prescale 1309-1313):
  * field = alpha * W^T q + beta * field, with beta == 0 overwriting (NaN-safe).
  * Deterministic: the result is bitwise identical run to run and independent of the
- * traversal (points are cell-sorted on the device and every node sums its
- * contributions in a fixed order, with no float atomics).  workspace: device scratch
+ * traversal (points are sorted by brick and cell on the device and every brick sums its
+ * nodes' contributions as 64-bit fixed-point integers, whose sum does not depend on the
+ * order of the additions; no float atomics).  workspace: device scratch
  * of at least gbg_anterpolate_workspace_size bytes, or NULL (the library then takes
  * stream-ordered scratch with cudaMallocAsync and releases it before returning). */
 gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp, void *field,
@@ -263,8 +264,9 @@ gbg_status gbg_bins_order(gbg_bins bins, int32_t *order, void *stream);
 gbg_status gbg_interpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype out_dtype, void *out, void *stream);
 /* Deterministic scatter of q (M, ncomp) of q_dtype at binned points into a resident
- * field: field = alpha * W^T q + beta * field.  No float atomics; the ghost layer is
- * refreshed.  In FP32 storage each node's sum is compensated (Neumaier). */
+ * field: field = alpha * W^T q + beta * field.  No float atomics: each node's sum is
+ * kept as two 32-bit fixed-point words (the rounded contribution and its residual), so
+ * the result is bitwise reproducible; the ghost layer is refreshed. */
 gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype q_dtype, const void *q, double alpha, double beta,
                                   void *stream);
