@@ -496,7 +496,7 @@ def precision_form(gbg, lib, dev, peak):
                        "achieved": alg["gather"] / (k_gather / 1e3) / 1e9, "peak": peak,
                        "unit": "GB/s", "frac": alg["gather"] / (k_gather / 1e3) / 1e9 / peak,
                        "algorithmic_bytes": alg["gather"]},
-            "scatter": {"bound": "hbm", "kernel": "k_scatter_fixed<4, 1, 12>",
+            "scatter": {"bound": "hbm", "kernel": "k_scatter_nodes<4, 1, 12>",
                         "achieved": alg["scatter"] / (k_scatter / 1e3) / 1e9, "peak": peak,
                         "unit": "GB/s", "frac": alg["scatter"] / (k_scatter / 1e3) / 1e9 / peak,
                         "algorithmic_bytes": alg["scatter"]}},

@@ -63,6 +63,10 @@ struct gbg_bins_s {
   size_t bytes = 0;
   bool async = false;  // block from cudaMallocAsync (serving loop)
   int32_t gather_threads = 0, scatter_threads = 0;  // 0: the defaults (gbg_bins_set_launch)
+  // work lists rebuilt with the bins: bricks holding a point (gathers), bricks a point's
+  // stencil reaches (scatters with beta == 1; valid when reach_ok), and their lengths
+  uint32_t *active = nullptr, *reach = nullptr, *lists_n = nullptr;
+  bool reach_ok = false;
 };
 
 namespace gbg {
@@ -79,6 +83,9 @@ inline void bins_layout(Arena &a, gbg_bins_s *b) {
   b->scan_tmp = a.take<uint32_t>(scan_temp_elems(b->nkeys + 1));
   b->qs = a.take<float>((size_t)m * 12);
   b->qmax_bits = a.take<unsigned>(64);
+  b->active = a.take<uint32_t>((size_t)b->nbricks);
+  b->reach = a.take<uint32_t>((size_t)b->nbricks);
+  b->lists_n = a.take<uint32_t>(4);
 }
 }  // namespace gbg
 
@@ -315,6 +322,29 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// The bins' work lists: bricks holding a point, and bricks whose 27 neighbours (periodic)
+// hold one -- the bricks a stencil of up to 8 nodes can reach when every brick (and the
+// last, partial one) is at least 4 cells wide (reach_ok).  Their order is whatever the
+// atomics give: each list only says which bricks to visit.
+__global__ void k_brick_lists(const uint32_t *__restrict__ cell_start, int64_t nbx, int64_t nby, int64_t nbz,
+                              int64_t bvol, int reach_ok, uint32_t *__restrict__ active,
+                              uint32_t *__restrict__ reach, uint32_t *__restrict__ lists_n) {
+  const int64_t nbricks = nbx * nby * nbz;
+  auto holds = [&](int64_t b) { return __ldg(cell_start + (b + 1) * bvol) > __ldg(cell_start + b * bvol); };
+  for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nbricks; b += (int64_t)gridDim.x * blockDim.x) {
+    if (holds(b)) active[atomicAdd(lists_n, 1u)] = (uint32_t)b;
+    if (!reach_ok) continue;
+    const int64_t bx = b % nbx, by = (b / nbx) % nby, bz = b / (nbx * nby);
+    bool near = false;
+    for (int d = 0; d < 27 && !near; ++d) {
+      const int64_t x = (bx + d % 3 - 1 + nbx) % nbx, y = (by + (d / 3) % 3 - 1 + nby) % nby,
+                    z = (bz + d / 9 - 1 + nbz) % nbz;
+      near = holds((z * nby + y) * nbx + x);
+    }
+    if (near) reach[atomicAdd(lists_n + 1, 1u)] = (uint32_t)b;
+  }
+}
+
 __global__ void k_gather_records(const float4 *__restrict__ rec_user, const uint32_t *__restrict__ perm,
                                  int64_t m, float4 *__restrict__ rec) {
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m;
@@ -444,7 +474,8 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     k_gather_staged4(const __grid_constant__ CUtensorMap tmap, StagedGeo g, SchemeT<float, 4> s,
                      const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                      const uint32_t *__restrict__ perm, TO *__restrict__ out, int32_t *status, int nbuf,
-                     uint32_t tile_bytes, uint32_t box_bytes) {
+                     uint32_t tile_bytes, uint32_t box_bytes, const uint32_t *__restrict__ list,
+                     const uint32_t *__restrict__ list_n) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nbuf * tile_bytes);
   if (threadIdx.x == 0) {
@@ -470,13 +501,16 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
   };
   auto nonempty = [&](int64_t b) { return __ldg(cell_start + (b + 1) * g.bvol) > __ldg(cell_start + b * g.bvol); };
 
-  int64_t b = blockIdx.x;
-  if (threadIdx.x == 0 && b < g.nbricks && nonempty(b)) issue(b, 0);
-  for (int it = 0; b < g.nbricks; ++it, b += gridDim.x) {
+  // the bricks to visit: the bins' list of bricks holding points, or every brick
+  const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
+  auto unit = [&](int64_t i) -> int64_t { return i >= nunits ? -1 : (list ? (int64_t)__ldg(list + i) : i); };
+  int64_t ui = blockIdx.x;
+  if (threadIdx.x == 0 && unit(ui) >= 0 && nonempty(unit(ui))) issue(unit(ui), 0);
+  for (int it = 0; ui < nunits; ++it, ui += gridDim.x) {
     const int buf = nbuf == 2 ? (it & 1) : 0;
-    const int64_t bn = b + gridDim.x;
+    const int64_t b = unit(ui), bn = unit(ui + gridDim.x);
     const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
-    if (nbuf == 2 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, buf ^ 1);
+    if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
       if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
@@ -552,7 +586,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
       }
     }
     __syncthreads();  // every lane is done with this buffer before it is refilled
-    if (nbuf == 1 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, 0);
+    if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
   }
   if (failed) {
     // a copy that never completed: give any other in-flight copy a bounded chance to land
@@ -566,7 +600,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_gather_staged_generic(const __grid_constant__ CUtensorMap tmap, StagedGeo g, SchemeT<float, N2> s,
                             const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                             const uint32_t *__restrict__ perm, TO *__restrict__ out, int32_t *status,
-                            int nbuf, uint32_t tile_bytes, uint32_t box_bytes) {
+                            int nbuf, uint32_t tile_bytes, uint32_t box_bytes, const uint32_t *__restrict__ list,
+                            const uint32_t *__restrict__ list_n) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nbuf * tile_bytes);
   if (threadIdx.x == 0) {
@@ -584,13 +619,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                   (int)(by * g.b[1]) + g.box_off, (int)(bz * g.b[2]) + g.box_off, bars + buf);
   };
   auto nonempty = [&](int64_t b) { return __ldg(cell_start + (b + 1) * g.bvol) > __ldg(cell_start + b * g.bvol); };
-  int64_t b = blockIdx.x;
-  if (threadIdx.x == 0 && b < g.nbricks && nonempty(b)) issue(b, 0);
-  for (int it = 0; b < g.nbricks; ++it, b += gridDim.x) {
+  // the bricks to visit: the bins' list of bricks holding points, or every brick
+  const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
+  auto unit = [&](int64_t i) -> int64_t { return i >= nunits ? -1 : (list ? (int64_t)__ldg(list + i) : i); };
+  int64_t ui = blockIdx.x;
+  if (threadIdx.x == 0 && unit(ui) >= 0 && nonempty(unit(ui))) issue(unit(ui), 0);
+  for (int it = 0; ui < nunits; ++it, ui += gridDim.x) {
     const int buf = nbuf == 2 ? (it & 1) : 0;
-    const int64_t bn = b + gridDim.x;
+    const int64_t b = unit(ui), bn = unit(ui + gridDim.x);
     const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
-    if (nbuf == 2 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, buf ^ 1);
+    if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
       if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
@@ -643,7 +681,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
     __syncthreads();
-    if (nbuf == 1 && threadIdx.x == 0 && bn < g.nbricks && nonempty(bn)) issue(bn, 0);
+    if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
   }
   if (failed)
     for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
@@ -686,36 +724,9 @@ struct FixGeo {
   int64_t px, py;
   int32_t halo, cp, ncomp;
   int32_t neighbour_skip;  // every brick edge >= width/2: the region lies in the 27 neighbouring bricks
-  double l3;  // bound on |w1*w2*w3| (the cube of the scheme's Bernstein weight bound)
+  int32_t chunk;           // points staged in shared memory at a time (a multiple of 4)
+  int32_t chunk1;          // the same when the region's points fit at once (no running sums kept)
 };
-
-// Deterministic scatter.  A CTA owns a brick's nodes; it walks the points of every cell
-// whose stencil reaches the brick (the extended region) and adds each contribution
-// w*alpha*q to fixed-point accumulators in shared memory.  Integer addition is
-// associative, so the sums -- and the result -- do not depend on the order in which the
-// threads add, and no float atomics are involved.
-//
-// Each contribution x = w*q*S1 (S1 a power of two) is split into its nearest integer hi
-// and the residual r = x - hi, |r| <= 1/2, kept as lo = round(r * 2^k); hi and lo go to
-// two int32 accumulators.  Both roundings use the float "magic number" 1.5*2^23 (an FMA
-// lands the value where the float's ulp is 1), so no slow int64 conversion or atomic is
-// needed.  S1 and k come from bounds on one contribution (max|alpha q| * l3) and on a
-// node's sum (points in the region times that), so neither accumulator can overflow; the
-// result carries about 2^-41 of max|alpha q| * l3 per contribution.
-constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
-constexpr int kMagicBits = 0x4B400000;
-
-// The accumulators receive the raw bit patterns of h and l: each add carries the magic
-// number's bits once, and the write-back removes K * bits(magic) (modulo 2^32), K being the
-// node's number of contributions (its coverage count), so no subtraction runs per add.
-__device__ __forceinline__ void add_fixed(unsigned *hi_acc, unsigned *lo_acc, int idx, float w, float q,
-                                          float lo_scale) {
-  const float h = fmaf(w, q, kMagic);
-  const float r = fmaf(w, q, -(h - kMagic));  // h - kMagic is exact: an integer below 2^21
-  const float l = fmaf(r, lo_scale, kMagic);
-  atomicAdd(hi_acc + idx, __float_as_uint(h));
-  atomicAdd(lo_acc + idx, __float_as_uint(l));
-}
 
 // All N2 weights from coefficients in memory ([q + N2*p], M2 == N2 powers).
 template <int N2>
@@ -739,45 +750,70 @@ __device__ __forceinline__ void weights_rt(const float *c, int m2, float t, floa
     for (int q = 0; q < N2; ++q) w[q] = fmaf(w[q], t, c[q + N2 * p]);
 }
 
-constexpr int kFlatChunk32 = 2048;
-
-// Shared memory of one scatter CTA: two int32 accumulators per node and component, the
-// exclusive prefix of the extended region's per-cell counts and their first slots, one
-// chunk of the region's points (slot and packed cell coordinates), and the per-axis key
-// tables of the region's cells.
-size_t scatter32_smem(const FixGeo &g, int cp) {
+// Shared memory of one scatter CTA, in this order: the brick's running sums (CP floats per
+// node), one chunk of the region's points (CP quantities and 3*N2 weights each), the
+// region's per-cell point offsets (+ the total) and first slots, the per-axis key tables
+// of the region's cells, and the points' region x cells.
+size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
   const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
-  return 2 * sizeof(int) * (size_t)g.bvol * cp + 2 * sizeof(uint32_t) * ecount + 2 * sizeof(uint32_t) * kFlatChunk32 +
-         sizeof(uint32_t) * (size_t)(g.e[0] + g.e[1] + g.e[2]) + sizeof(uint32_t) * (size_t)(g.bvol + 1);
+  return sizeof(float) * (size_t)g.bvol * cp + sizeof(uint32_t) * (2 * ecount + 1 + (size_t)(g.e[0] + g.e[1] + g.e[2])) +
+         16;
 }
 
-// The scatter of one brick: list the region's points, give each warp a point (its lanes
-// cover the point's nodes in the brick), and add its contributions to the brick's
-// fixed-point accumulators; then write every node once.
-// All index arithmetic is 32-bit and division-free inside the loops: the region's cell
-// keys come from three per-axis tables (key = kx[ex] + ky[ey] + kz[ez]) and each thread
-// steps its (ex, ey, ez) incrementally.
+size_t scatter_nodes_smem(const FixGeo &g, int cp, int n2) {
+  return scatter_nodes_fixed(g, cp) + sizeof(float) * (size_t)g.chunk * (cp + 3 * n2) + (size_t)g.chunk1;
+}
+
+// Sets the chunk sizes: the largest chunk (a multiple of 4, 64..1024 points) whose CTA
+// fits in `budget` bytes, and the larger one that also takes the running sums' space when
+// the whole region fits in one chunk.
+void scatter_nodes_chunk(FixGeo &g, int cp, int n2, size_t budget) {
+  const size_t per = sizeof(float) * (cp + 3 * n2) + 1, fixed = scatter_nodes_fixed(g, cp);
+  const size_t fit = budget > fixed ? (budget - fixed) / per : 0;
+  g.chunk = (int32_t)std::max<size_t>(64, std::min<size_t>(1024, fit & ~size_t(3)));
+  g.chunk1 = g.chunk + (int32_t)(((size_t)g.bvol * cp * sizeof(float) / per) & ~size_t(3));
+}
+
+// Shared memory per scatter CTA: the SM's share for as many CTAs as the kernel's registers
+// allow (at most 4), less the block's reserved and static share.
+size_t scatter_nodes_budget(int regs, int threads) {
+  const int by_regs = std::max(1, std::min(4, 65536 / std::max(1, regs * threads)));
+  return std::min<size_t>(200 * 1024, 228 * 1024 / by_regs - 4096);
+}
+
+// Deterministic scatter, output-driven.  A CTA owns a brick's nodes and a thread owns a
+// node: it sums, in registers, the contributions w*alpha*q of every point whose stencil
+// reaches the node, in a fixed order -- the node's N2 x N2 rows of cells (z outer, y
+// inner), within a row the points in their binned order.  The order depends on the
+// points alone, not on the launch shape, the chunking or the other instances of a batch,
+// so the result is reproducible bitwise; no atomics are involved.
+//
+// The brick's region (its cells widened by N2 - 1) is listed in region order (x fastest)
+// with per-cell offsets; its points pass through shared memory in chunks of contiguous
+// region positions.  A node's points occupy increasing region positions, so a chunked
+// pass continues each node's running sum exactly where the previous chunk left it.
+// All index arithmetic is 32-bit: the region's cell keys come from three per-axis tables
+// (key = kx[ex] + ky[ey] + kz[ez]).
 template <int N2, bool FIXED, int CP>
-__device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int64_t b,
-                                const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
-                                const float *__restrict__ qs, float qmax, float *__restrict__ field, float beta,
-                                int beta_zero, unsigned char *smem, uint32_t *warp_tot, int32_t *status) {
+__device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, int64_t b,
+                                    const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
+                                    const float *__restrict__ qs, float *__restrict__ field, float beta,
+                                    int beta_zero, unsigned char *smem, uint32_t *warp_tot) {
   const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)g.bvol;
-  unsigned *acc_hi = reinterpret_cast<unsigned *>(smem);
-  unsigned *acc_lo = acc_hi + bvol * CP;
-  uint32_t *off = reinterpret_cast<uint32_t *>(acc_lo + bvol * CP);
-  uint32_t *r0s = off + ecount;
-  uint32_t *pslot = r0s + ecount;
-  uint32_t *pxyz = pslot + kFlatChunk32;
-  uint32_t *kx = pxyz + kFlatChunk32, *ky = kx + E0, *kz = ky + E1;
-  uint32_t *kcnt = kz + E2;  // bvol coverage counts, then their maximum
+  constexpr int W3 = 3 * N2;
+  // [running sums | chunk: quantities, weights] [offsets, first slots, key tables] [x cells]
+  float *sacc = reinterpret_cast<float *>(smem);
+  uint32_t *off = reinterpret_cast<uint32_t *>(sacc + bvol * CP + g.chunk * (CP + W3));
+  uint32_t *r0s = off + ecount + 1;
+  uint32_t *kx = r0s + ecount, *ky = kx + E0, *kz = ky + E1;
+  unsigned char *scx = reinterpret_cast<unsigned char *>(kz + E2);
   constexpr int half = N2 / 2;
   const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]), bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
+  const int B0 = g.b[0], B1 = g.b[1];
   // nodes of this brick inside the grid
-  const int vx = min(g.b[0], g.n[0] - bx * g.b[0]), vy = min(g.b[1], g.n[1] - by * g.b[1]),
-            vz = min(g.b[2], g.n[2] - bz * g.b[2]);
+  const int vx = min(B0, g.n[0] - bx * B0), vy = min(B1, g.n[1] - by * B1), vz = min(g.b[2], g.n[2] - bz * g.b[2]);
   // is any point near?  (the 27 neighbouring bricks hold the whole region)
   bool any = true;
   if (g.neighbour_skip) {
@@ -793,8 +829,6 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
   }
   if (!any && !beta_zero && beta == 1.0f) return;  // the brick keeps its values
   uint32_t count = 0;
-  int s1 = 0, kbits = 0;
-  bool finite = true, accumulated = false;
   if (any) {
     // per-axis key tables of the region's cells (periodic wrap, then brick and local index)
     for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
@@ -810,240 +844,149 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
     }
     __syncthreads();
     {
+      // four cells per thread in flight: their keys first, then all eight loads
       int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
       const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
-      for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
-        const uint32_t key = kx[ex] + ky[ey] + kz[ez];
-        const uint32_t r0 = __ldg(cell_start + key);
-        r0s[e] = r0;
-        off[e] = __ldg(cell_start + key + 1) - r0;
-        ex += sx;
-        ey += sy;
-        ez += sz;
-        if (ex >= E0) { ex -= E0; ++ey; }
-        if (ey >= E1) { ey -= E1; ++ez; }
-      }
-    }
-    __syncthreads();
-    // coverage of every node (points whose stencil reaches it): window sums of the cell
-    // counts, over x and y into acc_hi as scratch, then over z
-    const int B0 = g.b[0], B1 = g.b[1];
-    if (threadIdx.x == 0) kcnt[bvol] = 0u;
-    if (E2 <= g.b[2] * CP) {
-      for (int o = threadIdx.x; o < B0 * B1 * E2; o += blockDim.x) {
-        const int lx = o % B0, r = o / B0, ly = r % B1, ez = r / B1;
-        uint32_t sum = 0;
+      for (int e = threadIdx.x; e < ecount; e += 4 * (int)blockDim.x) {
+        uint32_t key[4], a[4], z[4];
 #pragma unroll
-        for (int j = 0; j < N2; ++j) {
-          const uint32_t *row = off + (ez * E1 + ly + j) * E0 + lx;
-#pragma unroll
-          for (int i = 0; i < N2; ++i) sum += row[i];
+        for (int u = 0; u < 4; ++u) {
+          key[u] = e + u * (int)blockDim.x < ecount ? kx[ex] + ky[ey] + kz[ez] : 0u;
+          ex += sx;
+          ey += sy;
+          ez += sz;
+          if (ex >= E0) { ex -= E0; ++ey; }
+          if (ey >= E1) { ey -= E1; ++ez; }
         }
-        acc_hi[o] = sum;
-      }
-      __syncthreads();
-      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
-        uint32_t sum = 0;
 #pragma unroll
-        for (int k = 0; k < N2; ++k) sum += acc_hi[nl + k * B0 * B1];
-        kcnt[nl] = sum;
-      }
-    } else {
-      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
-        const int lx = nl % B0, ly = (nl / B0) % B1, lz = nl / (B0 * B1);
-        uint32_t sum = 0;
-        for (int k = 0; k < N2; ++k)
-          for (int j = 0; j < N2; ++j)
-            for (int i = 0; i < N2; ++i) sum += off[((lz + k) * E1 + ly + j) * E0 + lx + i];
-        kcnt[nl] = sum;
+        for (int u = 0; u < 4; ++u) {
+          a[u] = __ldg(cell_start + key[u]);
+          z[u] = __ldg(cell_start + key[u] + 1);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int eu = e + u * (int)blockDim.x;
+          if (eu < ecount) {
+            r0s[eu] = a[u];
+            off[eu] = z[u] - a[u];
+          }
+        }
       }
     }
     __syncthreads();
-    {
-      uint32_t mx = 0;
-      for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) mx = max(mx, kcnt[nl]);
-      mx = __reduce_max_sync(0xffffffffu, mx);
-      if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
-    }
-    for (int i = threadIdx.x; i < 2 * bvol * CP; i += blockDim.x) acc_hi[i] = 0u;
-    __syncthreads();
-    const uint32_t kmax = kcnt[bvol];
     count = block_scan_counts(off, ecount, warp_tot);
-    const double one = (double)qmax * g.l3, bound = one * (double)kmax;
-    finite = isfinite(bound);
-    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
-    int e1 = 0, es = 0;
-    frexp(one, &e1);
-    frexp(bound, &es);
-    s1 = max(-120, min(120, min(20 - e1, 29 - es)));
-    kbits = min(21, 30 - (32 - __clz((int)max(kmax, 1u))));
-    const float S1 = exp2f((float)s1), LS = exp2f((float)kbits);
-    accumulated = finite && count > 0 && one > 0.0;
-    if (accumulated) {
-      for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk32) {
-        const uint32_t c1 = min(count, c0 + kFlatChunk32);
-        {
-          int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
-          const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
-          for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
-            const uint32_t lo = max(off[e], c0), hi = min(e + 1 < ecount ? off[e + 1] : count, c1);
-            const uint32_t base = r0s[e] - off[e];
-            const uint32_t packed = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16);
-            for (uint32_t t = lo; t < hi; ++t) {
-              pslot[t - c0] = base + t;
-              pxyz[t - c0] = packed;
-            }
-            ex += sx;
-            ey += sy;
-            ez += sz;
-            if (ex >= E0) { ex -= E0; ++ey; }
-            if (ey >= E1) { ey -= E1; ++ez; }
-          }
-        }
-        __syncthreads();
-        if constexpr (N2 <= 4) {
-          // stencils of up to 64 nodes: a thread per point
-          for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
-            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
-            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-            const float4 r = __ldg(rec + sl);
-            float wx[N2], wy[N2], wz[N2];
-            if constexpr (FIXED) {
-              weights_ptr<N2>(coef, r.x, wx);
-              weights_ptr<N2>(coef, r.y, wy);
-              weights_ptr<N2>(coef, r.z, wz);
-            } else {
-              weights_rt<N2>(coef, m2, r.x, wx);
-              weights_rt<N2>(coef, m2, r.y, wy);
-              weights_rt<N2>(coef, m2, r.z, wz);
-            }
-            float q[CP];
-            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
-  #pragma unroll
-            for (int v = 0; v < CP / 4; ++v) {
-              const float4 tq = __ldg(q4 + v);
-              q[4 * v] = tq.x;
-              q[4 * v + 1] = tq.y;
-              q[4 * v + 2] = tq.z;
-              q[4 * v + 3] = tq.w;
-            }
-            // node l = e + k - (N2 - 1) along each axis; the k that land inside the brick
-            const int kz0 = max(0, N2 - 1 - ez), kz1 = min(N2, vz + N2 - 1 - ez);
-            const int ky0 = max(0, N2 - 1 - ey), ky1 = min(N2, vy + N2 - 1 - ey);
-            const int lx0 = ex - (N2 - 1);
-  #pragma unroll 1
-            for (int k = kz0; k < kz1; ++k) {
-              const int lz = ez + k - (N2 - 1);
-              const float wzk = pick(wz, k) * S1;
-  #pragma unroll 1
-              for (int j = ky0; j < ky1; ++j) {
-                const int ly = ey + j - (N2 - 1);
-                const float wyz = pick(wy, j) * wzk;
-                const int row = (lz * g.b[1] + ly) * g.b[0];
-  #pragma unroll
-                for (int i = 0; i < N2; ++i) {
-                  const int lx = lx0 + i;
-                  if (lx < 0 || lx >= vx) continue;
-                  const float w = wx[i] * wyz;
-  #pragma unroll
-                  for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + row + lx, w, q[c], LS);
-                }
-              }
-            }
-          }
-        } else {
-          // a warp per point: its lanes cover the point's nodes inside the brick (the sub-box
-          // i0..i1 x j0..j1 x k0..k1); lanes 0..3*N2-1 evaluate one axis weight each and each
-          // node's three weights arrive by shuffle (product order wz*S1, *wy, *wx)
-          const int lane = (int)threadIdx.x & 31;
-          for (uint32_t t = c0 + (threadIdx.x >> 5); t < c1; t += (blockDim.x >> 5)) {
-            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
-            const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
-            const int i0 = max(0, N2 - 1 - ex), i1 = min(N2, vx + N2 - 1 - ex);
-            const int j0 = max(0, N2 - 1 - ey), j1 = min(N2, vy + N2 - 1 - ey);
-            const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
-            const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
-            if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-            const float4 r = __ldg(rec + sl);
-            float wl = 0.0f;
-            if (lane < 3 * N2) {
-              const int a = lane / N2, qn = lane - a * N2;
-              const float tt = a == 0 ? r.x : (a == 1 ? r.y : r.z);
-              const int mm = FIXED ? N2 : m2;
-              wl = coef[qn + N2 * (mm - 1)];
-              for (int p = mm - 2; p >= 0; --p) wl = fmaf(wl, tt, coef[qn + N2 * p]);
-              if (a == 2) wl *= S1;  // the z weights carry the brick's scale (a power of two)
-            }
-            float q[CP];
-            const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
-  #pragma unroll
-            for (int v = 0; v < CP / 4; ++v) {
-              const float4 tq = __ldg(q4 + v);
-              q[4 * v] = tq.x;
-              q[4 * v + 1] = tq.y;
-              q[4 * v + 2] = tq.z;
-              q[4 * v + 3] = tq.w;
-            }
-            const int count = nx * ny * nz;
-            // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
-            const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
-            const int node0 = ((ez - (N2 - 1)) * B1 + ey - (N2 - 1)) * B0 + ex - (N2 - 1);
-            for (int base = 0; base < count; base += 32) {
-              const int idx = base + lane;
-              const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
-              const int kk = (int)(((uint32_t)r1 * rny) >> 16), jj = r1 - kk * ny;
-              const int i = min(i0 + ii, N2 - 1), j = min(j0 + jj, N2 - 1), k = min(k0 + kk, N2 - 1);
-              const float wxi = __shfl_sync(0xffffffffu, wl, i);
-              const float wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
-              const float wzs = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);  // wz * S1
-              if (idx < count) {
-                const float w = wxi * (wyj * wzs);
-                const int node = node0 + (k * B1 + j) * B0 + i;
-  #pragma unroll
-                for (int c = 0; c < CP; ++c) add_fixed(acc_hi, acc_lo, c * bvol + node, w, q[c], LS);
-              }
-            }
-          }
-        }
-        __syncthreads();
+    if (threadIdx.x == 0) off[ecount] = count;
+  }
+  // a region that fits at once stages over the running sums' space too
+  const bool one = count <= (uint32_t)g.chunk1;
+  const int P = one ? g.chunk1 : g.chunk;
+  float *sq = one ? sacc : sacc + bvol * CP;
+  float *sw = sq + P * CP;
+  for (uint32_t c0 = 0;; c0 += (uint32_t)P) {
+    const uint32_t c1 = min(count, c0 + (uint32_t)P);
+    const bool first = c0 == 0, last = c1 == count;
+    __syncthreads();  // the previous chunk's points (and off[ecount]) are settled
+    // stage the chunk: each point's region cell by binary search of the offsets, its
+    // weights on the three axes and its quantities
+    for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
+      int lo = 0, hi = ecount;  // the last cell e with off[e] <= t
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= t) lo = mid; else hi = mid;
       }
+      const uint32_t sl = r0s[lo] + (t - off[lo]);
+      const int tl = (int)(t - c0);
+      scx[tl] = (unsigned char)(lo % E0);
+      const float4 r = __ldg(rec + sl);
+      float w[N2];
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.x, w); else weights_rt<N2>(coef, m2, r.x, w);
+#pragma unroll
+      for (int q = 0; q < N2; ++q) sw[tl * W3 + q] = w[q];
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.y, w); else weights_rt<N2>(coef, m2, r.y, w);
+#pragma unroll
+      for (int q = 0; q < N2; ++q) sw[tl * W3 + N2 + q] = w[q];
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.z, w); else weights_rt<N2>(coef, m2, r.z, w);
+#pragma unroll
+      for (int q = 0; q < N2; ++q) sw[tl * W3 + 2 * N2 + q] = w[q];
+      const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+#pragma unroll
+      for (int v = 0; v < CP / 4; ++v) reinterpret_cast<float4 *>(sq + tl * CP)[v] = __ldg(q4 + v);
     }
     __syncthreads();
-  }
-  // ordered write-back: every node of the brick is written once, its CP components as
-  // float4 stores (FP32: hi * 2^-s1 + lo * 2^-(s1+k), both exact scalings)
-  const float to_value = exp2f((float)-s1), lo_value = exp2f((float)(-s1 - kbits));
-  {
-    const int B0 = g.b[0], B1 = g.b[1];
     int lx = (int)threadIdx.x % B0, ly = ((int)threadIdx.x / B0) % B1, lz = (int)threadIdx.x / (B0 * B1);
     const int sx = (int)blockDim.x % B0, sy = ((int)blockDim.x / B0) % B1, sz = (int)blockDim.x / (B0 * B1);
     for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
       if (lx < vx && ly < vy && lz < vz) {
-        const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ly, z = (int64_t)bz * g.b[2] + lz;
-        float4 *d = reinterpret_cast<float4 *>(field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP);
+        float acc[CP];
+        if (first) {
 #pragma unroll
-        for (int v4 = 0; v4 < CP / 4; ++v4) {
-          float v[4];
+          for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
+        } else {
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int c = 4 * v4 + u;
-            const int a = c * bvol + nl;
-            float val = 0.0f;
-            if (accumulated) {
-              const unsigned bias = kcnt[nl] * (unsigned)kMagicBits;  // modulo 2^32
-              val = fmaf((float)(int)(acc_hi[a] - bias), to_value, (float)(int)(acc_lo[a] - bias) * lo_value);
-            } else if (!finite) {
-              val = __int_as_float(0x7fc00000);
+          for (int v = 0; v < CP / 4; ++v) {
+            const float4 a = reinterpret_cast<const float4 *>(sacc + nl * CP)[v];
+            acc[4 * v] = a.x;
+            acc[4 * v + 1] = a.y;
+            acc[4 * v + 2] = a.z;
+            acc[4 * v + 3] = a.w;
+          }
+        }
+        if (count > 0) {
+          // the node's rows: region cells (lx..lx+N2-1, ly+j, lz+k); stencil index N2-1-j
+          // on y, N2-1-k on z and lx+N2-1-ex on x for a point in region cell ex
+          const int xk = lx + N2 - 1;
+          bool done = false;
+#pragma unroll 1
+          for (int k = 0; k < N2 && !done; ++k) {
+            const int zk = 2 * N2 + (N2 - 1 - k);
+#pragma unroll 1
+            for (int j = 0; j < N2; ++j) {
+              const int e0 = ((lz + k) * E1 + ly + j) * E0 + lx;
+              const uint32_t a = off[e0];
+              if (a >= c1) {  // this row and every later one start past the chunk
+                done = true;
+                break;
+              }
+              const uint32_t p1 = min(off[e0 + N2], c1);
+              const int yk = N2 + (N2 - 1 - j);
+              for (uint32_t p = max(a, c0); p < p1; ++p) {
+                const int tl = (int)(p - c0);
+                const float *w = sw + tl * W3;
+                const float wgt = w[xk - (int)scx[tl]] * (w[yk] * w[zk]);
+                const float4 *qv = reinterpret_cast<const float4 *>(sq + tl * CP);
+#pragma unroll
+                for (int v = 0; v < CP / 4; ++v) {
+                  const float4 qq = qv[v];
+                  acc[4 * v] = fmaf(wgt, qq.x, acc[4 * v]);
+                  acc[4 * v + 1] = fmaf(wgt, qq.y, acc[4 * v + 1]);
+                  acc[4 * v + 2] = fmaf(wgt, qq.z, acc[4 * v + 2]);
+                  acc[4 * v + 3] = fmaf(wgt, qq.w, acc[4 * v + 3]);
+                }
+              }
             }
-            v[u] = c < g.ncomp ? val : 0.0f;
           }
-          if (beta_zero) {
-            d[v4] = make_float4(v[0], v[1], v[2], v[3]);
-          } else {
-            const float4 o = d[v4];
-            d[v4] = make_float4(__fadd_rn(__fmul_rn(beta, o.x), v[0]), __fadd_rn(__fmul_rn(beta, o.y), v[1]),
-                                __fadd_rn(__fmul_rn(beta, o.z), v[2]), __fadd_rn(__fmul_rn(beta, o.w), v[3]));
+        }
+        if (last) {
+          const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ly, z = (int64_t)bz * g.b[2] + lz;
+          float4 *d = reinterpret_cast<float4 *>(field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP);
+#pragma unroll
+          for (int v4 = 0; v4 < CP / 4; ++v4) {
+            float v[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) v[u] = 4 * v4 + u < g.ncomp ? acc[4 * v4 + u] : 0.0f;
+            if (beta_zero) {
+              d[v4] = make_float4(v[0], v[1], v[2], v[3]);
+            } else {
+              const float4 o = d[v4];
+              d[v4] = make_float4(__fadd_rn(__fmul_rn(beta, o.x), v[0]), __fadd_rn(__fmul_rn(beta, o.y), v[1]),
+                                  __fadd_rn(__fmul_rn(beta, o.z), v[2]), __fadd_rn(__fmul_rn(beta, o.w), v[3]));
+            }
           }
+        } else {
+#pragma unroll
+          for (int v = 0; v < CP / 4; ++v)
+            reinterpret_cast<float4 *>(sacc + nl * CP)[v] =
+                make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
         }
       }
       lx += sx;
@@ -1052,25 +995,31 @@ __device__ void scatter_brick32(const FixGeo &g, const float *coef, int m2, int6
       if (lx >= B0) { lx -= B0; ++ly; }
       if (ly >= B1) { ly -= B1; ++lz; }
     }
+    if (last) break;
   }
   __syncthreads();
 }
 
 template <int N2, bool FIXED, int CP>
 __global__ void __launch_bounds__(kThreads, 2)
-    k_scatter_fixed(FixGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
+    k_scatter_nodes(FixGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
                     const float4 *__restrict__ rec, const float *__restrict__ qs,
                     const unsigned *__restrict__ qmax_bits, float *__restrict__ field, float beta,
-                    int beta_zero, int32_t *status) {
+                    int beta_zero, int32_t *status, const uint32_t *__restrict__ list,
+                    const uint32_t *__restrict__ list_n) {
   extern __shared__ __align__(16) unsigned char smem_scatter[];
   __shared__ uint32_t warp_tot[32];
   __shared__ float coef[N2 * GBG_MAX_POWERS];
   for (int i = threadIdx.x; i < N2 * s.m2; i += blockDim.x) coef[i] = s.c[i];
   __syncthreads();
-  const float qmax = __uint_as_float(*qmax_bits);
-  for (int64_t b = blockIdx.x; b < g.nbricks; b += gridDim.x)
-    scatter_brick32<N2, FIXED, CP>(g, coef, s.m2, b, cell_start, rec, qs, qmax, field, beta, beta_zero, smem_scatter,
-                                   warp_tot, status);
+  // a non-finite quantity propagates into the nodes it reaches; the status says so
+  if (blockIdx.x == 0 && threadIdx.x == 0 && status && !isfinite(__uint_as_float(*qmax_bits)))
+    atomicOr(status, GBG_DEV_NONFINITE);
+  // the bricks to write: those a point reaches (beta == 1 leaves the others unchanged), or all
+  const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
+  for (int64_t ui = blockIdx.x; ui < nunits; ui += gridDim.x)
+    scatter_brick_nodes<N2, FIXED, CP>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start, rec, qs,
+                                       field, beta, beta_zero, smem_scatter, warp_tot);
 }
 
 gbg_status check_field_bins(const gbg_field_s *f, const gbg_bins_s *b, const gbg_scheme *s) {
@@ -1143,7 +1092,7 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
     const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
     mark_main_start(st);
     kernel<<<blocks, threads, smem, st>>>(*map, g, s, b->cell_start, b->rec, b->perm, out, status, nbuf, tile_bytes,
-                                           box_bytes);
+                                           box_bytes, b->active, b->lists_n);
     mark_main_stop(st);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
@@ -1188,31 +1137,34 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   g.halo = f->halo;
   g.cp = f->cp;
   g.ncomp = f->ncomp;
-  const double L = weight_bound(sch, std::ldexp(1.0, -16));
-  g.l3 = L * L * L;
   const SchemeT<float, N2> s = make_scheme<float, N2>(sch);
-  const size_t smem = scatter32_smem(g, f->cp);
-  if (smem > 200 * 1024 || (size_t)g.e[0] * g.e[1] * g.e[2] > 65535)
-    return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared accumulators");
+  if (g.e[0] > 255) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter");
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int threads = b->scatter_threads ? b->scatter_threads : kThreads;
   auto go = [&](auto kernel) -> gbg_status {
+    cudaFuncAttributes fa{};
+    GBG_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+    scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(fa.numRegs, threads));
+    const size_t smem = scatter_nodes_smem(g, f->cp, N2);
+    if (smem > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared memory");
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
     mark_main_start(st);
+    const bool reach = beta == 1.0 && b->reach_ok;
     kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
-                                           beta == 0.0, status);
+                                           beta == 0.0, status, reach ? b->reach : nullptr, b->lists_n + 1);
     mark_main_stop(st);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   };
-  if (f->cp == 4) return go(k_scatter_fixed<N2, FIXED, 4>);
-  return go(k_scatter_fixed<N2, FIXED, 12>);
+  if (f->cp == 4) return go(k_scatter_nodes<N2, FIXED, 4>);
+  return go(k_scatter_nodes<N2, FIXED, 12>);
 }
 
 // ------------------------------------------------------------ batched form
@@ -1231,6 +1183,8 @@ struct BatchDev {
   float *dest;   // scatter destination storage or null
   const float *qs;
   const unsigned *qmax_bits;
+  // the bricks each launch visits: a list and its length on the device, or null for all
+  const uint32_t *glist, *gcount, *slist, *scount;
   float coef[8 * 8];  // [q + n2*p], n2 == m2 <= 8
   int32_t n2, cp;
   uint32_t box_bytes;
@@ -1241,15 +1195,21 @@ struct BatchDev {
 constexpr int kBatchGatherThreads = 512;
 
 // Work unit u of a batch launch -> (instance, brick): the k-th instance in cost order,
-// idx[k], owns the units [off[k], off[k+1]) (off[0] = 0, u < off[n]).
-__device__ __forceinline__ uint2 batch_unit(uint32_t u, const uint32_t *__restrict__ off,
-                                            const uint32_t *__restrict__ idx, int n) {
+// idx[k], owns the units [off[k], off[k+1]) (off[0] = 0, u < off[n]); its j-th unit is
+// the j-th brick of its list (gather: the bricks holding points; scatter: the bricks in
+// reach of a point when beta == 1), or brick j when it has no list.
+template <bool SCATTER>
+__device__ __forceinline__ uint2 batch_unit(const BatchDev *__restrict__ items, uint32_t u,
+                                            const uint32_t *__restrict__ off, const uint32_t *__restrict__ idx,
+                                            int n) {
   int lo = 0, hi = n;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
     if (__ldg(off + mid) <= u) lo = mid; else hi = mid;
   }
-  return make_uint2(__ldg(idx + lo), u - __ldg(off + lo));
+  const uint32_t i = __ldg(idx + lo), j = u - __ldg(off + lo);
+  const uint32_t *list = SCATTER ? items[i].slist : items[i].glist;
+  return make_uint2(i, list ? __ldg(list + j) : j);
 }
 
 // The points of one brick, from its staged tile: a point per quarter-warp (width 4) or
@@ -1370,9 +1330,10 @@ __device__ __forceinline__ bool batch_issue(const BatchDev *items, const CUtenso
 
 __global__ void __launch_bounds__(kBatchGatherThreads, 1)
     k_batch_gather(const BatchDev *__restrict__ items, const CUtensorMap *__restrict__ maps,
-                   const uint32_t *__restrict__ off, const uint32_t *__restrict__ idx, int n, uint32_t nwork,
+                   const uint32_t *__restrict__ off, const uint32_t *__restrict__ idx, int n,
                    uint32_t *counter, uint32_t buf_bytes, int nbuf, int32_t *status) {
   extern __shared__ __align__(1024) unsigned char smem[];
+  const uint32_t nwork = off[n];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + nbuf * buf_bytes);
   __shared__ uint32_t s_unit[2];
   __shared__ int s_issued[2];
@@ -1382,7 +1343,7 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     const uint32_t u = atomicAdd(counter, 1u);
     s_unit[0] = u;
-    s_issued[0] = u < nwork ? batch_issue(items, maps, batch_unit(u, off, idx, n), smem, bars) : 0;
+    s_issued[0] = u < nwork ? batch_issue(items, maps, batch_unit<false>(items, u, off, idx, n), smem, bars) : 0;
   }
   __syncthreads();
   uint32_t phase[2] = {0, 0};
@@ -1395,7 +1356,7 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
       const uint32_t un = atomicAdd(counter, 1u);
       s_unit[buf ^ 1] = un;
       s_issued[buf ^ 1] =
-          un < nwork ? batch_issue(items, maps, batch_unit(un, off, idx, n), smem + (buf ^ 1) * buf_bytes, bars + (buf ^ 1))
+          un < nwork ? batch_issue(items, maps, batch_unit<false>(items, un, off, idx, n), smem + (buf ^ 1) * buf_bytes, bars + (buf ^ 1))
                      : 0;
     }
     if (s_issued[buf]) {
@@ -1405,7 +1366,7 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
         break;
       }
       phase[buf] ^= 1;
-      const uint2 wu = batch_unit(u, off, idx, n);
+      const uint2 wu = batch_unit<false>(items, u, off, idx, n);
       const BatchDev *d = items + wu.x;
       const uint32_t s0 = __ldg(d->cell_start + (int64_t)wu.y * d->g.bvol);
       const uint32_t s1 = __ldg(d->cell_start + ((int64_t)wu.y + 1) * d->g.bvol);
@@ -1427,7 +1388,7 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
       if (threadIdx.x == 0) {
         const uint32_t un = atomicAdd(counter, 1u);
         s_unit[0] = un;
-        s_issued[0] = un < nwork ? batch_issue(items, maps, batch_unit(un, off, idx, n), smem, bars) : 0;
+        s_issued[0] = un < nwork ? batch_issue(items, maps, batch_unit<false>(items, un, off, idx, n), smem, bars) : 0;
       }
       __syncthreads();
     } else {
@@ -1438,11 +1399,12 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
     for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
 }
 
-// The scatter of every brick of every instance: units taken from the device counter.
+// The scatter of every listed brick of every instance: units taken from the device counter.
 __global__ void __launch_bounds__(kThreads, 2)
     k_batch_scatter(const BatchDev *__restrict__ items, const uint32_t *__restrict__ off,
-                    const uint32_t *__restrict__ idx, int n, uint32_t nwork, uint32_t *counter, int32_t *status) {
+                    const uint32_t *__restrict__ idx, int n, uint32_t *counter, int32_t *status) {
   extern __shared__ __align__(16) unsigned char bsmem[];
+  const uint32_t nwork = off[n];
   __shared__ uint32_t s_u;
   __shared__ uint32_t warp_tot[32];
   while (true) {
@@ -1451,13 +1413,13 @@ __global__ void __launch_bounds__(kThreads, 2)
     const uint32_t u = s_u;
     __syncthreads();
     if (u >= nwork) break;
-    const uint2 wu = batch_unit(u, off, idx, n);
+    const uint2 wu = batch_unit<true>(items, u, off, idx, n);
     const BatchDev *d = items + wu.x;
-    const float qmax = __uint_as_float(*d->qmax_bits);
+    if (threadIdx.x == 0 && status && !isfinite(__uint_as_float(*d->qmax_bits))) atomicOr(status, GBG_DEV_NONFINITE);
     const int kind = d->n2 * 100 + d->cp;
-#define GBG_BATCH_SCATTER(N2, CP)                                                                              \
-  scatter_brick32<N2, true, CP>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, qmax, d->dest, d->beta, \
-                                d->beta_zero, bsmem, warp_tot, status)
+#define GBG_BATCH_SCATTER(N2, CP)                                                                          \
+  scatter_brick_nodes<N2, true, CP>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, d->dest, d->beta, \
+                                    d->beta_zero, bsmem, warp_tot)
     switch (kind) {
       case 404: GBG_BATCH_SCATTER(4, 4); break;
       case 412: GBG_BATCH_SCATTER(4, 12); break;
@@ -1507,11 +1469,27 @@ __global__ void k_batch_qprep(const BatchDev *__restrict__ items, const float *c
   if (cur >= 0) atomicMax(qmax_out[cur], mx);
 }
 
-// Resets the batch's unit counters and the max|alpha q| word of every destination.
-__global__ void k_batch_reset(uint32_t *counters, unsigned *const *qmax_out, int32_t count) {
+// Resets the batch's unit counters and the max|alpha q| word of every destination, and
+// lays out the work units: off[k] = the units of the instances before the k-th in cost
+// order, from the list lengths the bins' builds left on the device.  One block.
+__global__ void k_batch_reset(const BatchDev *__restrict__ items, uint32_t *counters, unsigned *const *qmax_out,
+                              int32_t count, const uint32_t *__restrict__ gidx, int32_t ng, uint32_t *goff,
+                              const uint32_t *__restrict__ sidx, int32_t ns, uint32_t *soff) {
+  __shared__ uint32_t warp_tot[32];
   for (int i = threadIdx.x; i < count; i += blockDim.x)
     if (qmax_out[i]) *qmax_out[i] = 0u;
   if (threadIdx.x < 2) counters[threadIdx.x] = 0u;
+  for (int k = threadIdx.x; k <= ng; k += blockDim.x) {
+    const BatchDev *d = items + gidx[k < ng ? k : 0];
+    goff[k] = k == ng ? 0u : d->glist ? *d->gcount : (uint32_t)d->g.nbricks;
+  }
+  for (int k = threadIdx.x; k <= ns; k += blockDim.x) {
+    const BatchDev *d = items + sidx[k < ns ? k : 0];
+    soff[k] = k == ns ? 0u : d->slist ? *d->scount : (uint32_t)d->fg.nbricks;
+  }
+  __syncthreads();
+  block_scan_counts(goff, ng + 1, warp_tot);
+  block_scan_counts(soff, ns + 1, warp_tot);
 }
 
 }  // namespace
@@ -1536,6 +1514,7 @@ gbg_status bins_plan(const gbg_grid &grid, int64_t max_points, const int32_t *br
   b->nbricks = b->nb[0] * b->nb[1] * b->nb[2];
   b->nkeys = b->nbricks * b->bvol;
   if (b->nkeys >= (int64_t(1) << 32) - 1) return set_error(GBG_EUNSUPPORTED, "bins: 2^32 or more cells");
+  b->reach_ok = neighbour_skip_ok(b->b, b->nb, grid.n, 8) != 0;
   Arena a;
   bins_layout(a, b);
   b->bytes = a.used + 256;
@@ -1747,6 +1726,7 @@ gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, i
                            cudaStream_t st, const DisplaceArgs<T> *disp) {
   b->npoints = npoints;
   GBG_CUDA_TRY(cudaMemsetAsync(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1), st));
+  GBG_CUDA_TRY(cudaMemsetAsync(b->lists_n, 0, sizeof(uint32_t) * 2, st));
   if (npoints == 0) return GBG_OK;
   BinGeom g;
   for (int d = 0; d < 3; ++d) {
@@ -1774,6 +1754,9 @@ gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, i
   GBG_TRY(radix_sort_pairs(b->keys, nullptr, b->skeys, b->perm, npoints, bits, b->sort_tmp, st));
   GBG_TRY(exclusive_scan_u32(b->cell_start, b->cell_start, b->nkeys + 1, b->scan_tmp, st));
   k_gather_records<<<blocks, kThreads, 0, st>>>(b->rec_user, b->perm, npoints, b->rec);
+  note_launch();
+  k_brick_lists<<<launch_blocks(b->nbricks, kThreads), kThreads, 0, st>>>(
+      b->cell_start, b->nb[0], b->nb[1], b->nb[2], b->bvol, b->reach_ok ? 1 : 0, b->active, b->reach, b->lists_n);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
@@ -1951,7 +1934,7 @@ struct gbg_batch_s {
   gbg::BatchDev *items = nullptr;
   CUtensorMap *maps = nullptr;
   uint32_t *goff = nullptr, *gidx = nullptr, *soff = nullptr, *sidx = nullptr;
-  uint32_t ngwork = 0, nswork = 0;
+  uint32_t ngwork = 0, nswork = 0;  // bounds on the units (every brick); the lists may hold fewer
   uint32_t *counters = nullptr;
   const float **qptrs = nullptr;
   float **qs_out = nullptr;
@@ -2026,6 +2009,9 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   std::vector<double> cost(count);
   uint32_t buf_max = 0;
   size_t scat_max = 0;
+  cudaFuncAttributes scat_fa{};
+  cudaFuncGetAttributes(&scat_fa, k_batch_scatter);
+  const size_t scat_budget = scatter_nodes_budget(scat_fa.numRegs, kThreads);
   for (int32_t i = 0; i < count; ++i) {
     const gbg_batch_item &it = items[i];
     gbg_field_s *f = it.field;
@@ -2048,6 +2034,11 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
     d.dest = it.dest ? it.dest->data : nullptr;
     d.qs = b->qs;
     d.qmax_bits = b->qmax_bits;
+    d.glist = b->active;
+    d.gcount = b->lists_n;
+    const bool reach = it.beta == 1.0 && b->reach_ok;
+    d.slist = reach ? b->reach : nullptr;
+    d.scount = reach ? b->lists_n + 1 : nullptr;
     for (int k = 0; k < 64; ++k) d.coef[k] = 0.0f;
     for (int q = 0; q < w; ++q)
       for (int p = 0; p < w; ++p) d.coef[q + w * p] = (float)it.scheme.coefficients[q + w * p];
@@ -2072,11 +2063,9 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
       d.fg.halo = ds->halo;
       d.fg.cp = ds->cp;
       d.fg.ncomp = ds->ncomp;
-      const double L = weight_bound(it.scheme, std::ldexp(1.0, -16));
-      d.fg.l3 = L * L * L;
-      scat_max = std::max(scat_max, scatter32_smem(d.fg, ds->cp));
-      if ((size_t)d.fg.e[0] * d.fg.e[1] * d.fg.e[2] > 65535)
-        return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");
+      scatter_nodes_chunk(d.fg, ds->cp, w, scat_budget);
+      scat_max = std::max(scat_max, scatter_nodes_smem(d.fg, ds->cp, w));
+      if (d.fg.e[0] > 255) return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");
       h.qptrs[i] = it.q;
       h.qs_out[i] = b->qs;
       h.qmax_out[i] = b->qmax_bits;
@@ -2096,7 +2085,8 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   }
   for (int32_t i = 0; i < count; ++i) h.qoff[i + 1] += h.qoff[i];
   bt->total_q = h.qoff[count];
-  // units: every brick of every instance, largest instances first
+  // instances in cost order, largest first; the offsets written here (every brick) are
+  // the bounds the launch shapes use, k_batch_reset rewrites them from the lists
   std::vector<int32_t> order(count);
   for (int32_t i = 0; i < count; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t c) { return cost[a] > cost[c]; });
@@ -2129,7 +2119,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   bt->nbuf = 2 * (size_t)buf_max + 64 <= 200 * 1024 ? 2 : 1;
   bt->gather_smem = (size_t)bt->nbuf * buf_max + 64;
   bt->scatter_smem = scat_max;
-  if (bt->gather_smem > 227 * 1024 || bt->scatter_smem > 200 * 1024)
+  if (bt->gather_smem > 227 * 1024 || bt->scatter_smem > 227 * 1024)
     return set_error(GBG_EUNSUPPORTED, "batch: a brick's tile does not fit in shared memory");
   bt->bytes = batch_layout(count).bytes;
   return GBG_OK;
@@ -2234,7 +2224,8 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
   clear_error();
   if (!bt) return set_error(GBG_EARG, "null batch");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  k_batch_reset<<<1, 256, 0, st>>>(bt->counters, bt->qmax_out, bt->count);
+  k_batch_reset<<<1, 256, 0, st>>>(bt->items, bt->counters, bt->qmax_out, bt->count, bt->gidx, bt->ng, bt->goff,
+                                   bt->sidx, bt->ns, bt->soff);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   int sms = 0;
@@ -2250,16 +2241,18 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
                                       (int)bt->gather_smem));
     const int blocks = (int)std::min<uint32_t>(bt->ngwork, (uint32_t)sms);
     k_batch_gather<<<blocks, kBatchGatherThreads, bt->gather_smem, st>>>(
-        bt->items, bt->maps, bt->goff, bt->gidx, bt->ng, bt->ngwork, bt->counters, bt->buf_bytes, bt->nbuf,
-        device_status);
+        bt->items, bt->maps, bt->goff, bt->gidx, bt->ng, bt->counters, bt->buf_bytes, bt->nbuf, device_status);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
   }
   if (bt->nswork > 0) {
     GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)bt->scatter_smem));
-    const int blocks = (int)std::min<uint32_t>(bt->nswork, (uint32_t)(2 * sms));
-    k_batch_scatter<<<blocks, kThreads, bt->scatter_smem, st>>>(bt->items, bt->soff, bt->sidx, bt->ns, bt->nswork,
+    GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_scatter, kThreads, bt->scatter_smem);
+    const int blocks = (int)std::min<uint32_t>(bt->nswork, (uint32_t)(std::max(per_sm, 1) * sms));
+    k_batch_scatter<<<blocks, kThreads, bt->scatter_smem, st>>>(bt->items, bt->soff, bt->sidx, bt->ns,
                                                                 bt->counters + 1, device_status);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());

@@ -264,9 +264,10 @@ gbg_status gbg_bins_order(gbg_bins bins, int32_t *order, void *stream);
 gbg_status gbg_interpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype out_dtype, void *out, void *stream);
 /* Deterministic scatter of q (M, ncomp) of q_dtype at binned points into a resident
- * field: field = alpha * W^T q + beta * field.  No float atomics: each node's sum is
- * kept as two 32-bit fixed-point words (the rounded contribution and its residual), so
- * the result is bitwise reproducible; the ghost layer is refreshed. */
+ * field: field = alpha * W^T q + beta * field.  No atomics: each node's sum is formed
+ * by one thread in a fixed order (the node's rows of cells, within a row the points in
+ * binned order), so the result is bitwise reproducible and independent of the launch
+ * shape; the ghost layer is refreshed. */
 gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype q_dtype, const void *q, double alpha, double beta,
                                   void *stream);
