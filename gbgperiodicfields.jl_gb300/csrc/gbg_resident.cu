@@ -751,7 +751,7 @@ __device__ __forceinline__ void weights_rt(const float *c, int m2, float t, floa
 }
 
 // Shared memory of one scatter CTA, in this order: the brick's running sums (CP floats per
-// node), one chunk of the region's points (CP quantities and 3*N2 weights each), the
+// node), one chunk of the region's points (CP quantities and 3*N2+4 weights each), the
 // region's per-cell point offsets (+ the total) and first slots, the per-axis key tables
 // of the region's cells, and the points' region x cells.
 size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
@@ -760,33 +760,50 @@ size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
          16;
 }
 
+// Floats of weights per staged point: the N2 x weights, then the y and the z weights each
+// with a zero on either side (so that a node's index past the stencil reads a zero),
+// rounded up to an odd count: lanes reading the same weight of different points then
+// fall in different banks (an even stride such as 16 would put 32 lanes in 2 banks).
+template <int N2>
+constexpr int kScatterWStride = (3 * N2 + 4) | 1;
+inline int scatter_wstride(int n2) { return (3 * n2 + 4) | 1; }
+
 size_t scatter_nodes_smem(const FixGeo &g, int cp, int n2) {
-  return scatter_nodes_fixed(g, cp) + sizeof(float) * (size_t)g.chunk * (cp + 3 * n2) + (size_t)g.chunk1;
+  return scatter_nodes_fixed(g, cp) + sizeof(float) * (size_t)g.chunk * (cp + scatter_wstride(n2)) + (size_t)g.chunk1;
 }
 
 // Sets the chunk sizes: the largest chunk (a multiple of 4, 64..1024 points) whose CTA
 // fits in `budget` bytes, and the larger one that also takes the running sums' space when
 // the whole region fits in one chunk.
 void scatter_nodes_chunk(FixGeo &g, int cp, int n2, size_t budget) {
-  const size_t per = sizeof(float) * (cp + 3 * n2) + 1, fixed = scatter_nodes_fixed(g, cp);
+  const size_t per = sizeof(float) * (cp + scatter_wstride(n2)) + 1, fixed = scatter_nodes_fixed(g, cp);
   const size_t fit = budget > fixed ? (budget - fixed) / per : 0;
   g.chunk = (int32_t)std::max<size_t>(64, std::min<size_t>(1024, fit & ~size_t(3)));
   g.chunk1 = g.chunk + (int32_t)(((size_t)g.bvol * cp * sizeof(float) / per) & ~size_t(3));
 }
 
 // Shared memory per scatter CTA: the SM's share for as many CTAs as the kernel's registers
-// allow (at most 4), less the block's reserved and static share.
-size_t scatter_nodes_budget(int regs, int threads) {
-  const int by_regs = std::max(1, std::min(4, 65536 / std::max(1, regs * threads)));
-  return std::min<size_t>(200 * 1024, 228 * 1024 / by_regs - 4096);
+// allow (at most 4), less the block's reserved and static share -- but never so little
+// that a region of 512 points needs more than one chunk (a brick's region holds a few
+// hundred at the usual densities, and each extra chunk re-stages and re-walks the rows;
+// a single chunk may also use the running sums' space).
+size_t scatter_nodes_budget(int regs, int threads, const FixGeo &g, int cp, int n2) {
+  const size_t per = sizeof(float) * (cp + scatter_wstride(n2)) + 1;
+  const size_t sums = sizeof(float) * (size_t)g.bvol * cp;
+  const size_t want = scatter_nodes_fixed(g, cp) + (512 * per > sums ? 512 * per - sums : 0) + 4 * per;
+  int ctas = std::max(1, std::min(4, 65536 / std::max(1, regs * threads)));
+  while (ctas > 1 && 228 * 1024 / ctas - 4096 < want) --ctas;
+  return std::min<size_t>(200 * 1024, 228 * 1024 / ctas - 4096);
 }
 
 // Deterministic scatter, output-driven.  A CTA owns a brick's nodes and a thread owns a
-// node: it sums, in registers, the contributions w*alpha*q of every point whose stencil
-// reaches the node, in a fixed order -- the node's N2 x N2 rows of cells (z outer, y
-// inner), within a row the points in their binned order.  The order depends on the
-// points alone, not on the launch shape, the chunking or the other instances of a batch,
-// so the result is reproducible bitwise; no atomics are involved.
+// 2 x 2 quad of nodes in y and z (one node for width 8): it sums, in registers, the
+// contributions ((wx*wy)*wz)*alpha*q of every point whose stencil reaches each node, in a
+// fixed order per node -- the node's N2 x N2 rows of cells (z outer, y inner), within a
+// row the points in their binned order.  A point is loaded once for all the quad's nodes
+// it reaches, and a node that a point does not reach takes no operation from it.  The
+// order depends on the points alone, not on the launch shape, the chunking or the other
+// instances of a batch, so the result is reproducible bitwise; no atomics are involved.
 //
 // The brick's region (its cells widened by N2 - 1) is listed in region order (x fastest)
 // with per-cell offsets; its points pass through shared memory in chunks of contiguous
@@ -798,14 +815,13 @@ template <int N2, bool FIXED, int CP>
 __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, int64_t b,
                                     const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                                     const float *__restrict__ qs, float *__restrict__ field, float beta,
-                                    int beta_zero, unsigned char *smem, uint32_t *warp_tot) {
+                                    int beta_zero, bool listed, unsigned char *smem, uint32_t *warp_tot) {
   const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)g.bvol;
-  constexpr int W3 = 3 * N2;
   // [running sums | chunk: quantities, weights] [offsets, first slots, key tables] [x cells]
   float *sacc = reinterpret_cast<float *>(smem);
-  uint32_t *off = reinterpret_cast<uint32_t *>(sacc + bvol * CP + g.chunk * (CP + W3));
+  uint32_t *off = reinterpret_cast<uint32_t *>(sacc + bvol * CP + g.chunk * (CP + kScatterWStride<N2>));
   uint32_t *r0s = off + ecount + 1;
   uint32_t *kx = r0s + ecount, *ky = kx + E0, *kz = ky + E1;
   unsigned char *scx = reinterpret_cast<unsigned char *>(kz + E2);
@@ -814,9 +830,11 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   const int B0 = g.b[0], B1 = g.b[1];
   // nodes of this brick inside the grid
   const int vx = min(B0, g.n[0] - bx * B0), vy = min(B1, g.n[1] - by * B1), vz = min(g.b[2], g.n[2] - bz * g.b[2]);
-  // is any point near?  (the 27 neighbouring bricks hold the whole region)
+  // is any point near?  (the 27 neighbouring bricks hold the whole region)  Only a
+  // scatter with beta == 1 may leave a brick alone, and a brick taken from the bins' list
+  // of bricks in reach of a point is known to be near.
   bool any = true;
-  if (g.neighbour_skip) {
+  if (g.neighbour_skip && !beta_zero && beta == 1.0f && !listed) {
     bool mine = false;
     if (threadIdx.x < 27) {
       const int dx = (int)threadIdx.x % 3 - 1, dy = ((int)threadIdx.x / 3) % 3 - 1, dz = (int)threadIdx.x / 9 - 1;
@@ -882,12 +900,19 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   const int P = one ? g.chunk1 : g.chunk;
   float *sq = one ? sacc : sacc + bvol * CP;
   float *sw = sq + P * CP;
+  // a thread owns BY x BZ nodes (lx, ly+a, lz+b) and walks the RY x RZ rows of region cells
+  // that feed any of them; each point it loads serves up to BY*BZ nodes
+  constexpr int BY = N2 <= 6 ? 2 : 1, BZ = BY;
+  constexpr int RY = N2 + BY - 1, RZ = N2 + BZ - 1;
+  const int QY = (B1 + BY - 1) / BY, QZ = (g.b[2] + BZ - 1) / BZ;
+  const int nquads = B0 * QY * QZ, slab = E1 * E0;
   for (uint32_t c0 = 0;; c0 += (uint32_t)P) {
     const uint32_t c1 = min(count, c0 + (uint32_t)P);
     const bool first = c0 == 0, last = c1 == count;
     __syncthreads();  // the previous chunk's points (and off[ecount]) are settled
     // stage the chunk: each point's region cell by binary search of the offsets, its
-    // weights on the three axes and its quantities
+    // weights (x, then y and z each with a zero either side) and its quantities
+    int nonfinite = 0;
     for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
       int lo = 0, hi = ecount;  // the last cell e with off[e] <= t
       while (hi - lo > 1) {
@@ -898,82 +923,170 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
       const int tl = (int)(t - c0);
       scx[tl] = (unsigned char)(lo % E0);
       const float4 r = __ldg(rec + sl);
+      float *wt = sw + tl * kScatterWStride<N2>;
       float w[N2];
       if constexpr (FIXED) weights_ptr<N2>(coef, r.x, w); else weights_rt<N2>(coef, m2, r.x, w);
 #pragma unroll
-      for (int q = 0; q < N2; ++q) sw[tl * W3 + q] = w[q];
+      for (int q = 0; q < N2; ++q) wt[q] = w[q];
       if constexpr (FIXED) weights_ptr<N2>(coef, r.y, w); else weights_rt<N2>(coef, m2, r.y, w);
+      wt[N2] = 0.0f;
 #pragma unroll
-      for (int q = 0; q < N2; ++q) sw[tl * W3 + N2 + q] = w[q];
+      for (int q = 0; q < N2; ++q) wt[N2 + 1 + q] = w[q];
+      wt[2 * N2 + 1] = 0.0f;
       if constexpr (FIXED) weights_ptr<N2>(coef, r.z, w); else weights_rt<N2>(coef, m2, r.z, w);
+      wt[2 * N2 + 2] = 0.0f;
 #pragma unroll
-      for (int q = 0; q < N2; ++q) sw[tl * W3 + 2 * N2 + q] = w[q];
+      for (int q = 0; q < N2; ++q) wt[2 * N2 + 3 + q] = w[q];
+      wt[3 * N2 + 3] = 0.0f;
       const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+      float qa = 0.0f;
 #pragma unroll
-      for (int v = 0; v < CP / 4; ++v) reinterpret_cast<float4 *>(sq + tl * CP)[v] = __ldg(q4 + v);
+      for (int v = 0; v < CP / 4; ++v) {
+        const float4 t4 = __ldg(q4 + v);
+        reinterpret_cast<float4 *>(sq + tl * CP)[v] = t4;
+        qa += fabsf(t4.x) + fabsf(t4.y) + fabsf(t4.z) + fabsf(t4.w);
+      }
+      // NaN or infinity in the point's offsets or quantities (the sum is finite otherwise)
+      if (!isfinite(r.x + r.y + r.z + qa)) nonfinite = 1;
     }
-    __syncthreads();
-    int lx = (int)threadIdx.x % B0, ly = ((int)threadIdx.x / B0) % B1, lz = (int)threadIdx.x / (B0 * B1);
-    const int sx = (int)blockDim.x % B0, sy = ((int)blockDim.x / B0) % B1, sz = (int)blockDim.x / (B0 * B1);
-    for (int nl = threadIdx.x; nl < bvol; nl += blockDim.x) {
-      if (lx < vx && ly < vy && lz < vz) {
-        float acc[CP];
-        if (first) {
+    // a chunk with a non-finite value takes the exact path: each point only touches the
+    // nodes it reaches; otherwise a point adds w*q to all of a quad's nodes, with w == 0
+    // exactly for the nodes it does not reach, and fmaf(0, q, s) == s for finite q
+    const bool exact = __syncthreads_or(nonfinite);
+    for (int qi = threadIdx.x; qi < nquads; qi += blockDim.x) {
+      const int lx = qi % B0, ly = ((qi / B0) % QY) * BY, lz = (qi / (B0 * QY)) * BZ;
+      float acc[BY * BZ][CP];
 #pragma unroll
-          for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
-        } else {
+      for (int n = 0; n < BY * BZ; ++n) {
+        const int a = n % BY, bb = n / BY;
+        const bool mine = ly + a < B1 && lz + bb < g.b[2];
 #pragma unroll
-          for (int v = 0; v < CP / 4; ++v) {
-            const float4 a = reinterpret_cast<const float4 *>(sacc + nl * CP)[v];
-            acc[4 * v] = a.x;
-            acc[4 * v + 1] = a.y;
-            acc[4 * v + 2] = a.z;
-            acc[4 * v + 3] = a.w;
-          }
+        for (int v = 0; v < CP / 4; ++v) {
+          float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (!first && mine) s4 = reinterpret_cast<const float4 *>(sacc + (((lz + bb) * B1 + ly + a) * B0 + lx) * CP)[v];
+          acc[n][4 * v] = s4.x;
+          acc[n][4 * v + 1] = s4.y;
+          acc[n][4 * v + 2] = s4.z;
+          acc[n][4 * v + 3] = s4.w;
         }
-        if (count > 0) {
-          // the node's rows: region cells (lx..lx+N2-1, ly+j, lz+k); stencil index N2-1-j
-          // on y, N2-1-k on z and lx+N2-1-ex on x for a point in region cell ex
-          const int xk = lx + N2 - 1;
-          bool done = false;
-#pragma unroll 1
-          for (int k = 0; k < N2 && !done; ++k) {
-            const int zk = 2 * N2 + (N2 - 1 - k);
-#pragma unroll 1
-            for (int j = 0; j < N2; ++j) {
-              const int e0 = ((lz + k) * E1 + ly + j) * E0 + lx;
-              const uint32_t a = off[e0];
-              if (a >= c1) {  // this row and every later one start past the chunk
-                done = true;
-                break;
-              }
-              const uint32_t p1 = min(off[e0 + N2], c1);
-              const int yk = N2 + (N2 - 1 - j);
-              for (uint32_t p = max(a, c0); p < p1; ++p) {
-                const int tl = (int)(p - c0);
-                const float *w = sw + tl * W3;
-                const float wgt = w[xk - (int)scx[tl]] * (w[yk] * w[zk]);
-                const float4 *qv = reinterpret_cast<const float4 *>(sq + tl * CP);
+      }
+      if (count > 0) {
+        // row (jj, kk) holds the region cells (lx..lx+N2-1, ly+jj, lz+kk); its bit in the
+        // mask is kk*8 + jj, so bits rise with region order.  Node (lx, ly+a, lz+b) takes a
+        // point of that row in region cell ex with stencil indices lx+N2-1-ex on x,
+        // N2-1-jj+a on y and N2-1-kk+b on z (a zero weight outside 0..N2-1).  The rows
+        // holding points of this chunk are marked, and the loop runs once per point: a
+        // lane's trip count is its quad's number of points, not a count per row.
+        const int ebase = (lz * E1 + ly) * E0 + lx;
+        unsigned long long rows = 0;
 #pragma unroll
-                for (int v = 0; v < CP / 4; ++v) {
-                  const float4 qq = qv[v];
-                  acc[4 * v] = fmaf(wgt, qq.x, acc[4 * v]);
-                  acc[4 * v + 1] = fmaf(wgt, qq.y, acc[4 * v + 1]);
-                  acc[4 * v + 2] = fmaf(wgt, qq.z, acc[4 * v + 2]);
-                  acc[4 * v + 3] = fmaf(wgt, qq.w, acc[4 * v + 3]);
+        for (int kk = 0; kk < RZ; ++kk)
+#pragma unroll
+          for (int jj = 0; jj < RY; ++jj)
+            if (ly + jj < E1 && lz + kk < E2) {
+              const int e0 = ebase + kk * slab + jj * E0;
+              if (max(off[e0], c0) < min(off[e0 + N2], c1)) rows |= 1ull << (kk * 8 + jj);
+            }
+        if (rows) {
+          const int xk = lx + N2 - 1;
+          const float *wp = nullptr, *wy = nullptr, *wz = nullptr;
+          const float4 *qp = nullptr;
+          const unsigned char *xp = nullptr;
+          uint32_t left = 0;
+          int jj = 0, kk = 0;
+          auto next_row = [&]() {
+            const int s = __ffsll((long long)rows) - 1;
+            rows &= rows - 1;
+            kk = s >> 3;
+            jj = s & 7;
+            const int e0 = ebase + kk * slab + jj * E0;
+            const uint32_t p0 = max(off[e0], c0);
+            left = min(off[e0 + N2], c1) - p0;
+            const int tl = (int)(p0 - c0);
+            wp = sw + tl * kScatterWStride<N2>;
+            wy = wp + (2 * N2 - jj);      // y weight of node ly (padded; +1 for node ly+1)
+            wz = wp + (3 * N2 + 2 - kk);  // z weight of node lz (padded; +1 for node lz+1)
+            qp = reinterpret_cast<const float4 *>(sq) + tl * (CP / 4);
+            xp = scx + tl;
+          };
+          next_row();
+          if (!exact) {
+            while (true) {
+              const float wx = wp[xk - (int)*xp];
+              float q[CP];
+#pragma unroll
+              for (int v = 0; v < CP / 4; ++v) {
+                const float4 t4 = qp[v];
+                q[4 * v] = t4.x;
+                q[4 * v + 1] = t4.y;
+                q[4 * v + 2] = t4.z;
+                q[4 * v + 3] = t4.w;
+              }
+#pragma unroll
+              for (int n = 0; n < BY * BZ; ++n) {
+                const float wgt = (wx * wy[n % BY]) * wz[n / BY];
+#pragma unroll
+                for (int c = 0; c < CP; ++c) acc[n][c] = fmaf(wgt, q[c], acc[n][c]);
+              }
+              wp += kScatterWStride<N2>;
+              wy += kScatterWStride<N2>;
+              wz += kScatterWStride<N2>;
+              qp += CP / 4;
+              ++xp;
+              if (--left == 0) {
+                if (!rows) break;
+                next_row();
+              }
+            }
+          } else {
+            while (true) {
+              const float wx = wp[xk - (int)*xp];
+              float q[CP];
+#pragma unroll
+              for (int v = 0; v < CP / 4; ++v) {
+                const float4 t4 = qp[v];
+                q[4 * v] = t4.x;
+                q[4 * v + 1] = t4.y;
+                q[4 * v + 2] = t4.z;
+                q[4 * v + 3] = t4.w;
+              }
+#pragma unroll
+              for (int n = 0; n < BY * BZ; ++n) {
+                const int a = n % BY, bb = n / BY;
+                const bool reach = jj - a >= 0 && jj - a <= N2 - 1 && kk - bb >= 0 && kk - bb <= N2 - 1;
+                if (reach) {
+                  const float wgt = (wx * wy[a]) * wz[bb];
+#pragma unroll
+                  for (int c = 0; c < CP; ++c) acc[n][c] = fmaf(wgt, q[c], acc[n][c]);
                 }
+              }
+              wp += kScatterWStride<N2>;
+              wy += kScatterWStride<N2>;
+              wz += kScatterWStride<N2>;
+              qp += CP / 4;
+              ++xp;
+              if (--left == 0) {
+                if (!rows) break;
+                next_row();
               }
             }
           }
         }
+      }
+#pragma unroll
+      for (int n = 0; n < BY * BZ; ++n) {
+        const int a = n % BY, bb = n / BY;
+        const int ny = ly + a, nz = lz + bb;
+        if (ny >= B1 || nz >= g.b[2]) continue;  // past the brick (odd edge)
         if (last) {
-          const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ly, z = (int64_t)bz * g.b[2] + lz;
+          if (lx >= vx || ny >= vy || nz >= vz) continue;  // past the grid (last brick)
+          const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ny, z = (int64_t)bz * g.b[2] + nz;
           float4 *d = reinterpret_cast<float4 *>(field + ((x + g.halo) + g.px * ((y + g.halo) + g.py * (z + g.halo))) * CP);
 #pragma unroll
           for (int v4 = 0; v4 < CP / 4; ++v4) {
             float v[4];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) v[u] = 4 * v4 + u < g.ncomp ? acc[4 * v4 + u] : 0.0f;
+            for (int u = 0; u < 4; ++u) v[u] = 4 * v4 + u < g.ncomp ? acc[n][4 * v4 + u] : 0.0f;
             if (beta_zero) {
               d[v4] = make_float4(v[0], v[1], v[2], v[3]);
             } else {
@@ -985,15 +1098,10 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
         } else {
 #pragma unroll
           for (int v = 0; v < CP / 4; ++v)
-            reinterpret_cast<float4 *>(sacc + nl * CP)[v] =
-                make_float4(acc[4 * v], acc[4 * v + 1], acc[4 * v + 2], acc[4 * v + 3]);
+            reinterpret_cast<float4 *>(sacc + ((nz * B1 + ny) * B0 + lx) * CP)[v] =
+                make_float4(acc[n][4 * v], acc[n][4 * v + 1], acc[n][4 * v + 2], acc[n][4 * v + 3]);
         }
       }
-      lx += sx;
-      ly += sy;
-      lz += sz;
-      if (lx >= B0) { lx -= B0; ++ly; }
-      if (ly >= B1) { ly -= B1; ++lz; }
     }
     if (last) break;
   }
@@ -1019,7 +1127,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
   for (int64_t ui = blockIdx.x; ui < nunits; ui += gridDim.x)
     scatter_brick_nodes<N2, FIXED, CP>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start, rec, qs,
-                                       field, beta, beta_zero, smem_scatter, warp_tot);
+                                       field, beta, beta_zero, list != nullptr, smem_scatter, warp_tot);
 }
 
 gbg_status check_field_bins(const gbg_field_s *f, const gbg_bins_s *b, const gbg_scheme *s) {
@@ -1146,7 +1254,7 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   auto go = [&](auto kernel) -> gbg_status {
     cudaFuncAttributes fa{};
     GBG_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
-    scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(fa.numRegs, threads));
+    scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(fa.numRegs, threads, g, f->cp, N2));
     const size_t smem = scatter_nodes_smem(g, f->cp, N2);
     if (smem > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared memory");
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1419,7 +1527,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     const int kind = d->n2 * 100 + d->cp;
 #define GBG_BATCH_SCATTER(N2, CP)                                                                          \
   scatter_brick_nodes<N2, true, CP>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, d->dest, d->beta, \
-                                    d->beta_zero, bsmem, warp_tot)
+                                    d->beta_zero, d->slist != nullptr, bsmem, warp_tot)
     switch (kind) {
       case 404: GBG_BATCH_SCATTER(4, 4); break;
       case 412: GBG_BATCH_SCATTER(4, 12); break;
@@ -2011,7 +2119,6 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   size_t scat_max = 0;
   cudaFuncAttributes scat_fa{};
   cudaFuncGetAttributes(&scat_fa, k_batch_scatter);
-  const size_t scat_budget = scatter_nodes_budget(scat_fa.numRegs, kThreads);
   for (int32_t i = 0; i < count; ++i) {
     const gbg_batch_item &it = items[i];
     gbg_field_s *f = it.field;
@@ -2063,7 +2170,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
       d.fg.halo = ds->halo;
       d.fg.cp = ds->cp;
       d.fg.ncomp = ds->ncomp;
-      scatter_nodes_chunk(d.fg, ds->cp, w, scat_budget);
+      scatter_nodes_chunk(d.fg, ds->cp, w, scatter_nodes_budget(scat_fa.numRegs, kThreads, d.fg, ds->cp, w));
       scat_max = std::max(scat_max, scatter_nodes_smem(d.fg, ds->cp, w));
       if (d.fg.e[0] > 255) return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");
       h.qptrs[i] = it.q;
