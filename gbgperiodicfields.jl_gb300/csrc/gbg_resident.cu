@@ -137,21 +137,48 @@ __global__ void k_export(const float *__restrict__ srcp, int cp, int ncomp, int6
 }
 
 // Copies interior nodes into the ghost layer (after a scatter wrote the interior).
+// Refreshes the periodic ghost layer from the interior.  Only the ghost nodes are
+// visited: the ghost z-planes (whole padded planes), then the ghost y-rows of the
+// interior planes, then the ghost x-runs of the interior rows -- about 3 * (2n+1) / N of
+// the storage instead of all of it.  Every ghost copies an interior node, so the order
+// of the copies does not matter.
 __global__ void k_fill_ghosts(float *__restrict__ d, int cp, int64_t px, int64_t py, int64_t pz,
                               int halo, int64_t nx, int64_t ny, int64_t nz) {
-  const int64_t total = px * py * pz;
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < total;
-       n += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = n % px, j = (n / px) % py, k = n / (px * py);
-    const bool interior = i >= halo && i < halo + nx && j >= halo && j < halo + ny && k >= halo &&
-                          k < halo + nz;
-    if (interior) continue;
+  const int64_t gz = pz - nz, gy = py - ny, gx = px - nx;
+  const int64_t zs = px * py * gz, ys = px * gy * nz, xs = gx * ny * nz;
+  const int64_t total = zs + ys + xs;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < total;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    int64_t i, j, k;
+    if (g < zs) {
+      i = g % px;
+      const int64_t r = g / px;
+      j = r % py;
+      const int64_t kk = r / py;
+      k = kk < halo ? kk : kk + nz;
+    } else if (g < zs + ys) {
+      const int64_t h = g - zs;
+      i = h % px;
+      const int64_t r = h / px, jj = r % gy;
+      j = jj < halo ? jj : jj + ny;
+      k = r / gy + halo;
+    } else {
+      const int64_t h = g - zs - ys, ii = h % gx, r = h / gx;
+      i = ii < halo ? ii : ii + nx;
+      j = r % ny + halo;
+      k = r / ny + halo;
+    }
     const int64_t x = imod(i - halo, nx) + halo, y = imod(j - halo, ny) + halo,
                   z = imod(k - halo, nz) + halo;
-    const float4 *s = reinterpret_cast<const float4 *>(d + (x + px * (y + py * z)) * cp);
-    float4 *t = reinterpret_cast<float4 *>(d + n * cp);
-    for (int c = 0; c < cp / 4; ++c) t[c] = s[c];
+    const float4 *src = reinterpret_cast<const float4 *>(d + (x + px * (y + py * z)) * cp);
+    float4 *dst = reinterpret_cast<float4 *>(d + (i + px * (j + py * k)) * cp);
+    for (int c = 0; c < cp / 4; ++c) dst[c] = src[c];
   }
+}
+
+// Threads for k_fill_ghosts: one per ghost node.
+inline int64_t ghost_count(int64_t px, int64_t py, int64_t pz, int64_t nx, int64_t ny, int64_t nz) {
+  return px * py * (pz - nz) + px * (py - ny) * nz + (px - nx) * ny * nz;
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -800,8 +827,10 @@ size_t scatter_nodes_budget(int regs, int threads, const FixGeo &g, int cp, int 
 // 2 x 2 quad of nodes in y and z (one node for width 8): it sums, in registers, the
 // contributions ((wx*wy)*wz)*alpha*q of every point whose stencil reaches each node, in a
 // fixed order per node -- the node's N2 x N2 rows of cells (z outer, y inner), within a
-// row the points in their binned order.  A point is loaded once for all the quad's nodes
-// it reaches, and a node that a point does not reach takes no operation from it.  The
+// row the points in their binned order.  A point is loaded once for all the quad's nodes;
+// a node that it does not reach adds w == 0 exactly (or, in a chunk holding a non-finite
+// value, takes no operation from it), which leaves the node's sum unchanged.  SU points
+// per thread are staged per round so that their load latencies overlap.  The
 // order depends on the points alone, not on the launch shape, the chunking or the other
 // instances of a batch, so the result is reproducible bitwise; no atomics are involved.
 //
@@ -811,7 +840,7 @@ size_t scatter_nodes_budget(int regs, int threads, const FixGeo &g, int cp, int 
 // pass continues each node's running sum exactly where the previous chunk left it.
 // All index arithmetic is 32-bit: the region's cell keys come from three per-axis tables
 // (key = kx[ex] + ky[ey] + kz[ez]).
-template <int N2, bool FIXED, int CP>
+template <int N2, bool FIXED, int CP, int SU>
 __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, int64_t b,
                                     const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                                     const float *__restrict__ qs, float *__restrict__ field, float beta,
@@ -862,13 +891,15 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     }
     __syncthreads();
     {
-      // four cells per thread in flight: their keys first, then all eight loads
+      // eight cells per thread in flight (one round for a 15x8x8 brick's 2178 cells at
+      // 256 threads): their keys first, then all sixteen loads
+      constexpr int U = 8;
       int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
       const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
-      for (int e = threadIdx.x; e < ecount; e += 4 * (int)blockDim.x) {
-        uint32_t key[4], a[4], z[4];
+      for (int e = threadIdx.x; e < ecount; e += U * (int)blockDim.x) {
+        uint32_t key[U], a[U], z[U];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
           key[u] = e + u * (int)blockDim.x < ecount ? kx[ex] + ky[ey] + kz[ez] : 0u;
           ex += sx;
           ey += sy;
@@ -877,12 +908,12 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
           if (ey >= E1) { ey -= E1; ++ez; }
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
           a[u] = __ldg(cell_start + key[u]);
           z[u] = __ldg(cell_start + key[u] + 1);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
+        for (int u = 0; u < U; ++u) {
           const int eu = e + u * (int)blockDim.x;
           if (eu < ecount) {
             r0s[eu] = a[u];
@@ -913,41 +944,64 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     // stage the chunk: each point's region cell by binary search of the offsets, its
     // weights (x, then y and z each with a zero either side) and its quantities
     int nonfinite = 0;
-    for (uint32_t t = c0 + threadIdx.x; t < c1; t += blockDim.x) {
-      int lo = 0, hi = ecount;  // the last cell e with off[e] <= t
-      while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (off[mid] <= t) lo = mid; else hi = mid;
+    // up to SU points per thread per round: every search first, then every global load,
+    // then the weights, so the latencies of the points overlap
+    for (uint32_t t0 = c0 + threadIdx.x; t0 < c1; t0 += SU * blockDim.x) {
+      uint32_t sl[SU];
+      int cell[SU];
+#pragma unroll
+      for (int u = 0; u < SU; ++u) {
+        const uint32_t t = t0 + u * blockDim.x;
+        int lo = 0, hi = ecount;  // the last cell e with off[e] <= t
+        if (t < c1) {
+          while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (off[mid] <= t) lo = mid; else hi = mid;
+          }
+        }
+        cell[u] = lo;
+        sl[u] = t < c1 ? r0s[lo] + (t - off[lo]) : 0u;
       }
-      const uint32_t sl = r0s[lo] + (t - off[lo]);
-      const int tl = (int)(t - c0);
-      scx[tl] = (unsigned char)(lo % E0);
-      const float4 r = __ldg(rec + sl);
-      float *wt = sw + tl * kScatterWStride<N2>;
-      float w[N2];
-      if constexpr (FIXED) weights_ptr<N2>(coef, r.x, w); else weights_rt<N2>(coef, m2, r.x, w);
+      float4 r[SU], qv[SU][CP / 4];
 #pragma unroll
-      for (int q = 0; q < N2; ++q) wt[q] = w[q];
-      if constexpr (FIXED) weights_ptr<N2>(coef, r.y, w); else weights_rt<N2>(coef, m2, r.y, w);
-      wt[N2] = 0.0f;
+      for (int u = 0; u < SU; ++u) {
+        if (t0 + u * blockDim.x < c1) {
+          r[u] = __ldg(rec + sl[u]);
+          const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl[u] * CP);
 #pragma unroll
-      for (int q = 0; q < N2; ++q) wt[N2 + 1 + q] = w[q];
-      wt[2 * N2 + 1] = 0.0f;
-      if constexpr (FIXED) weights_ptr<N2>(coef, r.z, w); else weights_rt<N2>(coef, m2, r.z, w);
-      wt[2 * N2 + 2] = 0.0f;
-#pragma unroll
-      for (int q = 0; q < N2; ++q) wt[2 * N2 + 3 + q] = w[q];
-      wt[3 * N2 + 3] = 0.0f;
-      const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
-      float qa = 0.0f;
-#pragma unroll
-      for (int v = 0; v < CP / 4; ++v) {
-        const float4 t4 = __ldg(q4 + v);
-        reinterpret_cast<float4 *>(sq + tl * CP)[v] = t4;
-        qa += fabsf(t4.x) + fabsf(t4.y) + fabsf(t4.z) + fabsf(t4.w);
+          for (int v = 0; v < CP / 4; ++v) qv[u][v] = __ldg(q4 + v);
+        }
       }
-      // NaN or infinity in the point's offsets or quantities (the sum is finite otherwise)
-      if (!isfinite(r.x + r.y + r.z + qa)) nonfinite = 1;
+#pragma unroll
+      for (int u = 0; u < SU; ++u) {
+        const uint32_t t = t0 + u * blockDim.x;
+        if (t >= c1) break;
+        const int tl = (int)(t - c0);
+        scx[tl] = (unsigned char)(cell[u] % E0);
+        float *wt = sw + tl * kScatterWStride<N2>;
+        float w[N2];
+        if constexpr (FIXED) weights_ptr<N2>(coef, r[u].x, w); else weights_rt<N2>(coef, m2, r[u].x, w);
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[q] = w[q];
+        if constexpr (FIXED) weights_ptr<N2>(coef, r[u].y, w); else weights_rt<N2>(coef, m2, r[u].y, w);
+        wt[N2] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[N2 + 1 + q] = w[q];
+        wt[2 * N2 + 1] = 0.0f;
+        if constexpr (FIXED) weights_ptr<N2>(coef, r[u].z, w); else weights_rt<N2>(coef, m2, r[u].z, w);
+        wt[2 * N2 + 2] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[2 * N2 + 3 + q] = w[q];
+        wt[3 * N2 + 3] = 0.0f;
+        float qa = 0.0f;
+#pragma unroll
+        for (int v = 0; v < CP / 4; ++v) {
+          reinterpret_cast<float4 *>(sq + tl * CP)[v] = qv[u][v];
+          qa += fabsf(qv[u][v].x) + fabsf(qv[u][v].y) + fabsf(qv[u][v].z) + fabsf(qv[u][v].w);
+        }
+        // NaN or infinity in the point's offsets or quantities (the sum is finite otherwise)
+        if (!isfinite(r[u].x + r[u].y + r[u].z + qa)) nonfinite = 1;
+      }
     }
     // a chunk with a non-finite value takes the exact path: each point only touches the
     // nodes it reaches; otherwise a point adds w*q to all of a quad's nodes, with w == 0
@@ -1126,7 +1180,7 @@ __global__ void __launch_bounds__(kThreads, 2)
   // the bricks to write: those a point reaches (beta == 1 leaves the others unchanged), or all
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
   for (int64_t ui = blockIdx.x; ui < nunits; ui += gridDim.x)
-    scatter_brick_nodes<N2, FIXED, CP>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start, rec, qs,
+    scatter_brick_nodes<N2, FIXED, CP, CP == 4 ? 3 : 1>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start, rec, qs,
                                        field, beta, beta_zero, list != nullptr, smem_scatter, warp_tot);
 }
 
@@ -1526,7 +1580,7 @@ __global__ void __launch_bounds__(kThreads, 2)
     if (threadIdx.x == 0 && status && !isfinite(__uint_as_float(*d->qmax_bits))) atomicOr(status, GBG_DEV_NONFINITE);
     const int kind = d->n2 * 100 + d->cp;
 #define GBG_BATCH_SCATTER(N2, CP)                                                                          \
-  scatter_brick_nodes<N2, true, CP>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, d->dest, d->beta, \
+  scatter_brick_nodes<N2, true, CP, 1>(d->fg, d->coef, N2, wu.y, d->cell_start, d->rec, d->qs, d->dest, d->beta, \
                                     d->beta_zero, d->slist != nullptr, bsmem, warp_tot)
     switch (kind) {
       case 404: GBG_BATCH_SCATTER(4, 4); break;
@@ -2024,7 +2078,7 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
     s = fixed ? launch_staged_scatter<8, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
               : launch_staged_scatter<8, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
   GBG_TRY(s);
-  const int64_t total = f->px * f->py * f->pz;
+  const int64_t total = ghost_count(f->px, f->py, f->pz, f->grid.n[0], f->grid.n[1], f->grid.n[2]);
   k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
                                                                      f->grid.n[0], f->grid.n[1], f->grid.n[2]);
   note_launch();
@@ -2364,7 +2418,7 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     for (gbg_field_s *f : bt->dests) {
-      const int64_t total = f->px * f->py * f->pz;
+      const int64_t total = ghost_count(f->px, f->py, f->pz, f->grid.n[0], f->grid.n[1], f->grid.n[2]);
       k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
                                                                          f->grid.n[0], f->grid.n[1], f->grid.n[2]);
       note_launch();
