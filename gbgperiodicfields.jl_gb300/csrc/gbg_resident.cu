@@ -312,6 +312,18 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// A point record's fourth word: the point's cell within its brick as packed coordinates
+// (brick edges are at most 64 cells), so readers take it apart with shifts.
+__device__ __forceinline__ uint32_t pack_local(uint32_t lx, uint32_t ly, uint32_t lz) {
+  return lx | (ly << 8) | (lz << 16);
+}
+__device__ __forceinline__ void unpack_local(float w, int &lx, int &ly, int &lz) {
+  const uint32_t loc = __float_as_uint(w);
+  lx = (int)(loc & 0xffu);
+  ly = (int)((loc >> 8) & 0xffu);
+  lz = (int)(loc >> 16);
+}
+
 // Keys, counts and per-point records of the bins; with DISP the positions are first
 // displaced (and wrapped) from `disp`, written to disp.dst, and binned in the same pass.
 template <typename T, bool DISP = false>
@@ -340,12 +352,13 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
     const int64_t bx = c[0] / g.b[0], by = c[1] / g.b[1], bz = c[2] / g.b[2];
-    const uint32_t local = (uint32_t)((c[2] - bz * g.b[2]) * g.b[1] * g.b[0] +
-                                      (c[1] - by * g.b[1]) * g.b[0] + (c[0] - bx * g.b[0]));
+    const uint32_t lx = (uint32_t)(c[0] - bx * g.b[0]), ly = (uint32_t)(c[1] - by * g.b[1]),
+                   lz = (uint32_t)(c[2] - bz * g.b[2]);
+    const uint32_t local = (lz * (uint32_t)g.b[1] + ly) * (uint32_t)g.b[0] + lx;
     const uint32_t key = (uint32_t)(((bz * g.nb[1] + by) * g.nb[0] + bx) * g.bvol + local);
     keys[p] = key;
     atomicAdd(counts + key, 1u);
-    rec_user[p] = make_float4(t[0], t[1], t[2], __uint_as_float(local));
+    rec_user[p] = make_float4(t[0], t[1], t[2], __uint_as_float(pack_local(lx, ly, lz)));
   }
 }
 
@@ -515,6 +528,16 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
   const int qi = sub & 3, jj = sub >> 2;
   const unsigned seg_mask = 0xFFu << (lane & ~7);
   const int qw = threadIdx.x >> 3;  // quarter-warp id within the CTA
+  // this lane's coefficient columns (x node qi, y nodes 2jj and 2jj+1), fixed for the launch
+  float cx[M2 > 0 ? M2 : 1], cya[M2 > 0 ? M2 : 1], cyb[M2 > 0 ? M2 : 1];
+  if constexpr (M2 > 0) {
+#pragma unroll
+    for (int p = 0; p < M2; ++p) {
+      cx[p] = s.c[qi + 4 * p];
+      cya[p] = s.c[2 * jj + 4 * p];
+      cyb[p] = s.c[2 * jj + 1 + 4 * p];
+    }
+  }
   const int nqw = (int)blockDim.x / 8;
   uint32_t phase[2] = {0, 0};
   bool failed = false;
@@ -557,14 +580,30 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
           r_next = __ldg(rec + sl + nqw);
           p_next = __ldg(perm + sl + nqw);
         }
-        const uint32_t loc = __float_as_uint(r.w);
-        const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
-        float wx[4], wy[4], w3[4];
-        weights_all<4, M2>(s, r.x, wx);
-        weights_all<4, M2>(s, r.y, wy);
-        weights_all<4, M2>(s, r.z, w3);
-        const float w1 = pick(wx, qi);
-        const float w2a = pick(wy, 2 * jj), w2b = pick(wy, 2 * jj + 1);
+        int lx, ly, lz;
+        unpack_local(r.w, lx, ly, lz);
+        float w1, w2a, w2b, w3[4];
+        if constexpr (M2 > 0) {
+          // only the weights this lane uses: its x node, its two y nodes, all four z nodes
+          w1 = cx[M2 - 1];
+          w2a = cya[M2 - 1];
+          w2b = cyb[M2 - 1];
+#pragma unroll
+          for (int p = M2 - 2; p >= 0; --p) {
+            w1 = fmaf(w1, r.x, cx[p]);
+            w2a = fmaf(w2a, r.y, cya[p]);
+            w2b = fmaf(w2b, r.y, cyb[p]);
+          }
+          weights_all<4, M2>(s, r.z, w3);
+        } else {
+          float wx[4], wy[4];
+          weights_all<4, M2>(s, r.x, wx);
+          weights_all<4, M2>(s, r.y, wy);
+          weights_all<4, M2>(s, r.z, w3);
+          w1 = pick(wx, qi);
+          w2a = pick(wy, 2 * jj);
+          w2b = pick(wy, 2 * jj + 1);
+        }
         float acc[CP];
 #pragma unroll
         for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
@@ -667,8 +706,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
       for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += blockDim.x) {
         const float4 r = __ldg(rec + sl);
-        const uint32_t loc = __float_as_uint(r.w);
-        const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
+        int lx, ly, lz;
+        unpack_local(r.w, lx, ly, lz);
         float w1[N2], w2[N2], w3[N2];
         weights_all<N2, M2>(s, r.x, w1);
         weights_all<N2, M2>(s, r.y, w2);
@@ -1385,8 +1424,8 @@ __device__ void batch_gather_points(const BatchDev *d, const float *tile, uint32
     for (uint32_t sl = s0 + (threadIdx.x >> 3); sl < s1; sl += kBatchGatherThreads / 8) {
       const float4 r = __ldg(d->rec + sl);
       const int64_t p = __ldg(d->perm + sl);
-      const uint32_t loc = __float_as_uint(r.w);
-      const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
+      int lx, ly, lz;
+      unpack_local(r.w, lx, ly, lz);
       float wx[4], wy[4], w3[4];
       weights_ptr<4>(d->coef, r.x, wx);
       weights_ptr<4>(d->coef, r.y, wy);
@@ -1437,8 +1476,8 @@ __device__ void batch_gather_points(const BatchDev *d, const float *tile, uint32
   } else {
     for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += kBatchGatherThreads) {
       const float4 r = __ldg(d->rec + sl);
-      const uint32_t loc = __float_as_uint(r.w);
-      const int lx = loc % g.b[0], ly = (loc / g.b[0]) % g.b[1], lz = loc / (g.b[0] * g.b[1]);
+      int lx, ly, lz;
+      unpack_local(r.w, lx, ly, lz);
       float w1[N2], w2[N2], w3[N2];
       weights_ptr<N2>(d->coef, r.x, w1);
       weights_ptr<N2>(d->coef, r.y, w2);
