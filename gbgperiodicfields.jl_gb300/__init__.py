@@ -1,12 +1,13 @@
 """GB300-native (sm_103a) particle gather/scatter for GBGPeriodicFields.jl's spline
 transfer path: interpolate!/anterpolate! of periodic scalar, vector and tensor fields at
-points, the traversal order, and the resident precision/batched/served forms.
+points, the traversal order, the resident precision/batched/served forms, and the NUFFT
+spectral transfer built on the same window gather/scatter.
 
 The compute runs in hand-written CUDA kernels in libgbg_gb300.so, reached through the C
 ABI in include/gbg_transfer.h.  This package is the host-side mirror of the reference's
 API over that ABI (the Julia facade binds the same ABI with ccall)."""
 from . import _lib
-from ._lib import ArgumentError, DimensionMismatch, GBGError, InexactError
+from ._lib import ArgumentError, DimensionMismatch, GBGError, InexactError, MethodError
 from .api import (AbstractFieldPhysical, AbstractPointValues, Grid3D, LagrangeSpline, LalescuSpline,
                   PointSet, PointTraversalOrder, PointTraversalOrderScratch, ScalarFieldPhysical,
                   ScalarPointValues, TensorFieldPhysical, TensorPointValues, VectorFieldPhysical,
@@ -14,6 +15,9 @@ from .api import (AbstractFieldPhysical, AbstractPointValues, Grid3D, LagrangeSp
                   field_data, field_grid, interpolate, interpolate_, npoints, point_positions,
                   point_traversal_order, point_traversal_order_, point_values, sample_field, wrap_,
                   zeros_colmajor)
+from .nufft import (NUFFT, AbstractFieldSpectral, FieldTransformPlans, RealFourierLayout, ScalarFieldSpectral,
+                    TensorFieldSpectral, VectorFieldSpectral, field_layout, field_spectral_shape, to_physical,
+                    to_spectral)
 
 
 def __getattr__(name):

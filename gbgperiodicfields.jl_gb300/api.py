@@ -506,7 +506,11 @@ def _raise_device_status(status: torch.Tensor):
 
 def interpolate_(out: AbstractPointValues, field: AbstractFieldPhysical, points: PointSet, scheme,
                  traversal: Optional[PointTraversalOrder] = None) -> AbstractPointValues:
-    """interpolate! (Interpolation.jl:1181-1198): out = field sampled at points."""
+    """interpolate! (Interpolation.jl:1181-1198): out = field sampled at points.  A
+    field in spectral representation with a NUFFT scheme goes to the NUFFT path."""
+    from . import nufft as _nufft
+    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+        return _nufft.dispatch_interpolate_(out, field, points, scheme, traversal)
     if out.tensor_order != field.tensor_order:
         raise ArgumentError(f"output tensor order {out.tensor_order} must equal field tensor order {field.tensor_order}")
     _check_npoints_match(out, points)
@@ -531,6 +535,9 @@ def interpolate_(out: AbstractPointValues, field: AbstractFieldPhysical, points:
 def interpolate(field: AbstractFieldPhysical, points: PointSet, scheme,
                 traversal: Optional[PointTraversalOrder] = None) -> AbstractPointValues:
     """Allocating form of interpolate! (Interpolation.jl:1212-1217)."""
+    from . import nufft as _nufft
+    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+        return _nufft.dispatch_interpolate(field, points, scheme, traversal)
     data = empty_colmajor((points.npoints,) + (3,) * field.tensor_order, field.data.dtype, points.device)
     return interpolate_(AbstractPointValues(data, field.tensor_order), field, points, scheme, traversal)
 
@@ -543,6 +550,9 @@ def anterpolate_(field: AbstractFieldPhysical, points: PointSet, quantities: Abs
         raise ArgumentError("alpha and beta come as a pair or not at all")
     if alpha is None:
         alpha, beta = 1.0, 0.0
+    from . import nufft as _nufft
+    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+        return _nufft.dispatch_anterpolate_(field, points, quantities, scheme, alpha, beta, traversal)
     if field.tensor_order != quantities.tensor_order:
         raise ArgumentError(f"field tensor order {field.tensor_order} must equal quantities tensor order {quantities.tensor_order}")
     _check_npoints_match(points, quantities)
@@ -572,9 +582,12 @@ def anterpolate_(field: AbstractFieldPhysical, points: PointSet, quantities: Abs
 
 
 def anterpolate(grid: Grid3D, points: PointSet, quantities: AbstractPointValues, scheme,
-                traversal: Optional[PointTraversalOrder] = None) -> AbstractFieldPhysical:
+                traversal: Optional[PointTraversalOrder] = None, layout=None) -> AbstractFieldPhysical:
     """Allocating form (Interpolation.jl:1344-1350): a fresh field in the quantities'
-    array family."""
+    array family (in spectral representation, in `layout` or the plan's, for a NUFFT)."""
+    from . import nufft as _nufft
+    if isinstance(scheme, _nufft.NUFFT):
+        return _nufft.anterpolate_nufft(grid, points, quantities, scheme, layout=layout, traversal=traversal)
     R = quantities.tensor_order
     data = empty_colmajor(tuple(grid.grid_size) + (3,) * R, grid.dtype, quantities.data.device)
     return anterpolate_(AbstractFieldPhysical(data, grid, R), points, quantities, scheme, traversal=traversal)

@@ -378,6 +378,46 @@ gbg_status gbg_server_destroy(gbg_server server);
 gbg_status gbg_server_plan(const int32_t *kinds, const uint64_t *fields, const size_t *bytes, int32_t n,
                            size_t free_bytes, int32_t max_batch, int32_t *run_length);
 
+/* ------------------------------------------------------------- NUFFT window transfers
+ *
+ * The per-point steps of the reference's fast spectral transfer (Interpolation.jl:1611-2070,
+ * NUFFT): a gather from, and a spread onto, the oversampled (sigma*N) physical grid with
+ * the exponential-of-semicircle window psi(s) = exp(beta*(sqrt(1 - (2s/W)^2) - 1)) over W
+ * nodes per axis (_es_weights, 1638-1645; odd widths follow the nearer node, 1634-1635).
+ * `fine` is the oversampled grid (its origin and spacing locate the points); fields on
+ * it are (n0, n1, n2, ncomp) column-major in dtype.  Widths 1..16 (the reference derives
+ * W = max(4, ceil(-log10(tolerance)) + 2), 16 at tolerance 1e-14); GBG_EUNSUPPORTED above.
+ * The FFT of the oversampled grid, the exchange of modes with the reference grid and the
+ * deconvolution are whole-array steps done by the caller (cuFFT). */
+
+/* Host helper: the per-axis deconvolution factors 1/psi_hat(omega) of one axis of the
+ * reference grid -- _nufft_deconvolution / _es_window_transform (Interpolation.jl:1652-1705):
+ * for stored index i (frequency i on the half axis, else i or i - n), omega =
+ * 2*pi*frequency/(oversampling*n), psi_hat by the 256-interval trapezoidal rule in theta
+ * (z = sin theta), computed in dtype; an even axis's Nyquist entry is 0.  host_out holds
+ * n/2+1 (is_half) or n values. */
+gbg_status gbg_nufft_deconvolution_axis(int64_t n, int32_t is_half, int32_t oversampling, int32_t width,
+                                        double beta, gbg_dtype dtype, double *host_out);
+/* Type 2 window gather -- _nufft_gather_kernel! (Interpolation.jl:1864-1914):
+ * out[p + M*c] = sum over the W^3 stencil of psi_x psi_y psi_z field[node, c].  A
+ * non-finite position sets GBG_DEV_NONFINITE and yields NaN. */
+gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, const void *field,
+                            const void *positions, int64_t npoints, const int32_t *traversal, int32_t width,
+                            double beta, void *out, int32_t *device_status, void *stream);
+/* Device bytes of the spread's workspace (int64 node sums and one word). */
+gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, int32_t ncomp, size_t *bytes);
+/* Type 1 window spread -- _nufft_spread_kernel! (Interpolation.jl:1919-1950): field (on
+ * the oversampled grid, overwritten) = sum over points of ((psi_y psi_z) psi_x) q.
+ * Deterministic where the reference adds floats atomically: each contribution is rounded
+ * to 64-bit fixed point at one scale per call (2^k, M*max|q| < 2^(61-k)) and added with an
+ * integer atomic, so the result is the same bits whatever the thread order or traversal;
+ * its absolute resolution is M*max|q|*2^-62 per contribution.  A non-finite quantity
+ * makes the whole field NaN (the FFT spreads it over every mode in the reference too). */
+gbg_status gbg_nufft_spread(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, void *field,
+                            const void *positions, int64_t npoints, const void *quantities,
+                            const int32_t *traversal, int32_t width, double beta, void *workspace,
+                            size_t workspace_bytes, int32_t *device_status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
