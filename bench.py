@@ -326,6 +326,7 @@ def run_gb300(args, rank, world):
         result["precision_form"] = precision_form(gbg, lib, dev, peak)
         result["batched_form"] = batched_form(gbg, dev)
         result["served_form"] = served_form(gbg, dev)
+        result["nufft_form"] = nufft_form(gbg, lib, dev)
         result["forms_gpu_launches"] = int(lib.gbg_kernel_launches() - launches1)
     return result
 
@@ -505,6 +506,62 @@ def precision_form(gbg, lib, dev, peak):
     }
     del f64, field, dest, out64, dep64, q64, q32, pos, bins, out
     torch.cuda.empty_cache()
+    return res
+
+
+def nufft_form(gbg, lib, dev, n=128, M=2_000_000, samples=32):
+    """The NUFFT spectral transfer: a band-limited 128^3 3-component field in spectral
+    representation (|k| <= 32), 2e6 uniform points, type 2 (interpolate) and type 1
+    (anterpolate) at FP64 tolerance 1e-6 (window width 8) and FP32 tolerance 1e-4 (width 6),
+    oversampling 2.  Error of the gather against the exact DirectDFT sum at a sample of
+    points (computed here with torch on the device), and the adjoint identity
+    M<Wf,q> = N<f,W^T q> for the whole deposit."""
+    import torch
+    from gbgperiodicfields_gb300.workloads import spectral_field, uniform_points
+    res = {"workload": f"{n}^3 x 3 spectral field (|k|<=32), {M:.0e} uniform points, oversampling 2, "
+                       "type 2 + type 1 per step", "unit": UNIT}
+    pos64 = torch.from_numpy(uniform_points(M, seed=12)).to(dev)
+    for dtype, tol in ((torch.float64, 1e-6), (torch.float32, 1e-4)):
+        grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3, dtype=dtype)
+        phys = spectral_field((n,) * 3, 3, kmax=32, seed=13, project=True, device=dev, dtype=dtype)
+        fh = gbg.to_spectral(gbg.VectorFieldPhysical(phys, grid))
+        plan = gbg.NUFFT(fh, tolerance=tol)
+        pts = gbg.PointSet(gbg.colmajor(pos64.to(dtype)))
+        q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=dtype, device=dev)))
+        out = gbg.VectorPointValues(gbg.empty_colmajor((M, 3), dtype, dev))
+        dep = gbg.VectorFieldSpectral(torch.zeros_like(fh.data), grid)
+        t2 = _time_ms(lambda: gbg.interpolate_(out, fh, pts, plan))
+        t1 = _time_ms(lambda: gbg.anterpolate_(dep, pts, q, plan))
+        k2 = _kernel_ms(lib, lambda: gbg.interpolate_(out, fh, pts, plan))
+        k1 = _kernel_ms(lib, lambda: gbg.anterpolate_(dep, pts, q, plan))
+        # the exact sum at a sample of points
+        F = fh.data.to(torch.complex128)
+        k = [torch.fft.rfftfreq(n, 1.0 / n, device=dev, dtype=torch.float64) if d == 0 else
+             torch.fft.fftfreq(n, 1.0 / n, device=dev, dtype=torch.float64) for d in range(3)]
+        alpha = torch.full((n // 2 + 1,), 2.0, dtype=torch.float64, device=dev)
+        alpha[0] = 1.0
+        alpha[-1] = 1.0
+        P = pos64[:samples]
+        exact = torch.empty((samples, 3), dtype=torch.float64, device=dev)
+        for i in range(samples):
+            ph = (torch.exp(1j * k[0] * P[i, 0])[:, None, None] * torch.exp(1j * k[1] * P[i, 1])[None, :, None]
+                  * torch.exp(1j * k[2] * P[i, 2])[None, None, :])
+            exact[i] = (alpha[:, None, None, None] * torch.real(F * ph[..., None])).sum(dim=(0, 1, 2)) / float(n ** 3)
+        got = out.data[:samples].to(torch.float64)
+        err = float((got - exact).abs().max() / exact.abs().max())
+        left = float((out.data.to(torch.float64) * q.data.to(torch.float64)).sum())
+        D = dep.data.to(torch.complex128)
+        right = float((alpha[:, None, None, None] * torch.real(F * torch.conj(D))).sum()) / float(n ** 3)
+        res["f64" if dtype == torch.float64 else "f32"] = {
+            "tolerance": tol, "window_width": plan.width, "window_shape": plan.beta,
+            "per_call_ms": {"interpolate": t2, "anterpolate": t1},
+            "kernel_ms": {"gather": k2, "spread": k1},
+            "value": 2 * M / ((t1 + t2) / 1e3),
+            "max_rel_error_vs_directdft": err,
+            "adjoint_rel_gap": abs(left - right) / max(abs(left), 1e-300),
+        }
+        del phys, fh, plan, pts, q, out, dep, F, D
+        torch.cuda.empty_cache()
     return res
 
 
