@@ -779,9 +779,10 @@ def run_reference(args, rank, world):
 
 # ------------------------------------------------------- profiling cases
 
-def case_resident(n=256, C=12, M=4_000_000):
+def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), threads=256):
     """256^3 x 12 FP32 resident field (0.85 GB), 4e6 uniform points in binned order,
-    cubic gather and scatter, twice."""
+    cubic gather and scatter, twice, at the precision form's tuned launch shape (15x8x8
+    bricks, 256 threads for both kernels)."""
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
@@ -792,14 +793,43 @@ def case_resident(n=256, C=12, M=4_000_000):
     field = resident.ResidentField(grid, C, max_stencil_width=4).load(
         torch.randn((C, n, n, n), device=dev).permute(3, 2, 1, 0))
     pos = torch.from_numpy(uniform_points(M, seed=2)).to(dev)
-    bins = resident.PointBins(grid, M).build(pos)
+    bins = resident.PointBins(grid, M, brick=brick).build(pos)
     pos = gbg.colmajor(pos[bins.order().long() - 1])
     bins.build(pos)
+    bins.set_launch(threads, threads)
     out = gbg.empty_colmajor((M, C), torch.float32, dev)
     q = gbg.colmajor(torch.randn((M, C), dtype=torch.float32, device=dev))
     for _ in range(2):
+        bins.build(pos)
         resident.interpolate_binned(field, bins, gbg.CatmullRom, out=out)
         resident.anterpolate_binned(field, bins, gbg.CatmullRom, q)
+    torch.cuda.synchronize()
+
+
+def case_resident_full():
+    """The precision form's step at full size: 512^3 x 12 FP32 resident field, 3.2e7
+    points in binned order, bins + cubic gather + scatter, twice (for a one-pass launch
+    list only)."""
+    case_resident(n=512, C=12, M=32_000_000)
+
+
+def case_nufft(n=64, M=500_000):
+    """NUFFT at FP64 tolerance 1e-6 (window width 8): a 64^3 x 3 spectral field, 5e5
+    uniform points, type 2 then type 1, twice."""
+    import torch
+    from __graft_entry__ import load_package
+    gbg = load_package()
+    from gbgperiodicfields_gb300.workloads import spectral_field, uniform_points
+    dev = torch.device("cuda:0")
+    grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3)
+    fh = gbg.to_spectral(gbg.VectorFieldPhysical(spectral_field((n,) * 3, 3, kmax=16, seed=1, project=True,
+                                                                device=dev), grid))
+    plan = gbg.NUFFT(fh, tolerance=1e-6)
+    pts = gbg.PointSet(torch.from_numpy(uniform_points(M, seed=2)).to(dev))
+    q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=torch.float64, device=dev)))
+    for _ in range(2):
+        gbg.interpolate(fh, pts, plan)
+        gbg.anterpolate(grid, pts, q, plan)
     torch.cuda.synchronize()
 
 
@@ -823,7 +853,8 @@ def case_plain(n=256, M=4_000_000):
     torch.cuda.synchronize()
 
 
-PROFILE_CASES = {"resident_256c12_4e6": case_resident, "plain_256c3_4e6_quintic": case_plain}
+PROFILE_CASES = {"resident_256c12_4e6": case_resident, "resident_512c12_3p2e7": case_resident_full,
+                 "plain_256c3_4e6_quintic": case_plain, "nufft_64c3_5e5": case_nufft}
 
 
 def main():
