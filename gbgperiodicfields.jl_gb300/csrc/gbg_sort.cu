@@ -120,17 +120,23 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t *keys, in
 }
 
 // Stable scatter of one digit pass.  Each warp owns a contiguous run of 512 items of the
-// tile and ranks them in index order, so equal digits keep their relative order.
+// tile and ranks them in index order, so equal digits keep their relative order.  The tile
+// is first put in digit order in shared memory, then every digit's run is written out
+// contiguously (coalesced) at its global offset.
 __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t *keys_in,
                                                            const uint32_t *vals_in, int64_t n,
                                                            int shift, const uint32_t *offsets,
                                                            int64_t nb, uint32_t *keys_out,
                                                            uint32_t *vals_out) {
+  static_assert(kRsThreads == kRsBins, "one thread per digit in the tile's digit scan");
   __shared__ uint32_t wh[kRsWarps][kRsBins];
+  __shared__ uint32_t sbase[kRsBins], goff[kRsBins], ws[32];
+  __shared__ uint32_t skey[kRsTile], sval[kRsTile];
   for (int i = threadIdx.x; i < kRsWarps * kRsBins; i += kRsThreads) (&wh[0][0])[i] = 0u;
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t seg = (int64_t)blockIdx.x * kRsTile + warp * (kRsItems * 32);
+  const int64_t tile0 = (int64_t)blockIdx.x * kRsTile;
+  const int64_t seg = tile0 + warp * (kRsItems * 32);
   uint32_t key[kRsItems];
 #pragma unroll
   for (int r = 0; r < kRsItems; ++r) {
@@ -139,8 +145,17 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t *keys_
     if (i < n) atomicAdd(&wh[warp][(key[r] >> shift) & 0xFFu], 1u);
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < kRsBins; d += kRsThreads) {
-    uint32_t run = offsets[(int64_t)d * nb + blockIdx.x];
+  {
+    // thread d: the tile's digit-d items start at sbase[d] (an exclusive scan over digits);
+    // warp w's start at sbase[d] plus the counts of the warps before it
+    const int d = threadIdx.x;
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int w = 0; w < kRsWarps; ++w) cnt += wh[w][d];
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(cnt, ws, &total);
+    sbase[d] = run;
+    goff[d] = offsets[(int64_t)d * nb + blockIdx.x];
 #pragma unroll
     for (int w = 0; w < kRsWarps; ++w) {
       const uint32_t c = wh[w][d];
@@ -162,9 +177,18 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t *keys_
     if (valid && lane == 31 - __clz(peers)) wh[warp][digit] += __popc(peers);
     __syncwarp();
     if (valid) {
-      keys_out[pos] = key[r];
-      vals_out[pos] = vals_in ? vals_in[i] : (uint32_t)i;
+      skey[pos] = key[r];
+      sval[pos] = vals_in ? vals_in[i] : (uint32_t)i;
     }
+  }
+  __syncthreads();
+  const int count = (int)min((int64_t)kRsTile, n - tile0);
+  for (int j = threadIdx.x; j < count; j += kRsThreads) {
+    const uint32_t k = skey[j];
+    const uint32_t d = (k >> shift) & 0xFFu;
+    const uint32_t gp = goff[d] + (uint32_t)j - sbase[d];
+    keys_out[gp] = k;
+    vals_out[gp] = sval[j];
   }
 }
 
