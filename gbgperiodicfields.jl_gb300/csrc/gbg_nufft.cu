@@ -13,13 +13,18 @@
 // The gather is a thread per point: the three axes' W window weights, then the W^3
 // stencil with the periodic wrap, the x direction contracted first with FMAs.
 //
-// The spread is deterministic, unlike the reference's atomic float adds: every
-// contribution ((wy*wz)*wx)*q is rounded to a 64-bit fixed-point integer at one scale for
-// the whole call, 2^k with k = 61 - e and M*max|q| < 2^e, and added with an integer
-// atomic.  Integer addition is associative, so the sums -- and the field -- do not depend
-// on the order in which threads add.  No node's sum can reach 2^61 (each window weight is
-// at most 1), and a contribution keeps M*max|q|*2^-62 of absolute resolution.
+// The spread is deterministic, unlike the reference's atomic float adds: the window
+// weights (evaluated in T as the reference does) and the quantities are converted once per
+// point to 64-bit fixed point, every contribution is formed from them with integer high
+// products and added as an integer.  Integer addition is associative, so the sums -- and
+// the field -- do not depend on the order in which threads add.  The scales leave no
+// node's sum able to overflow and keep about M*max|q|*2^-62 of absolute resolution per
+// contribution.  The points are binned by tile of the oversampled grid and each tile's sums
+// are formed in shared memory before one global add per node: no FP64 arithmetic and no
+// global atomic runs per node and point (GB300 runs FP64 at 1/58 of its FP32 rate, while
+// 64-bit integer products run on the integer pipes).
 
+#include <algorithm>
 #include <cmath>
 #include <type_traits>
 
@@ -169,52 +174,146 @@ __global__ void __launch_bounds__(kNThreads)
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
-// The fixed-point exponent k of a call: max|q| < 2^eq and M <= 2^em, so M*max|q| < 2^(61-k)
-// with k = 61 - eq - em (the exponents are taken apart, so no product can overflow).
-__device__ __forceinline__ int spread_exponent(unsigned long long qmax_bits, int64_t m) {
+// The fixed-point scales of a spread.  Weights are w * 2^62 (ES weights lie in [0, 1]);
+// quantities q * 2^(62 - eq) with max|q| < 2^eq; a contribution is
+// hi(hi(hi(Wy, Wz), Wx), |Q|) = w |q| 2^(56 - eq) < 2^56, shifted right (rounded) by
+// s = max(0, em - 6) with M <= 2^em, so that no node's sum of at most M contributions can
+// reach 2^62.  A node's value is its sum times 2^(eq + s - 56).
+struct SpreadScale {
+  int eq, s;
+};
+__device__ __forceinline__ SpreadScale spread_scale(unsigned long long qmax_bits, int64_t m) {
   int eq = 0, em = 0;
   frexp(__longlong_as_double((long long)qmax_bits), &eq);
   frexp((double)m, &em);
-  return 61 - eq - em;
+  return {eq, em > 6 ? em - 6 : 0};
 }
+
+// Spread, pass 1: each point's window weights (in T, as the reference evaluates them, then
+// as 64-bit fixed point) and first stencil node per axis, and its
+// tile (kTile^3 nodes holding the first node) with its rank there from an atomic count --
+// the order within a tile does not matter, the sums being integer.  A point with a
+// non-finite position goes to the extra bucket ntiles, which no tile visits.
+constexpr int kTile = 8;
 
 template <typename T, int W>
 __global__ void __launch_bounds__(kNThreads)
-    k_nufft_spread(NGrid<T> g, const T *__restrict__ pos, int64_t m, const T *__restrict__ q, int ncomp, T beta,
-                   const int32_t *__restrict__ trav, const unsigned long long *__restrict__ qmax_bits,
-                   unsigned long long *__restrict__ acc, int32_t *status) {
-  const double qmax = __longlong_as_double((long long)*qmax_bits);
-  if (!isfinite(qmax)) return;  // the field is set to NaN by k_nufft_finish
-  const int k = spread_exponent(*qmax_bits, m);
-  const bool plain = k > -1000 && k < 1000;  // 2^k is a finite double: scale by one product
-  const double scale = plain ? ldexp(1.0, k) : 0.0;
-  const int64_t nxy = g.n[0] * g.n[1], npf = nxy * g.n[2];
+    k_nufft_bin(NGrid<T> g, const T *__restrict__ pos, int64_t m, T beta, int64_t nt0, int64_t nt1,
+                int64_t ntiles, const int32_t *__restrict__ trav, uint32_t *__restrict__ tcount,
+                uint32_t *__restrict__ tkey, uint32_t *__restrict__ rank, int32_t *__restrict__ first,
+                unsigned long long *__restrict__ wbuf, int32_t *status) {
   for (int64_t wi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; wi < m; wi += (int64_t)gridDim.x * blockDim.x) {
     int64_t p;
-    if (!nvisit(trav, wi, m, p, status)) continue;
-    Stencil<T, W> s;
-    if (!point_stencil<T, W>(g, pos, p, m, beta, s)) {
-      if (status) atomicOr(status, GBG_DEV_NONFINITE);
+    if (!nvisit(trav, wi, m, p, status)) {
+      // a bad traversal entry: the visit slot wi carries no point
+      tkey[wi] = (uint32_t)ntiles;
+      rank[wi] = atomicAdd(tcount + ntiles, 1u);
       continue;
     }
-    for (int c = 0; c < ncomp; ++c) {
-      const T qv = q[p + m * c];
-      unsigned long long *ac = acc + npf * c;
-#pragma unroll 1
-      for (int k = 0; k < W; ++k) {
-        unsigned long long *plane = ac + nxy * s.iz[k];
-#pragma unroll 1
-        for (int j = 0; j < W; ++j) {
-          unsigned long long *row = plane + g.n[0] * s.iy[j];
-          const T wyz = mul_rn(s.w[1][j], s.w[2][k]);
+    bool ok = true;
+    int64_t s[3];
 #pragma unroll
-          for (int i = 0; i < W; ++i) {
-            const T v = mul_rn(mul_rn(wyz, s.w[0][i]), qv);
-            const double x = plain ? (double)v * scale : ldexp((double)v, k);
-            atomicAdd(row + s.ix[i], (unsigned long long)__double2ll_rn(x));
+    for (int a = 0; a < 3; ++a) {
+      int64_t base;
+      T t;
+      ok &= locate(__ldg(pos + p + m * a), g.o[a], g.d[a], base, t);
+      const int half = stencil_half<W>(t);
+      T w[W];
+      es_weights<W>(t, beta, half, w);
+#pragma unroll
+      for (int i = 0; i < W; ++i)  // w * 2^62, exact to the rounding of one conversion
+        wbuf[(3 * wi + a) * W + i] = ok ? (unsigned long long)__double2ll_rn(ldexp((double)w[i], 62)) : 0ull;
+      s[a] = imod(base + (1 - half), g.n[a]);
+      first[3 * wi + a] = (int32_t)s[a];
+    }
+    if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    const int64_t key = ok ? ((s[2] / kTile) * nt1 + s[1] / kTile) * nt0 + s[0] / kTile : ntiles;
+    tkey[wi] = (uint32_t)key;
+    rank[wi] = atomicAdd(tcount + key, 1u);
+  }
+}
+
+// Spread, pass 2: the visit slots in tile order.
+__global__ void __launch_bounds__(kNThreads)
+    k_nufft_place(int64_t m, const uint32_t *__restrict__ tkey, const uint32_t *__restrict__ rank,
+                  const uint32_t *__restrict__ tstart, uint32_t *__restrict__ order) {
+  for (int64_t wi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; wi < m; wi += (int64_t)gridDim.x * blockDim.x)
+    order[tstart[tkey[wi]] + rank[wi]] = (uint32_t)wi;
+}
+
+// Spread, pass 3: a CTA per tile.  For a group of CG components at a time the tile's
+// region ((kTile + W - 1)^3 nodes) is summed in shared memory -- a warp per point, its lanes
+// over the point's W^3 nodes, each contribution hi(hi(Wyz, Wx), |Q|) formed with integer
+// high products (no FP64 arithmetic per node) and added by a shared 64-bit integer atomic
+// -- then every nonzero node sum is added to the grid's by one global integer atomic.
+// Integer sums do not depend on the order of the adds.
+constexpr int kMaxGroup = 32;
+
+template <int W>
+__global__ void __launch_bounds__(kNThreads)
+    k_nufft_spread_tiles(NGrid<double> g, int64_t m, const void *__restrict__ qv_, int q_f64,
+                         const int32_t *__restrict__ trav, int ncomp, int group, int64_t nt0, int64_t nt1,
+                         int64_t ntiles, const uint32_t *__restrict__ tstart, const uint32_t *__restrict__ order,
+                         const int32_t *__restrict__ first, const unsigned long long *__restrict__ wbuf,
+                         const unsigned long long *__restrict__ qmax_bits, unsigned long long *__restrict__ acc) {
+  constexpr int R = kTile + W - 1;
+  constexpr int R3 = R * R * R;
+  extern __shared__ unsigned long long sacc[];  // group x R3 sums
+  __shared__ unsigned long long swyz[kNThreads / 32][W * W], swx[kNThreads / 32][W];
+  __shared__ long long sq[kNThreads / 32][kMaxGroup];
+  const double qmax = __longlong_as_double((long long)*qmax_bits);
+  if (!isfinite(qmax)) return;  // the field is set to NaN by k_nufft_finish
+  const SpreadScale sc = spread_scale(*qmax_bits, m);
+  const unsigned long long round = sc.s ? (1ull << (sc.s - 1)) : 0ull;
+  const int64_t nxy = g.n[0] * g.n[1], npf = nxy * g.n[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t t0 = tstart[tile], t1 = tstart[tile + 1];
+    if (t1 == t0) continue;  // uniform over the CTA
+    const int64_t tx = (tile % nt0) * kTile, ty = ((tile / nt0) % nt1) * kTile, tz = (tile / (nt0 * nt1)) * kTile;
+    for (int c0 = 0; c0 < ncomp; c0 += group) {
+      const int cg = min(group, ncomp - c0);
+      for (int r = threadIdx.x; r < cg * R3; r += blockDim.x) sacc[r] = 0ull;
+      __syncthreads();
+      for (uint32_t pt = t0 + warp; pt < t1; pt += nwarps) {
+        const uint32_t wi = order[pt];
+        int64_t p = wi;
+        if (trav) p = (int64_t)__ldg(trav + wi) - 1;
+        const unsigned long long *wp = wbuf + 3 * (int64_t)wi * W;
+        for (int i = lane; i < W; i += 32) swx[warp][i] = wp[i];
+        for (int e = lane; e < W * W; e += 32) swyz[warp][e] = __umul64hi(wp[W + e % W], wp[2 * W + e / W]);
+        if (lane < cg) {
+          const int64_t qi = p + m * (c0 + lane);
+          const double q = q_f64 ? static_cast<const double *>(qv_)[qi] : (double)static_cast<const float *>(qv_)[qi];
+          sq[warp][lane] = __double2ll_rn(ldexp(q, 62 - sc.eq));
+        }
+        const int ox = (int)(first[3 * (int64_t)wi] - tx), oy = (int)(first[3 * (int64_t)wi + 1] - ty),
+                  oz = (int)(first[3 * (int64_t)wi + 2] - tz);
+        __syncwarp();
+        for (int idx = lane; idx < W * W * W; idx += 32) {
+          const int i = idx % W, jk = idx / W, j = jk % W, kk = jk / W;
+          const unsigned long long wxyz = __umul64hi(swyz[warp][jk], swx[warp][i]);
+          const int r = ((oz + kk) * R + oy + j) * R + ox + i;
+          for (int cc = 0; cc < cg; ++cc) {
+            const long long qq = sq[warp][cc];
+            const unsigned long long mag = (__umul64hi(wxyz, (unsigned long long)(qq < 0 ? -qq : qq)) + round) >> sc.s;
+            atomicAdd(sacc + cc * R3 + r, qq < 0 ? (unsigned long long)(-(long long)mag) : mag);
           }
         }
+        __syncwarp();
       }
+      __syncthreads();
+      for (int e = threadIdx.x; e < cg * R3; e += blockDim.x) {
+        const unsigned long long v = sacc[e];
+        if (v == 0ull) continue;
+        const int cc = e / R3, r = e - cc * R3;
+        const int rx = r % R, ry = (r / R) % R, rz = r / (R * R);
+        // the region may pass the end of an axis (and, for a window wider than a small
+        // axis, wrap more than once): several region nodes can land on one grid node
+        const int64_t x = (tx + rx) % g.n[0], y = (ty + ry) % g.n[1], z = (tz + rz) % g.n[2];
+        atomicAdd(acc + npf * (c0 + cc) + z * nxy + y * g.n[0] + x, v);
+      }
+      __syncthreads();
     }
   }
 }
@@ -228,9 +327,10 @@ __global__ void __launch_bounds__(kNThreads)
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   const bool finite = isfinite(qmax);
   if (!finite && status && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, GBG_DEV_NONFINITE);
-  const int k = spread_exponent(*qmax_bits, m);
+  const SpreadScale sc = spread_scale(*qmax_bits, m);
+  const int e = sc.eq + sc.s - 56;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    field[i] = finite ? (T)ldexp((double)(long long)acc[i], -k) : nan_t<T>();
+    field[i] = finite ? (T)ldexp((double)(long long)acc[i], e) : nan_t<T>();
 }
 
 gbg_status check_ngrid(const gbg_grid *g) {
@@ -351,13 +451,98 @@ gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp
   }
 }
 
-gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, int32_t ncomp, size_t *bytes) {
+}  // extern "C"
+
+namespace gbg {
+namespace {
+
+struct SpreadLayout {
+  unsigned long long *acc = nullptr, *qmax = nullptr;
+  uint32_t *tcount = nullptr, *scan_tmp = nullptr, *tkey = nullptr, *rank = nullptr, *order = nullptr;
+  int32_t *first = nullptr;
+  unsigned long long *wbuf = nullptr;
+  int64_t nt0 = 0, nt1 = 0, nt2 = 0, ntiles = 0;
+};
+
+// The spread's workspace, in order: node sums (ncomp per node), max|q|, tile counts (+ the
+// extra bucket and the end), scan scratch, per visit slot its tile, rank and place, first
+// stencil nodes (3) and fixed-point window weights (3 W).  With base == nullptr it only sizes.
+size_t spread_layout(char *base, const gbg_grid &fine, gbg_dtype dtype, int32_t ncomp, int64_t m, int32_t width,
+                     SpreadLayout &L) {
+  Arena a;
+  a.base = base;
+  L.nt0 = (fine.n[0] + kTile - 1) / kTile;
+  L.nt1 = (fine.n[1] + kTile - 1) / kTile;
+  L.nt2 = (fine.n[2] + kTile - 1) / kTile;
+  L.ntiles = L.nt0 * L.nt1 * L.nt2;
+  const int64_t npf = fine.n[0] * fine.n[1] * fine.n[2];
+  L.acc = a.take<unsigned long long>((size_t)(npf * ncomp));
+  L.qmax = a.take<unsigned long long>(1);
+  L.tcount = a.take<uint32_t>((size_t)L.ntiles + 2);
+  L.scan_tmp = a.take<uint32_t>(scan_temp_elems(L.ntiles + 2));
+  const size_t mm = (size_t)(m > 0 ? m : 1);
+  L.tkey = a.take<uint32_t>(mm);
+  L.rank = a.take<uint32_t>(mm);
+  L.order = a.take<uint32_t>(mm);
+  L.first = a.take<int32_t>(3 * mm);
+  L.wbuf = a.take<unsigned long long>(3 * (size_t)width * mm);
+  return a.used + 256;
+}
+
+template <typename T, int W>
+gbg_status spread_run(const gbg_grid &fine, int32_t ncomp, T *field, const T *pos, int64_t m, const T *q,
+                      const int32_t *trav, double beta, const SpreadLayout &L, int32_t *status, cudaStream_t st) {
+  const NGrid<T> g = make_ngrid<T>(fine);
+  const int64_t n = fine.n[0] * fine.n[1] * fine.n[2] * (int64_t)ncomp;
+  if (m > 0) {
+    const int64_t nq = m * (int64_t)ncomp;
+    k_nufft_qmax<T><<<launch_blocks(nq, kNThreads), kNThreads, 0, st>>>(q, nq, L.qmax);
+    note_launch();
+    k_nufft_bin<T, W><<<launch_blocks(m, kNThreads), kNThreads, 0, st>>>(
+        g, pos, m, (T)beta, L.nt0, L.nt1, L.ntiles, trav, L.tcount, L.tkey, L.rank, L.first, L.wbuf, status);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    GBG_TRY(exclusive_scan_u32(L.tcount, L.tcount, L.ntiles + 2, L.scan_tmp, st));
+    k_nufft_place<<<launch_blocks(m, kNThreads), kNThreads, 0, st>>>(m, L.tkey, L.rank, L.tcount, L.order);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+    constexpr int R = kTile + W - 1;
+    const size_t slice = sizeof(unsigned long long) * (size_t)R * R * R;
+    // components per pass: as many region slices as fit in 96 KB (two CTAs per SM), at least one
+    const int group = (int)std::max<size_t>(1, std::min<size_t>({(size_t)ncomp, (size_t)kMaxGroup, 98304 / slice}));
+    const size_t smem = slice * group;
+    auto kernel = k_nufft_spread_tiles<W>;
+    GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 1, sms = 0, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kNThreads, smem);
+    const int blocks = (int)std::min<int64_t>(L.ntiles, (int64_t)sms * std::max(per_sm, 1));
+    mark_main_start(st);
+    kernel<<<blocks, kNThreads, smem, st>>>(make_ngrid<double>(fine), m, q, sizeof(T) == 8, trav, ncomp, group, L.nt0,
+                                           L.nt1, L.ntiles, L.tcount, L.order, L.first, L.wbuf, L.qmax, L.acc);
+    mark_main_stop(st);
+    note_launch();
+    GBG_CUDA_TRY(cudaGetLastError());
+  }
+  k_nufft_finish<T><<<launch_blocks(n, kNThreads), kNThreads, 0, st>>>(L.acc, n, m > 0 ? m : 1, L.qmax, field, status);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
+}  // namespace
+}  // namespace gbg
+
+extern "C" {
+
+gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,
+                                           int32_t width, size_t *bytes) {
   clear_error();
-  GBG_TRY(check_ngrid(fine));
-  if (ncomp < 1) return set_error(GBG_EARG, "ncomp must be at least 1");
+  GBG_TRY(check_nufft(fine, dtype, ncomp, npoints, width, 1.0));
   if (!bytes) return set_error(GBG_EARG, "null bytes");
-  const int64_t n = fine->n[0] * fine->n[1] * fine->n[2] * (int64_t)ncomp;
-  *bytes = (size_t)n * 8 + 256;
+  SpreadLayout L;
+  *bytes = spread_layout(nullptr, *fine, dtype, ncomp, npoints, width, L);
   return GBG_OK;
 }
 
@@ -369,51 +554,31 @@ gbg_status gbg_nufft_spread(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp
   try {
     GBG_TRY(check_nufft(fine, dtype, ncomp, npoints, width, beta));
     size_t need = 0;
-    GBG_TRY(gbg_nufft_spread_workspace_size(fine, ncomp, &need));
+    GBG_TRY(gbg_nufft_spread_workspace_size(fine, dtype, ncomp, npoints, width, &need));
     if (!field) return set_error(GBG_EARG, "nufft_spread: null field");
     if (npoints > 0 && (!positions || !quantities)) return set_error(GBG_EARG, "nufft_spread: null array");
+    if (npoints > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "nufft_spread: more than 2^31-1 points");
     if (!workspace || workspace_bytes < need) return set_error(GBG_ENOMEM, "nufft_spread: workspace too small");
-    if ((reinterpret_cast<uintptr_t>(workspace) & 7u) != 0) return set_error(GBG_EARG, "nufft_spread: workspace not 8-byte aligned");
+    // the layout aligns its pieces to 256 bytes from the workspace's start
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0)
+      return set_error(GBG_EARG, "nufft_spread: workspace not 256-byte aligned");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SpreadLayout L;
+    spread_layout(static_cast<char *>(workspace), *fine, dtype, ncomp, npoints, width, L);
     const int64_t n = fine->n[0] * fine->n[1] * fine->n[2] * (int64_t)ncomp;
-    unsigned long long *acc = static_cast<unsigned long long *>(workspace);
-    unsigned long long *qmax = acc + n;
-    GBG_CUDA_TRY(cudaMemsetAsync(workspace, 0, (size_t)n * 8 + 8, st));
-    if (npoints > 0) {
-      const int64_t nq = npoints * (int64_t)ncomp;
+    GBG_CUDA_TRY(cudaMemsetAsync(L.acc, 0, (size_t)n * 8, st));
+    GBG_CUDA_TRY(cudaMemsetAsync(L.qmax, 0, 8, st));
+    GBG_CUDA_TRY(cudaMemsetAsync(L.tcount, 0, sizeof(uint32_t) * ((size_t)L.ntiles + 2), st));
+    return with_width(width, [&](auto wc) -> gbg_status {
+      constexpr int W = decltype(wc)::value;
       if (dtype == GBG_F64)
-        k_nufft_qmax<double><<<launch_blocks(nq, kNThreads), kNThreads, 0, st>>>(static_cast<const double *>(quantities), nq, qmax);
-      else
-        k_nufft_qmax<float><<<launch_blocks(nq, kNThreads), kNThreads, 0, st>>>(static_cast<const float *>(quantities), nq, qmax);
-      note_launch();
-      GBG_CUDA_TRY(cudaGetLastError());
-      GBG_TRY(with_width(width, [&](auto wc) -> gbg_status {
-        constexpr int W = decltype(wc)::value;
-        const int blocks = launch_blocks(npoints, kNThreads);
-        mark_main_start(st);
-        if (dtype == GBG_F64)
-          k_nufft_spread<double, W><<<blocks, kNThreads, 0, st>>>(
-              make_ngrid<double>(*fine), static_cast<const double *>(positions), npoints,
-              static_cast<const double *>(quantities), ncomp, beta, traversal, qmax, acc, device_status);
-        else
-          k_nufft_spread<float, W><<<blocks, kNThreads, 0, st>>>(
-              make_ngrid<float>(*fine), static_cast<const float *>(positions), npoints,
-              static_cast<const float *>(quantities), ncomp, (float)beta, traversal, qmax, acc, device_status);
-        mark_main_stop(st);
-        note_launch();
-        GBG_CUDA_TRY(cudaGetLastError());
-        return GBG_OK;
-      }));
-    }
-    if (dtype == GBG_F64)
-      k_nufft_finish<double><<<launch_blocks(n, kNThreads), kNThreads, 0, st>>>(acc, n, npoints > 0 ? npoints : 1, qmax,
-                                                                               static_cast<double *>(field), device_status);
-    else
-      k_nufft_finish<float><<<launch_blocks(n, kNThreads), kNThreads, 0, st>>>(acc, n, npoints > 0 ? npoints : 1, qmax,
-                                                                              static_cast<float *>(field), device_status);
-    note_launch();
-    GBG_CUDA_TRY(cudaGetLastError());
-    return GBG_OK;
+        return spread_run<double, W>(*fine, ncomp, static_cast<double *>(field), static_cast<const double *>(positions),
+                                     npoints, static_cast<const double *>(quantities), traversal, beta, L,
+                                     device_status, st);
+      return spread_run<float, W>(*fine, ncomp, static_cast<float *>(field), static_cast<const float *>(positions),
+                                  npoints, static_cast<const float *>(quantities), traversal, beta, L, device_status,
+                                  st);
+    });
   } catch (...) {
     return set_error(GBG_ENOMEM, "nufft_spread: host exception");
   }

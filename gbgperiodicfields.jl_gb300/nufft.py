@@ -366,7 +366,8 @@ def anterpolate_nufft_(field: AbstractFieldSpectral, points: PointSet, quantitie
     phys = empty_colmajor(tuple(fine.grid_size) + (3,) * R, fine.dtype, dev)
     lib = _lib.load()
     nbytes = ctypes.c_size_t()
-    _lib.check(lib.gbg_nufft_spread_workspace_size(fine.c(), field.ncomp, ctypes.byref(nbytes)), "anterpolate!")
+    _lib.check(lib.gbg_nufft_spread_workspace_size(fine.c(), _DTYPE_CODE[fine.dtype], field.ncomp, m, scheme.width,
+                                                   ctypes.byref(nbytes)), "anterpolate!")
     ws = torch.empty(int(nbytes.value), dtype=torch.uint8, device=dev)
     status = _status_buffer(dev)
     with torch.cuda.device(dev):

@@ -404,15 +404,19 @@ gbg_status gbg_nufft_deconvolution_axis(int64_t n, int32_t is_half, int32_t over
 gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, const void *field,
                             const void *positions, int64_t npoints, const int32_t *traversal, int32_t width,
                             double beta, void *out, int32_t *device_status, void *stream);
-/* Device bytes of the spread's workspace (int64 node sums and one word). */
-gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, int32_t ncomp, size_t *bytes);
+/* Device bytes of the spread's workspace: int64 node sums, the points' tiles, ranks and
+ * window weights (about npf*ncomp*8 + npoints*(24 + 3*width*sizeof(dtype)) bytes). */
+gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,
+                                           int32_t width, size_t *bytes);
 /* Type 1 window spread -- _nufft_spread_kernel! (Interpolation.jl:1919-1950): field (on
  * the oversampled grid, overwritten) = sum over points of ((psi_y psi_z) psi_x) q.
  * Deterministic where the reference adds floats atomically: each contribution is rounded
- * to 64-bit fixed point at one scale per call (2^k, M*max|q| < 2^(61-k)) and added with an
- * integer atomic, so the result is the same bits whatever the thread order or traversal;
- * its absolute resolution is M*max|q|*2^-62 per contribution.  A non-finite quantity
- * makes the whole field NaN (the FFT spreads it over every mode in the reference too). */
+ * to 64-bit fixed point at one scale per call (2^k, M*max|q| < 2^(61-k)) and added as an
+ * integer, so the result is the same bits whatever the thread order or traversal; its
+ * absolute resolution is M*max|q|*2^-62 per contribution.  The points are binned by 8^3-
+ * node tiles of the oversampled grid and each tile's sums are formed in shared memory
+ * before one global add per node.  A non-finite quantity makes the whole field NaN (the
+ * FFT spreads it over every mode in the reference too).  workspace: 256-byte aligned. */
 gbg_status gbg_nufft_spread(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, void *field,
                             const void *positions, int64_t npoints, const void *quantities,
                             const int32_t *traversal, int32_t width, double beta, void *workspace,
