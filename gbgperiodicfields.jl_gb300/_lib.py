@@ -160,7 +160,8 @@ SIGNATURES = {
     "gbg_server_plan": (_I32, [ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(_SZ), _I32,
                                _SZ, _I32, ctypes.POINTER(_I32)]),
     "gbg_nufft_deconvolution_axis": (_I32, [_I64, _I32, _I32, _I32, _D, _I32, ctypes.POINTER(_D)]),
-    "gbg_nufft_interp": (_I32, [_GP, _I32, _I32, _P, _P, _I64, _P, _I32, _D, _P, _P, _P]),
+    "gbg_nufft_interp_workspace_size": (_I32, [_GP, _I32, _I32, _I64, _I32, ctypes.POINTER(_SZ)]),
+    "gbg_nufft_interp": (_I32, [_GP, _I32, _I32, _P, _P, _I64, _P, _I32, _D, _P, _P, _SZ, _P, _P]),
     "gbg_nufft_spread_workspace_size": (_I32, [_GP, _I32, _I32, _I64, _I32, ctypes.POINTER(_SZ)]),
     "gbg_nufft_spread": (_I32, [_GP, _I32, _I32, _P, _P, _I64, _P, _P, _I32, _D, _P, _SZ, _P, _P]),
 }

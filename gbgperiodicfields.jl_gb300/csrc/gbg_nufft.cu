@@ -10,8 +10,10 @@
 // transform (_es_window_transform, 1652-1662); the array steps use cuFFT through the host
 // facade.
 //
-// The gather is a thread per point: the three axes' W window weights, then the W^3
-// stencil with the periodic wrap, the x direction contracted first with FMAs.
+// The FP32 gather bins the points by tile of the oversampled grid; a CTA per tile stages the
+// tile's region in shared memory and a warp per point contracts its W^3 stencil there (the
+// lanes over the W^2 rows, the x direction first), reduced across the warp.  The FP64 gather
+// is a thread per point reading the oversampled field directly (FP64-pipe-bound either way).
 //
 // The spread is deterministic, unlike the reference's atomic float adds: the window
 // weights (evaluated in T as the reference does) and the quantities are converted once per
@@ -35,6 +37,7 @@ namespace {
 
 constexpr int kNThreads = 256;
 constexpr int kMaxWidth = 16;
+constexpr int kTile = 8;  // points are binned by tiles of kTile^3 oversampled-grid nodes
 
 template <typename T>
 struct NGrid {
@@ -123,6 +126,10 @@ __device__ __forceinline__ bool point_stencil(const NGrid<T> &g, const T *__rest
   return ok;
 }
 
+// The FP64 gather, a thread per point straight from the oversampled field: the three axes'
+// weights, the W^3 stencil with the periodic wrap, the x direction contracted first.  It
+// keeps the FP64 pipe busier than the tiled form, whose cross-lane FP64 reductions and
+// per-lane window evaluations cost more than the loads it saves.
 template <typename T, int W>
 __global__ void __launch_bounds__(kNThreads)
     k_nufft_gather(NGrid<T> g, const T *__restrict__ f, const T *__restrict__ pos, int64_t m, int ncomp, T beta,
@@ -153,6 +160,89 @@ __global__ void __launch_bounds__(kNThreads)
         }
       }
       out[p + m * c] = acc;
+    }
+  }
+}
+
+// Tiled window gather: a CTA per tile stages the tile's region ((kTile + W - 1)^3 nodes of
+// the oversampled field, for a group of components) in shared memory; a warp per point
+// evaluates the point's 3W window weights across its lanes, its lanes take the W^2 rows of the
+// stencil, contract x first, and the row sums are reduced across the warp.
+template <typename T, int W>
+__global__ void __launch_bounds__(kNThreads)
+    k_nufft_gather_tiles(NGrid<T> g, const T *__restrict__ f, const T *__restrict__ pos, int64_t m, int ncomp,
+                         int group, T beta, const int32_t *__restrict__ trav, int64_t nt0, int64_t nt1,
+                         int64_t ntiles, const uint32_t *__restrict__ tstart, const uint32_t *__restrict__ order,
+                         const int32_t *__restrict__ first, T *__restrict__ out) {
+  constexpr int R = kTile + W - 1;
+  constexpr int R3 = R * R * R;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  T *reg = reinterpret_cast<T *>(gsm);  // group x R3 values
+  __shared__ T swt[kNThreads / 32][3 * W];
+  const int64_t nxy = g.n[0] * g.n[1], npf = nxy * g.n[2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint32_t t0 = tstart[tile], t1 = tstart[tile + 1];
+    if (t1 == t0) continue;  // uniform over the CTA
+    const int64_t tx = (tile % nt0) * kTile, ty = ((tile / nt0) % nt1) * kTile, tz = (tile / (nt0 * nt1)) * kTile;
+    for (int c0 = 0; c0 < ncomp; c0 += group) {
+      const int cg = min(group, ncomp - c0);
+      __syncthreads();  // the previous group's region is no longer read
+      for (int e = threadIdx.x; e < cg * R3; e += blockDim.x) {
+        const int cc = e / R3, r = e - cc * R3;
+        const int rx = r % R, ry = (r / R) % R, rz = r / (R * R);
+        const int64_t x = (tx + rx) % g.n[0], y = (ty + ry) % g.n[1], z = (tz + rz) % g.n[2];
+        reg[e] = __ldg(f + npf * (c0 + cc) + z * nxy + y * g.n[0] + x);
+      }
+      __syncthreads();
+      for (uint32_t pt = t0 + warp; pt < t1; pt += nwarps) {
+        const uint32_t wi = order[pt];
+        int64_t p = wi;
+        if (trav) p = (int64_t)__ldg(trav + wi) - 1;
+        for (int e = lane; e < 3 * W; e += 32) {  // 3W can exceed the 32 lanes (W > 10)
+          const int a = e / W, i = e - a * W;
+          int64_t base;
+          T t;
+          locate(__ldg(pos + p + m * a), g.o[a], g.d[a], base, t);
+          const int half = stencil_half<W>(t);
+          const T off = T(i + 1 - half);
+          const T z = div_rn(mul_rn(T(2), add_rn(t, -off)), T(W));
+          const T r = add_rn(T(1), -mul_rn(z, z));
+          swt[warp][e] = exp(mul_rn(beta, add_rn(sqrt(r > T(0) ? r : T(0)), T(-1))));
+        }
+        const int ox = (int)(first[3 * (int64_t)wi] - tx), oy = (int)(first[3 * (int64_t)wi + 1] - ty),
+                  oz = (int)(first[3 * (int64_t)wi + 2] - tz);
+        __syncwarp();
+        T acc[4] = {T(0), T(0), T(0), T(0)};  // up to four components per pass of the rows
+        for (int cb = 0; cb < cg; cb += 4) {
+          const int nc = min(4, cg - cb);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[q] = T(0);
+          for (int rw = lane; rw < W * W; rw += 32) {
+            const int j = rw % W, k = rw / W;
+            const T wyz = mul_rn(swt[warp][W + j], swt[warp][2 * W + k]);
+            const T *row = reg + ((oz + k) * R + oy + j) * R + ox;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              if (q < nc) {
+                const T *rq = row + (cb + q) * R3;
+                T sx = T(0);
+#pragma unroll
+                for (int i = 0; i < W; ++i) sx = fma_rn(swt[warp][i], rq[i], sx);
+                acc[q] = fma_rn(wyz, sx, acc[q]);
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            T v = acc[q];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (lane == 0 && q < nc) out[p + m * (c0 + cb + q)] = v;
+          }
+        }
+        __syncwarp();
+      }
     }
   }
 }
@@ -194,14 +284,16 @@ __device__ __forceinline__ SpreadScale spread_scale(unsigned long long qmax_bits
 // tile (kTile^3 nodes holding the first node) with its rank there from an atomic count --
 // the order within a tile does not matter, the sums being integer.  A point with a
 // non-finite position goes to the extra bucket ntiles, which no tile visits.
-constexpr int kTile = 8;
 
+// With wbuf == nullptr (the gather) only the tiles and first nodes are kept, and a point
+// with a non-finite position gets NaN in out (ncomp components) here.
 template <typename T, int W>
 __global__ void __launch_bounds__(kNThreads)
     k_nufft_bin(NGrid<T> g, const T *__restrict__ pos, int64_t m, T beta, int64_t nt0, int64_t nt1,
                 int64_t ntiles, const int32_t *__restrict__ trav, uint32_t *__restrict__ tcount,
                 uint32_t *__restrict__ tkey, uint32_t *__restrict__ rank, int32_t *__restrict__ first,
-                unsigned long long *__restrict__ wbuf, int32_t *status) {
+                unsigned long long *__restrict__ wbuf, int32_t *status, T *__restrict__ out = nullptr,
+                int ncomp = 0) {
   for (int64_t wi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; wi < m; wi += (int64_t)gridDim.x * blockDim.x) {
     int64_t p;
     if (!nvisit(trav, wi, m, p, status)) {
@@ -218,15 +310,19 @@ __global__ void __launch_bounds__(kNThreads)
       T t;
       ok &= locate(__ldg(pos + p + m * a), g.o[a], g.d[a], base, t);
       const int half = stencil_half<W>(t);
-      T w[W];
-      es_weights<W>(t, beta, half, w);
+      if (wbuf) {
+        T w[W];
+        es_weights<W>(t, beta, half, w);
 #pragma unroll
-      for (int i = 0; i < W; ++i)  // w * 2^62, exact to the rounding of one conversion
-        wbuf[(3 * wi + a) * W + i] = ok ? (unsigned long long)__double2ll_rn(ldexp((double)w[i], 62)) : 0ull;
+        for (int i = 0; i < W; ++i)  // w * 2^62, exact to the rounding of one conversion
+          wbuf[(3 * wi + a) * W + i] = ok ? (unsigned long long)__double2ll_rn(ldexp((double)w[i], 62)) : 0ull;
+      }
       s[a] = imod(base + (1 - half), g.n[a]);
       first[3 * wi + a] = (int32_t)s[a];
     }
     if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
+    if (!ok && out)
+      for (int c = 0; c < ncomp; ++c) out[p + m * c] = nan_t<T>();
     const int64_t key = ok ? ((s[2] / kTile) * nt1 + s[1] / kTile) * nt0 + s[0] / kTile : ntiles;
     tkey[wi] = (uint32_t)key;
     rank[wi] = atomicAdd(tcount + key, 1u);
@@ -325,8 +421,7 @@ __global__ void __launch_bounds__(kNThreads)
     k_nufft_finish(const unsigned long long *__restrict__ acc, int64_t n, int64_t m,
                    const unsigned long long *__restrict__ qmax_bits, T *__restrict__ field, int32_t *status) {
   const double qmax = __longlong_as_double((long long)*qmax_bits);
-  const bool finite = isfinite(qmax);
-  if (!finite && status && blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, GBG_DEV_NONFINITE);
+  const bool finite = isfinite(qmax);  // a non-finite quantity is not an error: it yields NaN
   const SpreadScale sc = spread_scale(*qmax_bits, m);
   const int e = sc.eq + sc.s - 56;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -420,37 +515,6 @@ gbg_status gbg_nufft_deconvolution_axis(int64_t n, int32_t is_half, int32_t over
   return GBG_OK;
 }
 
-gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, const void *field,
-                            const void *positions, int64_t npoints, const int32_t *traversal, int32_t width,
-                            double beta, void *out, int32_t *device_status, void *stream) {
-  clear_error();
-  try {
-    GBG_TRY(check_nufft(fine, dtype, ncomp, npoints, width, beta));
-    if (npoints == 0) return GBG_OK;
-    if (!field || !positions || !out) return set_error(GBG_EARG, "nufft_interp: null array");
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
-    return with_width(width, [&](auto wc) -> gbg_status {
-      constexpr int W = decltype(wc)::value;
-      const int blocks = launch_blocks(npoints, kNThreads);
-      mark_main_start(st);
-      if (dtype == GBG_F64)
-        k_nufft_gather<double, W><<<blocks, kNThreads, 0, st>>>(
-            make_ngrid<double>(*fine), static_cast<const double *>(field), static_cast<const double *>(positions),
-            npoints, ncomp, beta, traversal, static_cast<double *>(out), device_status);
-      else
-        k_nufft_gather<float, W><<<blocks, kNThreads, 0, st>>>(
-            make_ngrid<float>(*fine), static_cast<const float *>(field), static_cast<const float *>(positions),
-            npoints, ncomp, (float)beta, traversal, static_cast<float *>(out), device_status);
-      mark_main_stop(st);
-      note_launch();
-      GBG_CUDA_TRY(cudaGetLastError());
-      return GBG_OK;
-    });
-  } catch (...) {
-    return set_error(GBG_ENOMEM, "nufft_interp: host exception");
-  }
-}
-
 }  // extern "C"
 
 namespace gbg {
@@ -468,7 +532,7 @@ struct SpreadLayout {
 // extra bucket and the end), scan scratch, per visit slot its tile, rank and place, first
 // stencil nodes (3) and fixed-point window weights (3 W).  With base == nullptr it only sizes.
 size_t spread_layout(char *base, const gbg_grid &fine, gbg_dtype dtype, int32_t ncomp, int64_t m, int32_t width,
-                     SpreadLayout &L) {
+                     SpreadLayout &L, bool spread = true) {
   Arena a;
   a.base = base;
   L.nt0 = (fine.n[0] + kTile - 1) / kTile;
@@ -476,8 +540,10 @@ size_t spread_layout(char *base, const gbg_grid &fine, gbg_dtype dtype, int32_t 
   L.nt2 = (fine.n[2] + kTile - 1) / kTile;
   L.ntiles = L.nt0 * L.nt1 * L.nt2;
   const int64_t npf = fine.n[0] * fine.n[1] * fine.n[2];
-  L.acc = a.take<unsigned long long>((size_t)(npf * ncomp));
-  L.qmax = a.take<unsigned long long>(1);
+  if (spread) {
+    L.acc = a.take<unsigned long long>((size_t)(npf * ncomp));
+    L.qmax = a.take<unsigned long long>(1);
+  }
   L.tcount = a.take<uint32_t>((size_t)L.ntiles + 2);
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(L.ntiles + 2));
   const size_t mm = (size_t)(m > 0 ? m : 1);
@@ -485,8 +551,44 @@ size_t spread_layout(char *base, const gbg_grid &fine, gbg_dtype dtype, int32_t 
   L.rank = a.take<uint32_t>(mm);
   L.order = a.take<uint32_t>(mm);
   L.first = a.take<int32_t>(3 * mm);
-  L.wbuf = a.take<unsigned long long>(3 * (size_t)width * mm);
+  if (spread) L.wbuf = a.take<unsigned long long>(3 * (size_t)width * mm);
   return a.used + 256;
+}
+
+// The tiled gather: bin, place, then a CTA per tile over the staged region.
+template <typename T, int W>
+gbg_status gather_run(const gbg_grid &fine, int32_t ncomp, const T *field, const T *pos, int64_t m,
+                      const int32_t *trav, double beta, T *out, const SpreadLayout &L, int32_t *status,
+                      cudaStream_t st) {
+  const NGrid<T> g = make_ngrid<T>(fine);
+  k_nufft_bin<T, W><<<launch_blocks(m, kNThreads), kNThreads, 0, st>>>(
+      g, pos, m, (T)beta, L.nt0, L.nt1, L.ntiles, trav, L.tcount, L.tkey, L.rank, L.first, nullptr, status, out,
+      ncomp);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  GBG_TRY(exclusive_scan_u32(L.tcount, L.tcount, L.ntiles + 2, L.scan_tmp, st));
+  k_nufft_place<<<launch_blocks(m, kNThreads), kNThreads, 0, st>>>(m, L.tkey, L.rank, L.tcount, L.order);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  constexpr int R = kTile + W - 1;
+  const size_t slice = sizeof(T) * (size_t)R * R * R;
+  // components per pass: as many region slices as fit in 96 KB (two CTAs per SM), at least one
+  const int group = (int)std::max<size_t>(1, std::min<size_t>((size_t)ncomp, 98304 / slice));
+  const size_t smem = slice * group;
+  auto kernel = k_nufft_gather_tiles<T, W>;
+  GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 1, sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kNThreads, smem);
+  const int blocks = (int)std::min<int64_t>(L.ntiles, (int64_t)sms * std::max(per_sm, 1));
+  mark_main_start(st);
+  kernel<<<blocks, kNThreads, smem, st>>>(g, field, pos, m, ncomp, group, (T)beta, trav, L.nt0, L.nt1, L.ntiles,
+                                         L.tcount, L.order, L.first, out);
+  mark_main_stop(st);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
 }
 
 template <typename T, int W>
@@ -535,6 +637,55 @@ gbg_status spread_run(const gbg_grid &fine, int32_t ncomp, T *field, const T *po
 }  // namespace gbg
 
 extern "C" {
+
+gbg_status gbg_nufft_interp_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,
+                                           int32_t width, size_t *bytes) {
+  clear_error();
+  GBG_TRY(check_nufft(fine, dtype, ncomp, npoints, width, 1.0));
+  if (!bytes) return set_error(GBG_EARG, "null bytes");
+  SpreadLayout L;
+  *bytes = spread_layout(nullptr, *fine, dtype, ncomp, npoints, width, L, false);
+  return GBG_OK;
+}
+
+gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, const void *field,
+                            const void *positions, int64_t npoints, const int32_t *traversal, int32_t width,
+                            double beta, void *out, void *workspace, size_t workspace_bytes, int32_t *device_status,
+                            void *stream) {
+  clear_error();
+  try {
+    GBG_TRY(check_nufft(fine, dtype, ncomp, npoints, width, beta));
+    if (npoints == 0) return GBG_OK;
+    if (!field || !positions || !out) return set_error(GBG_EARG, "nufft_interp: null array");
+    if (npoints > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "nufft_interp: more than 2^31-1 points");
+    size_t need = 0;
+    GBG_TRY(gbg_nufft_interp_workspace_size(fine, dtype, ncomp, npoints, width, &need));
+    if (!workspace || workspace_bytes < need) return set_error(GBG_ENOMEM, "nufft_interp: workspace too small");
+    if ((reinterpret_cast<uintptr_t>(workspace) & 255u) != 0)
+      return set_error(GBG_EARG, "nufft_interp: workspace not 256-byte aligned");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    SpreadLayout L;
+    spread_layout(static_cast<char *>(workspace), *fine, dtype, ncomp, npoints, width, L, false);
+    GBG_CUDA_TRY(cudaMemsetAsync(L.tcount, 0, sizeof(uint32_t) * ((size_t)L.ntiles + 2), st));
+    return with_width(width, [&](auto wc) -> gbg_status {
+      constexpr int W = decltype(wc)::value;
+      if (dtype == GBG_F64) {
+        mark_main_start(st);
+        k_nufft_gather<double, W><<<launch_blocks(npoints, kNThreads), kNThreads, 0, st>>>(
+            make_ngrid<double>(*fine), static_cast<const double *>(field), static_cast<const double *>(positions),
+            npoints, ncomp, beta, traversal, static_cast<double *>(out), device_status);
+        mark_main_stop(st);
+        note_launch();
+        GBG_CUDA_TRY(cudaGetLastError());
+        return GBG_OK;
+      }
+      return gather_run<float, W>(*fine, ncomp, static_cast<const float *>(field), static_cast<const float *>(positions),
+                                  npoints, traversal, beta, static_cast<float *>(out), L, device_status, st);
+    });
+  } catch (...) {
+    return set_error(GBG_ENOMEM, "nufft_interp: host exception");
+  }
+}
 
 gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,
                                            int32_t width, size_t *bytes) {

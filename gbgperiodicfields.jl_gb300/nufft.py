@@ -336,12 +336,18 @@ def interpolate_nufft_(out: AbstractPointValues, field: AbstractFieldSpectral, p
     if m == 0:
         return out
     status = _status_buffer(field.data.device)
+    lib = _lib.load()
+    nbytes = ctypes.c_size_t()
+    _lib.check(lib.gbg_nufft_interp_workspace_size(fine.c(), _DTYPE_CODE[fine.dtype], field.ncomp, m, scheme.width,
+                                                   ctypes.byref(nbytes)), "interpolate!")
+    ws = torch.empty(int(nbytes.value), dtype=torch.uint8, device=field.data.device)
     with torch.cuda.device(field.data.device):
         stream = torch.cuda.current_stream()
-        st = _lib.load().gbg_nufft_interp(fine.c(), _DTYPE_CODE[fine.dtype], field.ncomp, phys.data_ptr(),
-                                          points.positions.data_ptr(), m,
-                                          trav.data_ptr() if trav is not None else None, scheme.width, scheme.beta,
-                                          out.data.data_ptr(), status.data_ptr(), stream.cuda_stream)
+        st = lib.gbg_nufft_interp(fine.c(), _DTYPE_CODE[fine.dtype], field.ncomp, phys.data_ptr(),
+                                  points.positions.data_ptr(), m,
+                                  trav.data_ptr() if trav is not None else None, scheme.width, scheme.beta,
+                                  out.data.data_ptr(), ws.data_ptr(), ws.numel(), status.data_ptr(),
+                                  stream.cuda_stream)
         _lib.check(st, "interpolate!")
         stream.synchronize()
     _raise_device_status(status)

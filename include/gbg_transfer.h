@@ -398,12 +398,19 @@ gbg_status gbg_server_plan(const int32_t *kinds, const uint64_t *fields, const s
  * n/2+1 (is_half) or n values. */
 gbg_status gbg_nufft_deconvolution_axis(int64_t n, int32_t is_half, int32_t oversampling, int32_t width,
                                         double beta, gbg_dtype dtype, double *host_out);
+/* Device bytes of the gather's workspace: the points' tiles, ranks, places and first
+ * stencil nodes (about 24 bytes per point) and the tile counts. */
+gbg_status gbg_nufft_interp_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,
+                                           int32_t width, size_t *bytes);
 /* Type 2 window gather -- _nufft_gather_kernel! (Interpolation.jl:1864-1914):
- * out[p + M*c] = sum over the W^3 stencil of psi_x psi_y psi_z field[node, c].  A
- * non-finite position sets GBG_DEV_NONFINITE and yields NaN. */
+ * out[p + M*c] = sum over the W^3 stencil of psi_x psi_y psi_z field[node, c].  FP32:
+ * the points are binned by 8^3-node tiles of the oversampled grid and each tile's region is
+ * staged in shared memory; FP64: a thread per point (the workspace is then unused).  A
+ * non-finite position sets GBG_DEV_NONFINITE and yields NaN.  workspace: 256-byte aligned. */
 gbg_status gbg_nufft_interp(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, const void *field,
                             const void *positions, int64_t npoints, const int32_t *traversal, int32_t width,
-                            double beta, void *out, int32_t *device_status, void *stream);
+                            double beta, void *out, void *workspace, size_t workspace_bytes,
+                            int32_t *device_status, void *stream);
 /* Device bytes of the spread's workspace: int64 node sums, the points' tiles, ranks and
  * window weights (about npf*ncomp*8 + npoints*(24 + 3*width*sizeof(dtype)) bytes). */
 gbg_status gbg_nufft_spread_workspace_size(const gbg_grid *fine, gbg_dtype dtype, int32_t ncomp, int64_t npoints,

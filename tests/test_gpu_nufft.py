@@ -193,3 +193,37 @@ def test_refusals(pkg):
     bad = pkg.PointSet(pkg.colmajor(torch.tensor([[float("nan"), 0.0, 0.0]], dtype=torch.float64, device=DEV)))
     with pytest.raises(pkg.InexactError):
         pkg.interpolate(fhd, bad, plan)
+
+
+def test_spread_edge_cases(pkg):
+    """No points (a zero deposit, beta still applied); quantities of 1e-300 and 1e290 (the
+    fixed-point scale follows max|q| over the whole range); a NaN quantity (NaN on every
+    resolved mode, as the FFT of the reference's NaN-holding grid gives; the Nyquist shell,
+    which no oversampled mode maps to, stays 0)."""
+    n = (8, 8, 8)
+    grid = pkg.Grid3D(n, (2 * np.pi,) * 3)
+    g = no.grid(n)
+    plan = pkg.NUFFT.for_grid(grid, 0, device=DEV, tolerance=1e-8)
+    empty = pkg.PointSet(pkg.colmajor(torch.empty((0, 3), dtype=torch.float64, device=DEV)))
+    dep = pkg.anterpolate(grid, empty, values(pkg, np.empty(0), 0, torch.float64), plan)
+    assert torch.count_nonzero(dep.data) == 0
+    fh = pkg.ScalarFieldSpectral(torch.ones_like(dep.data), grid)
+    pkg.anterpolate_(fh, empty, values(pkg, np.empty(0), 0, torch.float64), plan, 1.0, 0.5)
+    assert torch.allclose(fh.data, torch.full_like(fh.data, 0.5))
+    rng = np.random.default_rng(4)
+    P = rng.random((20, 3)) * 2 * np.pi
+    q = rng.standard_normal(20)
+    pts = points(pkg, P, torch.float64)
+    want = no.nufft_anterpolate(g, 0, P, q, plan.width, plan.beta)[..., 0]
+    for scale in (1e-300, 1e290):
+        got = pkg.anterpolate(grid, pts, values(pkg, q * scale, 0, torch.float64), plan).data.cpu().numpy()
+        assert np.isfinite(got).all()
+        assert rel(got / scale, want) <= 1e-12
+    qn = q.copy()
+    qn[3] = np.nan
+    got = pkg.anterpolate(grid, pts, values(pkg, qn, 0, torch.float64), plan).data.cpu()
+    band = torch.ones(got.shape, dtype=torch.bool)
+    band[4, :, :] = False  # the even axes' Nyquist shell is not a shared mode: it stays 0
+    band[:, 4, :] = False
+    band[:, :, 4] = False
+    assert torch.isnan(got[band]).all() and torch.count_nonzero(got[~band]) == 0
