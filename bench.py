@@ -850,22 +850,26 @@ def case_resident_full():
 
 
 def case_nufft(n=64, M=500_000):
-    """NUFFT at FP64 tolerance 1e-6 (window width 8): a 64^3 x 3 spectral field, 5e5
-    uniform points, type 2 then type 1, twice."""
+    """NUFFT on a 64^3 x 3 spectral field with 5e5 uniform points, type 2 then type 1, at
+    FP64 tolerance 1e-6 (window width 8) and FP32 tolerance 1e-4 (width 6); twice."""
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
     from gbgperiodicfields_gb300.workloads import spectral_field, uniform_points
     dev = torch.device("cuda:0")
-    grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3)
-    fh = gbg.to_spectral(gbg.VectorFieldPhysical(spectral_field((n,) * 3, 3, kmax=16, seed=1, project=True,
-                                                                device=dev), grid))
-    plan = gbg.NUFFT(fh, tolerance=1e-6)
-    pts = gbg.PointSet(torch.from_numpy(uniform_points(M, seed=2)).to(dev))
-    q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=torch.float64, device=dev)))
+    pos = torch.from_numpy(uniform_points(M, seed=2)).to(dev)
+    runs = []
+    for dtype, tol in ((torch.float64, 1e-6), (torch.float32, 1e-4)):
+        grid = gbg.Grid3D((n,) * 3, (2 * np.pi,) * 3, dtype=dtype)
+        fh = gbg.to_spectral(gbg.VectorFieldPhysical(spectral_field((n,) * 3, 3, kmax=16, seed=1, project=True,
+                                                                    device=dev, dtype=dtype), grid))
+        pts = gbg.PointSet(gbg.colmajor(pos.to(dtype)))
+        q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=dtype, device=dev)))
+        runs.append((grid, fh, gbg.NUFFT(fh, tolerance=tol), pts, q))
     for _ in range(2):
-        gbg.interpolate(fh, pts, plan)
-        gbg.anterpolate(grid, pts, q, plan)
+        for grid, fh, plan, pts, q in runs:
+            gbg.interpolate(fh, pts, plan)
+            gbg.anterpolate(grid, pts, q, plan)
     torch.cuda.synchronize()
 
 

@@ -13,16 +13,16 @@
 // o*(N/L)*2^32 in one FMA, floor to int64, cell = (u >> 32) mod N, fraction = the low 32
 // bits.  Points are then stably radix-sorted by (brick, cell within brick).
 //
-// Gather: one CTA per brick (persistent, double-buffered TMA halo tiles), a point per
-// quarter-warp: lane (i, jj) owns the x-offset i and the y-offsets 2jj, 2jj+1 for all
-// four z-offsets, reads each node's components with 128-bit shared loads (the tile's row
-// pitch makes the 8 lanes of a quarter-warp hit 8 distinct 16-byte bank groups), and the
-// quarter-warp reduces its partial sums with shuffles.
+// Gather: one CTA per brick (persistent; the brick's TMA halo tile double-buffered when
+// that keeps as many CTAs per SM), a point per quarter-warp: lane (i, jj) owns the
+// x-offset i and the y-offsets 2jj, 2jj+1 for all four z-offsets, reads each node's
+// components with 128-bit shared loads (the tile's row pitch makes the 8 lanes of a
+// quarter-warp hit 8 distinct 16-byte bank groups), and the quarter-warp reduces its
+// partial sums with shuffles.
 //
-// Scatter: a CTA owns a brick's nodes and adds every contribution of the points whose
-// stencils reach the brick into two-level int32 fixed-point accumulators in shared memory
-// (exact, order-independent integer sums: no float atomics, bitwise reproducible), then
-// writes each node once.
+// Scatter: output-driven.  A CTA owns a brick's nodes and a thread a 2x2 quad of them; the
+// points of the brick's region are staged in shared memory, and each node sums its points
+// in a fixed order in registers (no atomics, bitwise reproducible), then is written once.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
