@@ -15,6 +15,10 @@
 #include <mutex>
 #include <string>
 
+#include <array>
+#include <map>
+#include <vector>
+
 #include "gbg_common.cuh"
 
 namespace gbg {
@@ -365,6 +369,11 @@ struct BrickGeo {
   int32_t b[3];
   int64_t nb[3];
   int64_t bvol;
+  // the scatter's shared accumulators: node (x, y, z) of component c at
+  // c*slice + z*pp + y*p0 + x, pitches chosen so that a warp's 64-bit atomics on one
+  // point's stencil spread over the banks (choose_acc_pitches)
+  int32_t p0 = 0, pp = 0;
+  int64_t slice = 0;
 };
 
 // One pass over the points in their own order: the locate, the brick-major key and the
@@ -466,6 +475,8 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // overflow (sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
 // does not depend on which thread adds first, and no float atomics are used.
 constexpr int kFlatChunk = 2048;
+// the scatter's static shared memory: one count per warp for the block scan
+constexpr int kScanSlots = 32;
 
 template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
@@ -478,14 +489,14 @@ __global__ void __launch_bounds__(kThreads)
   const int E0 = bg.b[0] + N2 - 1, E1 = bg.b[1] + N2 - 1, E2 = bg.b[2] + N2 - 1;
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)bg.bvol;
-  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw);  // ncomp * bvol, comp-major
-  uint32_t *off = reinterpret_cast<uint32_t *>(acc + (size_t)bvol * ncomp);  // ecount: exclusive prefix
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw);  // ncomp * slice, comp-major, pitched
+  uint32_t *off = reinterpret_cast<uint32_t *>(acc + (size_t)bg.slice * ncomp);  // ecount: exclusive prefix
   uint32_t *r0s = off + ecount;                                              // ecount: first slot
   uint32_t *pslot = r0s + ecount;                                            // kFlatChunk: point slot
   uint32_t *pxyz = pslot + kFlatChunk;                                       // kFlatChunk: packed cell
   uint32_t *kx = pxyz + kFlatChunk, *ky = kx + E0, *kz = ky + E1;             // per-axis key tables
   uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
-  __shared__ uint32_t warp_tot[32];
+  __shared__ uint32_t warp_tot[kScanSlots];
   const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5, nwarps = (int)blockDim.x >> 5;
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
@@ -567,7 +578,7 @@ __global__ void __launch_bounds__(kThreads)
       mx = __reduce_max_sync(0xffffffffu, mx);
       if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
     }
-    for (int i = threadIdx.x; i < bvol * ncomp; i += blockDim.x) acc[i] = 0ull;
+    for (int i = threadIdx.x; i < (int)bg.slice * ncomp; i += blockDim.x) acc[i] = 0ull;
     __syncthreads();
     const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
@@ -626,14 +637,14 @@ __global__ void __launch_bounds__(kThreads)
               for (int j = ky0; j < ky1; ++j) {
                 const int ly = ey + j - (N2 - 1);
                 const long long wyz = __mul64hi(pick_t(w2, j), wz);
-                const int row = (lz * B1 + ly) * B0;
+                const int row = lz * bg.pp + ly * bg.p0;
   #pragma unroll
                 for (int i = 0; i < N2; ++i) {
                   const int lx = lxb + i;
                   if (lx < 0 || lx >= vx) continue;
                   const long long w = __mul64hi(w1[i], wyz);
                   for (int c = 0; c < ncomp; ++c)
-                    atomicAdd(acc + c * bvol + row + lx, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                    atomicAdd(acc + c * bg.slice + row + lx, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
                 }
               }
             }
@@ -657,7 +668,7 @@ __global__ void __launch_bounds__(kThreads)
             const int count = nx * ny * nz;
             // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
             const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
-            const int node0 = ((ez - (N2 - 1)) * B1 + ey - (N2 - 1)) * B0 + ex - (N2 - 1);
+            const int node0 = (ez - (N2 - 1)) * bg.pp + (ey - (N2 - 1)) * bg.p0 + ex - (N2 - 1);
             for (int base = 0; base < count; base += 32) {
               const int idx = base + lane;
               const int r1 = (int)(((uint32_t)idx * rnx) >> 16), ii = idx - r1 * nx;
@@ -668,9 +679,9 @@ __global__ void __launch_bounds__(kThreads)
               const long long wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
               if (idx < count) {
                 const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
-                const int node = node0 + (k * B1 + j) * B0 + i;
+                const int node = node0 + k * bg.pp + j * bg.p0 + i;
                 for (int c = 0; c < ncomp; ++c)
-                  atomicAdd(acc + c * bvol + node, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                  atomicAdd(acc + c * bg.slice + node, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
               }
             }
           }
@@ -686,7 +697,7 @@ __global__ void __launch_bounds__(kThreads)
         if (lx < vx && ly < vy && lz < vz) {
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-          const T v = accumulated ? (T)ldexp((double)(long long)acc[c * bvol + nl], -vexp)
+          const T v = accumulated ? (T)ldexp((double)(long long)acc[c * bg.slice + lz * bg.pp + ly * bg.p0 + lx], -vexp)
                                   : (finite ? T(0) : quiet_nan<T>());
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
         }
@@ -825,6 +836,52 @@ struct ScatterPlan {
   size_t smem = 0;
 };
 
+// Pitches of the scatter's shared accumulators.  A warp adds one point's contributions to
+// the nodes of its stencil inside the brick, x fastest, 32 nodes at a time, as 64-bit
+// atomics (two of the 32 four-byte banks each); with the brick's own row and plane pitches
+// the stencil's rows fall on the same banks (a 16-node row is 128 bytes).  Over row pitches
+// b0..b0+15 and plane pitches b1*p0..b1*p0+15 whose slice stays within max_slice words
+// (so that the padding costs no CTA per SM), this takes the pair with the fewest
+// shared-memory wavefronts summed over every position of a full n^3 stencil in the brick.
+void choose_acc_pitches(BrickGeo &bg, int n2, int64_t max_slice) {
+  const int b0 = bg.b[0], b1 = bg.b[1], b2 = bg.b[2];
+  const int nx = std::min(n2, b0), ny = std::min(n2, b1), nz = std::min(n2, b2);
+  int64_t best = -1;
+  int best_p0 = b0, best_pp = b0 * b1;
+  std::vector<int> words;
+  for (int p0 = b0; p0 < b0 + 16; ++p0) {
+    for (int pp = b1 * p0; pp < b1 * p0 + 16; ++pp) {
+      if ((int64_t)b2 * pp > max_slice && !(p0 == b0 && pp == b0 * b1)) continue;
+      int64_t total = 0;
+      for (int z0 = 0; z0 + nz <= b2; ++z0)
+        for (int y0 = 0; y0 + ny <= b1; ++y0)
+          for (int x0 = 0; x0 + nx <= b0; ++x0) {
+            words.clear();
+            for (int k = 0; k < nz; ++k)
+              for (int j = 0; j < ny; ++j)
+                for (int i = 0; i < nx; ++i) words.push_back((z0 + k) * pp + (y0 + j) * p0 + x0 + i);
+            for (size_t c = 0; c < words.size(); c += 32) {
+              // wavefronts of one warp instruction: the words are distinct and a 64-bit word
+              // w sits on the bank pair w mod 16, so the most words sharing a pair
+              int per_pair[16] = {0};
+              for (size_t l = c; l < std::min(words.size(), c + 32); ++l) ++per_pair[words[l] & 15];
+              int mx = 0;
+              for (int q = 0; q < 16; ++q) mx = std::max(mx, per_pair[q]);
+              total += mx;
+            }
+          }
+      if (best < 0 || total < best) {
+        best = total;
+        best_p0 = p0;
+        best_pp = pp;
+      }
+    }
+  }
+  bg.p0 = best_p0;
+  bg.pp = best_pp;
+  bg.slice = (int64_t)b2 * best_pp;
+}
+
 ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   ScatterPlan p;
   const int base[3] = {(size_t)ncomp * esize > 24 ? 8 : 16, 8, 8};
@@ -838,10 +895,36 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   }
   p.bg.bvol = (int64_t)p.bg.b[0] * p.bg.b[1] * p.bg.b[2];
   const size_t ecount = (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
-  p.smem = (size_t)p.bg.bvol * ncomp * sizeof(unsigned long long) + 2 * sizeof(uint32_t) * ecount +
-           2 * sizeof(uint32_t) * kFlatChunk +
-           sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1)) +
-           sizeof(uint32_t) * (size_t)(p.bg.bvol + 1);
+  // shared memory besides the accumulators: region offsets and first slots, the point
+  // chunk, the key tables, the coverage counts
+  const size_t rest = 2 * sizeof(uint32_t) * ecount + 2 * sizeof(uint32_t) * kFlatChunk +
+                      sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1)) +
+                      sizeof(uint32_t) * (size_t)(p.bg.bvol + 1);
+  {
+    // accumulator pitches that keep the unpadded layout's CTAs per SM (228 KB per SM, 1 KB
+    // reserved per CTA by the runtime, the kernel's static scan slots) and its 200 KB cap;
+    // they depend on the brick, the width and the components alone, so each is searched once
+    const size_t per_node = (size_t)ncomp * sizeof(unsigned long long), sm = 228 * 1024,
+                 reserve = 1024 + kScanSlots * sizeof(uint32_t);
+    const size_t unpadded = (size_t)p.bg.bvol * per_node + rest;
+    const size_t ctas = std::max<size_t>(1, sm / (unpadded + reserve));
+    const size_t room = std::min<size_t>(sm / ctas - reserve, 200 * 1024);
+    const int64_t max_slice = room > rest ? (int64_t)((room - rest) / per_node) : p.bg.bvol;
+    static std::mutex mu;
+    static std::map<std::array<int, 5>, std::pair<int, int>> cache;
+    const std::array<int, 5> key = {p.bg.b[0], p.bg.b[1], p.bg.b[2], n2, ncomp};
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+      choose_acc_pitches(p.bg, n2, std::max<int64_t>(max_slice, p.bg.bvol));
+      cache[key] = {p.bg.p0, p.bg.pp};
+    } else {
+      p.bg.p0 = it->second.first;
+      p.bg.pp = it->second.second;
+      p.bg.slice = (int64_t)p.bg.b[2] * p.bg.pp;
+    }
+  }
+  p.smem = (size_t)p.bg.slice * ncomp * sizeof(unsigned long long) + rest;
   (void)esize;
   if (ecount > 65535) wide_enough = false;
   p.bricked = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;
@@ -909,10 +992,25 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, P.smem);
+  // the padded pitches only where the occupancy query agrees that they cost no CTA per SM
+  BrickGeo bg = P.bg;
+  size_t smem = P.smem;
+  if (bg.slice != bg.bvol) {
+    const size_t flat = smem - (size_t)(bg.slice - bg.bvol) * ncomp * sizeof(unsigned long long);
+    int flat_per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&flat_per_sm, kernel, kThreads, flat);
+    if (flat_per_sm > per_sm) {
+      bg.p0 = bg.b[0];
+      bg.pp = bg.b[0] * bg.b[1];
+      bg.slice = bg.bvol;
+      smem = flat;
+      per_sm = flat_per_sm;
+    }
+  }
   const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
   mark_main_start(st);
-  kernel<<<blocks, kThreads, P.smem, st>>>(g, P.bg, ncomp, L.counts, static_cast<const long long *>(L.rec), L.qi,
-                                           L.qmax_bits, wexp, field, T(beta), beta == 0.0, status);
+  kernel<<<blocks, kThreads, smem, st>>>(g, bg, ncomp, L.counts, static_cast<const long long *>(L.rec), L.qi,
+                                         L.qmax_bits, wexp, field, T(beta), beta == 0.0, status);
   mark_main_stop(st);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
