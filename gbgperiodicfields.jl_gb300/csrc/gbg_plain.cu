@@ -386,6 +386,8 @@ __global__ void __launch_bounds__(kThreads)
                  const T *__restrict__ q, int ncomp, T alpha, unsigned long long *__restrict__ qmax_bits,
                  int32_t *status) {
   const int64_t n[3] = {g.nx, g.ny, g.nz};
+  // 2^wexp: a product with a normal power of two rounds once, as ldexp does
+  const double wscale = ldexp(1.0, wexp);
   unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(kThreads)
       axis_weights_fma<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
       // exact: a double times a power of two, then a 53-bit integer
 #pragma unroll
-      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = ok ? __double2ll_rn(ldexp((double)w[k], wexp)) : 0ll;
+      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = ok ? __double2ll_rn((double)w[k] * wscale) : 0ll;
     }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
@@ -437,6 +439,8 @@ __global__ void __launch_bounds__(kThreads)
   int e = 0;
   frexp(qmax, &e);
   const bool finite = isfinite(qmax);
+  // 2^(62-e) is a normal double (e <= 1024), so the product rounds once, as ldexp does
+  const double qscale = ldexp(1.0, 62 - e);
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[sl];
@@ -446,7 +450,7 @@ __global__ void __launch_bounds__(kThreads)
     for (int k = 0; k < 3 * N2; ++k) dst[k] = __ldg(src + k);
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);
-      qi[sl * ncomp + c] = finite ? __double2ll_rn(ldexp((double)v, 62 - e)) : 0ll;
+      qi[sl * ncomp + c] = finite ? __double2ll_rn((double)v * qscale) : 0ll;
     }
   }
 }
@@ -477,6 +481,8 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 constexpr int kFlatChunk = 2048;
 // the scatter's static shared memory: one count per warp for the block scan
 constexpr int kScanSlots = 32;
+// quantities of a point the warp-per-point scatter holds in registers (the rest are read per use)
+constexpr int kQReg = 4;
 
 template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
@@ -654,16 +660,32 @@ __global__ void __launch_bounds__(kThreads)
           // the brick (the sub-box i0..i1 x j0..j1 x k0..k1), so every lane of every atomic
           // does work; lanes 0..3*N2-1 load one axis weight each, and each node's three
           // weights arrive by shuffle.  The weight products are formed in the same order as
-          // in the gather (wz * S first, then wy, then wx).
-          for (uint32_t t = c0 + warp; t < c1; t += nwarps) {
-            const uint32_t sl = pslot[t - c0], packed = pxyz[t - c0];
+          // in the gather (wz * S first, then wy, then wx).  The next point's weights and
+          // first kQReg quantities are loaded while this one is added.
+          uint32_t t = c0 + warp;
+          uint32_t sl_n = 0, packed_n = 0;
+          long long wl_n = 0ll, q_n[kQReg];
+          auto fetch = [&](uint32_t tt) {
+            sl_n = pslot[tt - c0];
+            packed_n = pxyz[tt - c0];
+            wl_n = lane < 3 * N2 ? __ldg(wts + (int64_t)sl_n * (3 * N2) + lane) : 0ll;
+#pragma unroll
+            for (int r = 0; r < kQReg; ++r) q_n[r] = r < ncomp ? __ldg(qi + (int64_t)sl_n * ncomp + r) : 0ll;
+          };
+          if (t < c1) fetch(t);
+          for (; t < c1; t += nwarps) {
+            const uint32_t sl = sl_n, packed = packed_n;
+            const long long wl = wl_n;
+            long long qr[kQReg];
+#pragma unroll
+            for (int r = 0; r < kQReg; ++r) qr[r] = q_n[r];
+            if (t + nwarps < c1) fetch(t + nwarps);
             const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
             const int i0 = max(0, N2 - 1 - ex), i1 = min(N2, vx + N2 - 1 - ex);
             const int j0 = max(0, N2 - 1 - ey), j1 = min(N2, vy + N2 - 1 - ey);
             const int k0 = max(0, N2 - 1 - ez), k1 = min(N2, vz + N2 - 1 - ez);
             const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
             if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
-            const long long wl = lane < 3 * N2 ? __ldg(wts + (int64_t)sl * (3 * N2) + lane) : 0ll;
             const long long *qv = qi + (int64_t)sl * ncomp;
             const int count = nx * ny * nz;
             // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
@@ -680,7 +702,11 @@ __global__ void __launch_bounds__(kThreads)
               if (idx < count) {
                 const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
                 const int node = node0 + k * bg.pp + j * bg.p0 + i;
-                for (int c = 0; c < ncomp; ++c)
+#pragma unroll
+                for (int r = 0; r < kQReg; ++r)
+                  if (r < ncomp)
+                    atomicAdd(acc + r * bg.slice + node, (unsigned long long)((__mul64hi(w, qr[r]) + half) >> sh));
+                for (int c = kQReg; c < ncomp; ++c)
                   atomicAdd(acc + c * bg.slice + node, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
               }
             }
