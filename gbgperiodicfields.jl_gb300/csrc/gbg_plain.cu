@@ -377,17 +377,13 @@ struct BrickGeo {
 };
 
 // One pass over the points in their own order: the locate, the brick-major key and the
-// cell count, the three axes' stencil weights (the reference's Horner with fused
-// multiply-adds, once per point) as 64-bit fixed point w * 2^wexp, and max|alpha q|.
-template <typename T, int N2, int M2>
+// cell count, and max|alpha q|.
+template <typename T>
 __global__ void __launch_bounds__(kThreads)
-    k_brick_keys(GridT<T> g, BrickGeo bg, SchemeT<T, N2> sch, const T *__restrict__ pos, int64_t m,
-                 uint32_t *__restrict__ keys, uint32_t *__restrict__ counts, int wexp, long long *__restrict__ worig,
-                 const T *__restrict__ q, int ncomp, T alpha, unsigned long long *__restrict__ qmax_bits,
-                 int32_t *status) {
+    k_brick_keys(GridT<T> g, BrickGeo bg, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
+                 uint32_t *__restrict__ counts, const T *__restrict__ q, int ncomp, T alpha,
+                 unsigned long long *__restrict__ qmax_bits, int32_t *status) {
   const int64_t n[3] = {g.nx, g.ny, g.nz};
-  // 2^wexp: a product with a normal power of two rounds once, as ldexp does
-  const double wscale = ldexp(1.0, wexp);
   unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
@@ -405,15 +401,6 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t key = (uint32_t)(brick * bg.bvol + local);
     keys[p] = key;
     atomicAdd(counts + key, 1u);
-    long long *wp = worig + p * (3 * N2);
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      T w[N2];
-      axis_weights_fma<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
-      // exact: a double times a power of two, then a 53-bit integer
-#pragma unroll
-      for (int k = 0; k < N2; ++k) wp[d * N2 + k] = ok ? __double2ll_rn((double)w[k] * wscale) : 0ll;
-    }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
       const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs((double)v));
@@ -428,26 +415,37 @@ __global__ void __launch_bounds__(kThreads)
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
-// Into sorted order: each slot's weights, and alpha*q as 64-bit fixed point
-// q * 2^(62 - e) with max|alpha q| < 2^e (one scale for all points).
-template <typename T, int N2>
+// In sorted order, slot by slot: the point's three axes' stencil weights (the reference's
+// Horner with fused multiply-adds, once per point) as 64-bit fixed point w * 2^wexp, and
+// alpha*q as 64-bit fixed point q * 2^(62 - e) with max|alpha q| < 2^e (one scale for all
+// points).  The weights are evaluated here, from the position read through the
+// permutation, rather than in the key pass, so they are written once, already sorted.
+template <typename T, int N2, int M2>
 __global__ void __launch_bounds__(kThreads)
-    k_brick_order(const uint32_t *__restrict__ perm, int64_t m, const long long *__restrict__ worig,
-                  long long *__restrict__ wts, const T *__restrict__ q, int ncomp, T alpha,
+    k_brick_order(GridT<T> g, SchemeT<T, N2> sch, const T *__restrict__ pos, const uint32_t *__restrict__ perm,
+                  int64_t m, int wexp, long long *__restrict__ wts, const T *__restrict__ q, int ncomp, T alpha,
                   const unsigned long long *__restrict__ qmax_bits, long long *__restrict__ qi) {
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   int e = 0;
   frexp(qmax, &e);
   const bool finite = isfinite(qmax);
-  // 2^(62-e) is a normal double (e <= 1024), so the product rounds once, as ldexp does
-  const double qscale = ldexp(1.0, 62 - e);
+  // 2^wexp and 2^(62-e) are normal doubles (e <= 1024), so each product rounds once, as
+  // ldexp does; the weight products are exact, then 53-bit integers
+  const double wscale = ldexp(1.0, wexp), qscale = ldexp(1.0, 62 - e);
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[sl];
-    const long long *src = worig + p * (3 * N2);
+    int64_t b[3];
+    T t[3];
+    const bool ok = locate3(g, pos, p, m, b, t);
     long long *dst = wts + sl * (3 * N2);
 #pragma unroll
-    for (int k = 0; k < 3 * N2; ++k) dst[k] = __ldg(src + k);
+    for (int d = 0; d < 3; ++d) {
+      T w[N2];
+      axis_weights_fma<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
+#pragma unroll
+      for (int k = 0; k < N2; ++k) dst[d * N2 + k] = ok ? __double2ll_rn((double)w[k] * wscale) : 0ll;
+    }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);
       qi[sl * ncomp + c] = finite ? __double2ll_rn((double)v * qscale) : 0ll;
@@ -975,11 +973,11 @@ ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncom
   L.perm = a.take<uint32_t>((size_t)m);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  // the three axes' weights per point (64-bit fixed point for the brick scatter, whose
-  // qs region holds them in the points' own order before they are sorted)
+  // the three axes' weights per point, in sorted order (64-bit fixed point for the brick
+  // scatter, which keeps its quantities in qi and needs no qs)
   const size_t rec_bytes = 3 * (size_t)n2 * (P.bricked ? sizeof(long long) : esize);
   L.rec = a.take<char>((size_t)m * rec_bytes);
-  L.qs = a.take<char>((size_t)m * (P.bricked ? rec_bytes : ncomp * esize));
+  L.qs = P.bricked ? nullptr : a.take<char>((size_t)m * ncomp * esize);
   L.qi = P.bricked ? a.take<long long>((size_t)m * ncomp) : nullptr;
   L.qmax_bits = a.take<unsigned long long>(4);
   return L;
@@ -999,16 +997,14 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   const int wexp = fixed_weight_exp(sch);
   const int blocks_m = launch_blocks(m, kThreads);
   GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
-  k_brick_keys<T, N2, FIXED ? N2 : 0><<<blocks_m, kThreads, 0, st>>>(
-      g, P.bg, s, x, m, L.keys, L.counts, wexp, static_cast<long long *>(L.qs), q, ncomp, T(alpha), L.qmax_bits,
-      status);
+  k_brick_keys<T><<<blocks_m, kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, q, ncomp, T(alpha),
+                                                 L.qmax_bits, status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
   GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
-  k_brick_order<T, N2><<<blocks_m, kThreads, 0, st>>>(L.perm, m, static_cast<const long long *>(L.qs),
-                                                     static_cast<long long *>(L.rec), q, ncomp, T(alpha),
-                                                     L.qmax_bits, L.qi);
+  k_brick_order<T, N2, FIXED ? N2 : 0><<<blocks_m, kThreads, 0, st>>>(
+      g, s, x, L.perm, m, wexp, static_cast<long long *>(L.rec), q, ncomp, T(alpha), L.qmax_bits, L.qi);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   auto kernel = k_scatter_fixed64<T, N2>;
