@@ -51,6 +51,17 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
 
 // Julia's integer mod for a positive divisor: the result lies in [0, n).
+// Adds v to a 64-bit integer kept in shared memory as two 32-bit words, lo[i] and hi[i],
+// with native 32-bit atomics: the low word's add returns the old value, whose wrap is the
+// carry into the high word.  Each add wraps the low word at most once, so after all adds
+// the high word holds the sum of the high parts plus floor(sum of low parts / 2^32) in any
+// order: the pair is the exact 64-bit sum, as a 64-bit atomic would leave it.
+__device__ __forceinline__ void atomic_add_split64(uint32_t *lo, uint32_t *hi, int i, unsigned long long v) {
+  const uint32_t vl = (uint32_t)v, vh = (uint32_t)(v >> 32);
+  const uint32_t old = atomicAdd(lo + i, vl);
+  atomicAdd(hi + i, vh + (uint32_t)(old + vl < vl));
+}
+
 __host__ __device__ __forceinline__ int64_t imod(int64_t a, int64_t n) {
   int64_t r = a % n;
   return r < 0 ? r + n : r;

@@ -370,8 +370,8 @@ struct BrickGeo {
   int64_t nb[3];
   int64_t bvol;
   // the scatter's shared accumulators: node (x, y, z) of component c at
-  // c*slice + z*pp + y*p0 + x, pitches chosen so that a warp's 64-bit atomics on one
-  // point's stencil spread over the banks (choose_acc_pitches)
+  // c*slice + z*pp + y*p0 + x, pitches chosen so that a warp's atomics on one point's
+  // stencil spread over the banks (choose_acc_pitches)
   int32_t p0 = 0, pp = 0;
   int64_t slice = 0;
 };
@@ -475,7 +475,9 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // hi(hi(hi(wy, wz), wx), q) = w1 w2 w3 q * 2^(3P + Q - 192) (truncated, relative error
 // ~2^-56), shifted right by sh bits so that the brick's largest node coverage K_max cannot
 // overflow (sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
-// does not depend on which thread adds first, and no float atomics are used.
+// does not depend on which thread adds first, and no float atomics are used.  The 64-bit
+// sums are added as two 32-bit words with a carry (atomic_add_split64): native 32-bit
+// shared atomics (with 64-bit shared atomics ncu counted a shared load beside each one).
 constexpr int kFlatChunk = 2048;
 // the scatter's static shared memory: one count per warp for the block scan
 constexpr int kScanSlots = 32;
@@ -493,8 +495,11 @@ __global__ void __launch_bounds__(kThreads)
   const int E0 = bg.b[0] + N2 - 1, E1 = bg.b[1] + N2 - 1, E2 = bg.b[2] + N2 - 1;
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)bg.bvol;
-  unsigned long long *acc = reinterpret_cast<unsigned long long *>(smem_raw);  // ncomp * slice, comp-major, pitched
-  uint32_t *off = reinterpret_cast<uint32_t *>(acc + (size_t)bg.slice * ncomp);  // ecount: exclusive prefix
+  // ncomp * slice 64-bit accumulators, comp-major and pitched, as a plane of low words and
+  // a plane of high words (atomic_add_split64)
+  uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *acc_hi = acc_lo + (size_t)bg.slice * ncomp;
+  uint32_t *off = acc_hi + (size_t)bg.slice * ncomp;                         // ecount: exclusive prefix
   uint32_t *r0s = off + ecount;                                              // ecount: first slot
   uint32_t *pslot = r0s + ecount;                                            // kFlatChunk: point slot
   uint32_t *pxyz = pslot + kFlatChunk;                                       // kFlatChunk: packed cell
@@ -545,7 +550,7 @@ __global__ void __launch_bounds__(kThreads)
     // coverage of every node (points whose stencil reaches it): window sums of the cell
     // counts, over x and y into the accumulators as scratch, then over z
     if (threadIdx.x == 0) kcnt[bvol] = 0u;
-    uint32_t *scratch = reinterpret_cast<uint32_t *>(acc);
+    uint32_t *scratch = acc_lo;
     if (E2 <= 2 * bg.b[2] * ncomp) {
       for (int o = threadIdx.x; o < B0 * B1 * E2; o += blockDim.x) {
         const int lx = o % B0, r = o / B0, ly = r % B1, ez = r / B1;
@@ -582,7 +587,7 @@ __global__ void __launch_bounds__(kThreads)
       mx = __reduce_max_sync(0xffffffffu, mx);
       if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
     }
-    for (int i = threadIdx.x; i < (int)bg.slice * ncomp; i += blockDim.x) acc[i] = 0ull;
+    for (int i = threadIdx.x; i < 2 * (int)bg.slice * ncomp; i += blockDim.x) acc_lo[i] = 0u;
     __syncthreads();
     const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
@@ -648,7 +653,8 @@ __global__ void __launch_bounds__(kThreads)
                   if (lx < 0 || lx >= vx) continue;
                   const long long w = __mul64hi(w1[i], wyz);
                   for (int c = 0; c < ncomp; ++c)
-                    atomicAdd(acc + c * bg.slice + row + lx, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                    atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + row + lx,
+                                       (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
                 }
               }
             }
@@ -703,9 +709,11 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
                 for (int r = 0; r < kQReg; ++r)
                   if (r < ncomp)
-                    atomicAdd(acc + r * bg.slice + node, (unsigned long long)((__mul64hi(w, qr[r]) + half) >> sh));
+                    atomic_add_split64(acc_lo, acc_hi, r * (int)bg.slice + node,
+                                       (unsigned long long)((__mul64hi(w, qr[r]) + half) >> sh));
                 for (int c = kQReg; c < ncomp; ++c)
-                  atomicAdd(acc + c * bg.slice + node, (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                  atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + node,
+                                     (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
               }
             }
           }
@@ -721,7 +729,9 @@ __global__ void __launch_bounds__(kThreads)
         if (lx < vx && ly < vy && lz < vz) {
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-          const T v = accumulated ? (T)ldexp((double)(long long)acc[c * bg.slice + lz * bg.pp + ly * bg.p0 + lx], -vexp)
+          const int64_t ai = c * bg.slice + lz * bg.pp + ly * bg.p0 + lx;
+          const long long a = (long long)(((unsigned long long)acc_hi[ai] << 32) | acc_lo[ai]);
+          const T v = accumulated ? (T)ldexp((double)a, -vexp)
                                   : (finite ? T(0) : quiet_nan<T>());
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
         }
@@ -861,20 +871,21 @@ struct ScatterPlan {
 };
 
 // Pitches of the scatter's shared accumulators.  A warp adds one point's contributions to
-// the nodes of its stencil inside the brick, x fastest, 32 nodes at a time, as 64-bit
-// atomics (two of the 32 four-byte banks each); with the brick's own row and plane pitches
-// the stencil's rows fall on the same banks (a 16-node row is 128 bytes).  Over row pitches
-// b0..b0+15 and plane pitches b1*p0..b1*p0+15 whose slice stays within max_slice words
-// (so that the padding costs no CTA per SM), this takes the pair with the fewest
-// shared-memory wavefronts summed over every position of a full n^3 stencil in the brick.
+// the nodes of its stencil inside the brick, x fastest, 32 nodes at a time, with 32-bit
+// atomics on a plane of low words and then a plane of high words (node i's word on bank
+// i mod 32); with the brick's own row and plane pitches the stencil's rows fall on the same
+// banks.  Over row pitches b0..b0+31 and plane pitches b1*p0..b1*p0+31 whose slice stays
+// within max_slice nodes (so that the padding costs no CTA per SM), this takes the pair
+// with the fewest shared-memory wavefronts summed over every position of a full n^3
+// stencil in the brick.
 void choose_acc_pitches(BrickGeo &bg, int n2, int64_t max_slice) {
   const int b0 = bg.b[0], b1 = bg.b[1], b2 = bg.b[2];
   const int nx = std::min(n2, b0), ny = std::min(n2, b1), nz = std::min(n2, b2);
   int64_t best = -1;
   int best_p0 = b0, best_pp = b0 * b1;
   std::vector<int> words;
-  for (int p0 = b0; p0 < b0 + 16; ++p0) {
-    for (int pp = b1 * p0; pp < b1 * p0 + 16; ++pp) {
+  for (int p0 = b0; p0 < b0 + 32; ++p0) {
+    for (int pp = b1 * p0; pp < b1 * p0 + 32; ++pp) {
       if ((int64_t)b2 * pp > max_slice && !(p0 == b0 && pp == b0 * b1)) continue;
       int64_t total = 0;
       for (int z0 = 0; z0 + nz <= b2; ++z0)
@@ -885,12 +896,12 @@ void choose_acc_pitches(BrickGeo &bg, int n2, int64_t max_slice) {
               for (int j = 0; j < ny; ++j)
                 for (int i = 0; i < nx; ++i) words.push_back((z0 + k) * pp + (y0 + j) * p0 + x0 + i);
             for (size_t c = 0; c < words.size(); c += 32) {
-              // wavefronts of one warp instruction: the words are distinct and a 64-bit word
-              // w sits on the bank pair w mod 16, so the most words sharing a pair
-              int per_pair[16] = {0};
-              for (size_t l = c; l < std::min(words.size(), c + 32); ++l) ++per_pair[words[l] & 15];
+              // wavefronts of one warp instruction: the words are distinct and word w sits on
+              // bank w mod 32, so the most words sharing a bank
+              int per_bank[32] = {0};
+              for (size_t l = c; l < std::min(words.size(), c + 32); ++l) ++per_bank[words[l] & 31];
               int mx = 0;
-              for (int q = 0; q < 16; ++q) mx = std::max(mx, per_pair[q]);
+              for (int q = 0; q < 32; ++q) mx = std::max(mx, per_bank[q]);
               total += mx;
             }
           }
