@@ -374,6 +374,8 @@ struct BrickGeo {
   // stencil spread over the banks (choose_acc_pitches)
   int32_t p0 = 0, pp = 0;
   int64_t slice = 0;
+  // most runs of consecutive keys along x in one row of any brick's region (brick_segments)
+  int32_t nseg = 1;
 };
 
 // One pass over the points in their own order: the locate, the brick-major key and the
@@ -478,7 +480,7 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // does not depend on which thread adds first, and no float atomics are used.  The 64-bit
 // sums are added as two 32-bit words with a carry (atomic_add_split64): native 32-bit
 // shared atomics (with 64-bit shared atomics ncu counted a shared load beside each one).
-constexpr int kFlatChunk = 2048;
+constexpr int kFlatChunk = 1024;
 // the scatter's static shared memory: one count per warp for the block scan
 constexpr int kScanSlots = 32;
 // quantities of a point the warp-per-point scatter holds in registers (the rest are read per use)
@@ -500,11 +502,15 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem_raw);
   uint32_t *acc_hi = acc_lo + (size_t)bg.slice * ncomp;
   uint32_t *off = acc_hi + (size_t)bg.slice * ncomp;                         // ecount: exclusive prefix
-  uint32_t *r0s = off + ecount;                                              // ecount: first slot
-  uint32_t *pslot = r0s + ecount;                                            // kFlatChunk: point slot
+  // along a row of the region, cells whose keys are consecutive hold consecutive slots, so
+  // one base (first slot - prefix) serves each such run of cells (segment)
+  uint32_t *segbase = off + ecount;                                          // E1*E2*nseg: slot bases
+  uint32_t *pslot = segbase + E1 * E2 * bg.nseg;                             // kFlatChunk: point slot
   uint32_t *pxyz = pslot + kFlatChunk;                                       // kFlatChunk: packed cell
   uint32_t *kx = pxyz + kFlatChunk, *ky = kx + E0, *kz = ky + E1;             // per-axis key tables
   uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
+  uint32_t *segx = kcnt + bvol + 1;                                          // E0: segment of each x
+  uint32_t *segfirst = segx + E0;                                            // nseg: first x of each
   __shared__ uint32_t warp_tot[kScanSlots];
   const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5, nwarps = (int)blockDim.x >> 5;
   const double qmax = __longlong_as_double((long long)*qmax_bits);
@@ -532,12 +538,24 @@ __global__ void __launch_bounds__(kThreads)
       else kz[e] = cb * (uint32_t)nb1 * (uint32_t)nb0 * (uint32_t)bvol + cl * (uint32_t)(B0 * B1);
     }
     __syncthreads();
+    if (warp == 0) {
+      // segments along x (E0 <= 32): a new one wherever the key does not step by one
+      const bool in = lane < E0;
+      const bool brk = in && (lane == 0 || kx[lane] != kx[lane - 1] + 1u);
+      const uint32_t starts = __ballot_sync(0xffffffffu, brk);
+      if (in) segx[lane] = (uint32_t)__popc(starts & (0xffffffffu >> (31 - lane))) - 1u;
+      const int sg = __popc(starts & ((1u << lane) - 1u));
+      if (brk && sg < bg.nseg) segfirst[sg] = (uint32_t)lane;
+    }
+    __syncthreads();
     {
       int ex = ex0, ey = ey0, ez = ez0;
       for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
         const uint32_t key = kx[ex] + ky[ey] + kz[ez];
         const uint32_t r0 = __ldg(cell_start + key);
-        r0s[e] = r0;
+        const uint32_t sg = segx[ex];
+        // first slot, for now (the host's bound on the segments keeps sg below nseg)
+        if (segfirst[sg] == (uint32_t)ex && sg < (uint32_t)bg.nseg) segbase[(ez * E1 + ey) * bg.nseg + sg] = r0;
         off[e] = __ldg(cell_start + key + 1) - r0;
         ex += esx;
         ey += esy;
@@ -591,6 +609,15 @@ __global__ void __launch_bounds__(kThreads)
     __syncthreads();
     const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
+    {
+      // each segment's base: its first slot less its first cell's prefix
+      const int nsg = min((int)segx[E0 - 1] + 1, bg.nseg);
+      for (int r = threadIdx.x; r < E1 * E2 * nsg; r += blockDim.x) {
+        const int row = r / nsg, sg = r - row * nsg;
+        segbase[row * bg.nseg + sg] -= off[row * E0 + (int)segfirst[sg]];
+      }
+    }
+    __syncthreads();
     const bool finite = isfinite(qmax);
     if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
     int eq = 0;
@@ -607,7 +634,7 @@ __global__ void __launch_bounds__(kThreads)
           int ex = ex0, ey = ey0, ez = ez0;
           for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
             const uint32_t lo = max(off[e], c0), hi = min(e + 1 < ecount ? off[e + 1] : count, c1);
-            const uint32_t base = r0s[e] - off[e];
+            const uint32_t base = segbase[(ez * E1 + ey) * bg.nseg + min(segx[ex], (uint32_t)bg.nseg - 1u)];
             const uint32_t packed = (uint32_t)ex | ((uint32_t)ey << 8) | ((uint32_t)ez << 16);
             for (uint32_t t = lo; t < hi; ++t) {
               pslot[t - c0] = base + t;
@@ -917,6 +944,26 @@ void choose_acc_pitches(BrickGeo &bg, int n2, int64_t max_slice) {
   bg.slice = (int64_t)b2 * best_pp;
 }
 
+// The most segments (runs of consecutive keys) along x in one row of any brick's region:
+// the region's x cells of brick column bc0 are (bc0*b0 - n2/2 + e) mod n0, e < b0 + n2 - 1,
+// keyed by brick * bvol + cell-in-brick, exactly as the scatter kernel keys them.
+int brick_segments(const BrickGeo &bg, int64_t n0, int n2) {
+  const int e0 = bg.b[0] + n2 - 1;
+  int most = 1;
+  for (int64_t bc0 = 0; bc0 < bg.nb[0]; ++bc0) {
+    int segs = 0;
+    int64_t prev = 0;
+    for (int e = 0; e < e0; ++e) {
+      const int64_t c = imod(bc0 * bg.b[0] - n2 / 2 + e, n0);
+      const int64_t key = (c / bg.b[0]) * bg.bvol + c % bg.b[0];
+      if (e == 0 || key != prev + 1) ++segs;
+      prev = key;
+    }
+    most = std::max(most, segs);
+  }
+  return most;
+}
+
 ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   ScatterPlan p;
   const int base[3] = {(size_t)ncomp * esize > 24 ? 8 : 16, 8, 8};
@@ -929,12 +976,15 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
     if (g.n[d] < n2 || g.n[d] >= (int64_t(1) << 31)) wide_enough = false;
   }
   p.bg.bvol = (int64_t)p.bg.b[0] * p.bg.b[1] * p.bg.b[2];
-  const size_t ecount = (size_t)(p.bg.b[0] + n2 - 1) * (p.bg.b[1] + n2 - 1) * (p.bg.b[2] + n2 - 1);
-  // shared memory besides the accumulators: region offsets and first slots, the point
-  // chunk, the key tables, the coverage counts
-  const size_t rest = 2 * sizeof(uint32_t) * ecount + 2 * sizeof(uint32_t) * kFlatChunk +
-                      sizeof(uint32_t) * (size_t)(p.bg.b[0] + p.bg.b[1] + p.bg.b[2] + 3 * (n2 - 1)) +
-                      sizeof(uint32_t) * (size_t)(p.bg.bvol + 1);
+  const int e0 = p.bg.b[0] + n2 - 1, e1 = p.bg.b[1] + n2 - 1, e2 = p.bg.b[2] + n2 - 1;
+  const size_t ecount = (size_t)e0 * e1 * e2;
+  if (e0 > 32) wide_enough = false;  // the kernel finds the x segments with one warp
+  p.bg.nseg = brick_segments(p.bg, g.n[0], n2);
+  // shared memory besides the accumulators: region offsets and segment bases, the point
+  // chunk, the key tables, the coverage counts, the segment of each x and first x of each
+  const size_t rest = sizeof(uint32_t) * ecount + sizeof(uint32_t) * (size_t)e1 * e2 * p.bg.nseg +
+                      2 * sizeof(uint32_t) * kFlatChunk + sizeof(uint32_t) * (size_t)(e0 + e1 + e2) +
+                      sizeof(uint32_t) * (size_t)(p.bg.bvol + 1) + sizeof(uint32_t) * (size_t)(e0 + p.bg.nseg);
   {
     // accumulator pitches that keep the unpadded layout's CTAs per SM (228 KB per SM, 1 KB
     // reserved per CTA by the runtime, the kernel's static scan slots) and its 200 KB cap;
