@@ -474,9 +474,10 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // w * 2^P (P = 62 - lb, |w| <= 2^lb from the scheme's Bernstein bound) and the
 // quantities q * 2^Q (Q = 62 - e, max|alpha q| < 2^e), both converted once per point;
 // each contribution is the high half of three signed 64 x 64-bit products,
-// hi(hi(hi(wy, wz), wx), q) = w1 w2 w3 q * 2^(3P + Q - 192) (truncated, relative error
-// ~2^-56), shifted right by sh bits so that the brick's largest node coverage K_max cannot
-// overflow (sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
+// hi(hi(hi(wy, wz), wx) >> sh, q) = w1 w2 w3 q * 2^(3P + Q - 192 - sh) (truncated, relative
+// error ~2^-(56 - sh)): the node's weight is shifted right by sh bits, once for all the
+// components, so that the brick's largest node coverage K_max cannot overflow
+// (|contribution| < 2^(56 - sh), sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
 // does not depend on which thread adds first, and no float atomics are used.  The 64-bit
 // sums are added as two 32-bit words with a carry (atomic_add_split64): native 32-bit
 // shared atomics (with 64-bit shared atomics ncu counted a shared load beside each one).
@@ -623,7 +624,6 @@ __global__ void __launch_bounds__(kThreads)
     int eq = 0;
     frexp(qmax, &eq);
     const int sh = max(0, (32 - __clz((int)kmax)) - 5);
-    const long long half = sh > 0 ? (1ll << (sh - 1)) : 0ll;  // the shift rounds to nearest
     // value = acc * 2^-(3P + Q - 192 - sh), P = wexp, Q = 62 - eq
     const int vexp = 3 * wexp + (62 - eq) - 192 - sh;
     const bool accumulated = finite && count > 0 && qmax > 0.0;
@@ -678,10 +678,10 @@ __global__ void __launch_bounds__(kThreads)
                 for (int i = 0; i < N2; ++i) {
                   const int lx = lxb + i;
                   if (lx < 0 || lx >= vx) continue;
-                  const long long w = __mul64hi(w1[i], wyz);
+                  const long long w = __mul64hi(w1[i], wyz) >> sh;
                   for (int c = 0; c < ncomp; ++c)
                     atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + row + lx,
-                                       (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                                       (unsigned long long)__mul64hi(w, __ldg(qv + c)));
                 }
               }
             }
@@ -731,16 +731,16 @@ __global__ void __launch_bounds__(kThreads)
               const long long wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
               const long long wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
               if (idx < count) {
-                const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
+                const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk)) >> sh;
                 const int node = node0 + k * bg.pp + j * bg.p0 + i;
 #pragma unroll
                 for (int r = 0; r < kQReg; ++r)
                   if (r < ncomp)
                     atomic_add_split64(acc_lo, acc_hi, r * (int)bg.slice + node,
-                                       (unsigned long long)((__mul64hi(w, qr[r]) + half) >> sh));
+                                       (unsigned long long)__mul64hi(w, qr[r]));
                 for (int c = kQReg; c < ncomp; ++c)
                   atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + node,
-                                     (unsigned long long)((__mul64hi(w, __ldg(qv + c)) + half) >> sh));
+                                     (unsigned long long)__mul64hi(w, __ldg(qv + c)));
               }
             }
           }
