@@ -266,9 +266,9 @@ __global__ void __launch_bounds__(kNThreads)
 
 // The fixed-point scales of a spread.  Weights are w * 2^62 (ES weights lie in [0, 1]);
 // quantities q * 2^(62 - eq) with max|q| < 2^eq; a contribution is
-// hi(hi(hi(Wy, Wz), Wx), |Q|) = w |q| 2^(56 - eq) < 2^56, shifted right (rounded) by
-// s = max(0, em - 6) with M <= 2^em, so that no node's sum of at most M contributions can
-// reach 2^62.  A node's value is its sum times 2^(eq + s - 56).
+// hi(hi(hi(Wy, Wz), Wx) >> s, |Q|) = w |q| 2^(56 - eq - s) < 2^(56 - s), the node weight
+// shifted right by s = max(0, em - 6) with M <= 2^em, so that no node's sum of at most M
+// contributions can reach 2^62.  A node's value is its sum times 2^(eq + s - 56).
 struct SpreadScale {
   int eq, s;
 };
@@ -339,10 +339,11 @@ __global__ void __launch_bounds__(kNThreads)
 
 // Spread, pass 3: a CTA per tile.  For a group of CG components at a time the tile's
 // region ((kTile + W - 1)^3 nodes) is summed in shared memory -- a warp per point, its lanes
-// over the point's W^3 nodes, each contribution hi(hi(Wyz, Wx), |Q|) formed with integer
-// high products (no FP64 arithmetic per node) and added by a shared 64-bit integer atomic
-// -- then every nonzero node sum is added to the grid's by one global integer atomic.
-// Integer sums do not depend on the order of the adds.
+// over the point's W^3 nodes, each contribution hi(hi(Wyz, Wx) >> s, |Q|) formed with
+// integer high products (no FP64 arithmetic per node; the node weight shifted once for all
+// components) and added to the node's 64-bit sum as 32-bit low and high words with a carry
+// (native 32-bit shared atomics) -- then every nonzero node sum is added to the grid's by
+// one global integer atomic.  Integer sums do not depend on the order of the adds.
 constexpr int kMaxGroup = 32;
 
 template <int W>
@@ -354,13 +355,14 @@ __global__ void __launch_bounds__(kNThreads)
                          const unsigned long long *__restrict__ qmax_bits, unsigned long long *__restrict__ acc) {
   constexpr int R = kTile + W - 1;
   constexpr int R3 = R * R * R;
-  extern __shared__ unsigned long long sacc[];  // group x R3 sums
+  // group x R3 64-bit sums: a plane of low words, then a plane of high words
+  extern __shared__ uint32_t sacc_lo[];
+  uint32_t *sacc_hi = sacc_lo + group * R3;
   __shared__ unsigned long long swyz[kNThreads / 32][W * W], swx[kNThreads / 32][W];
   __shared__ long long sq[kNThreads / 32][kMaxGroup];
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   if (!isfinite(qmax)) return;  // the field is set to NaN by k_nufft_finish
   const SpreadScale sc = spread_scale(*qmax_bits, m);
-  const unsigned long long round = sc.s ? (1ull << (sc.s - 1)) : 0ull;
   const int64_t nxy = g.n[0] * g.n[1], npf = nxy * g.n[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -369,7 +371,10 @@ __global__ void __launch_bounds__(kNThreads)
     const int64_t tx = (tile % nt0) * kTile, ty = ((tile / nt0) % nt1) * kTile, tz = (tile / (nt0 * nt1)) * kTile;
     for (int c0 = 0; c0 < ncomp; c0 += group) {
       const int cg = min(group, ncomp - c0);
-      for (int r = threadIdx.x; r < cg * R3; r += blockDim.x) sacc[r] = 0ull;
+      for (int r = threadIdx.x; r < cg * R3; r += blockDim.x) {
+        sacc_lo[r] = 0u;
+        sacc_hi[r] = 0u;
+      }
       __syncthreads();
       for (uint32_t pt = t0 + warp; pt < t1; pt += nwarps) {
         const uint32_t wi = order[pt];
@@ -388,19 +393,19 @@ __global__ void __launch_bounds__(kNThreads)
         __syncwarp();
         for (int idx = lane; idx < W * W * W; idx += 32) {
           const int i = idx % W, jk = idx / W, j = jk % W, kk = jk / W;
-          const unsigned long long wxyz = __umul64hi(swyz[warp][jk], swx[warp][i]);
+          const unsigned long long wxyz = __umul64hi(swyz[warp][jk], swx[warp][i]) >> sc.s;
           const int r = ((oz + kk) * R + oy + j) * R + ox + i;
           for (int cc = 0; cc < cg; ++cc) {
             const long long qq = sq[warp][cc];
-            const unsigned long long mag = (__umul64hi(wxyz, (unsigned long long)(qq < 0 ? -qq : qq)) + round) >> sc.s;
-            atomicAdd(sacc + cc * R3 + r, qq < 0 ? (unsigned long long)(-(long long)mag) : mag);
+            const unsigned long long mag = __umul64hi(wxyz, (unsigned long long)(qq < 0 ? -qq : qq));
+            atomic_add_split64(sacc_lo, sacc_hi, cc * R3 + r, qq < 0 ? (unsigned long long)(-(long long)mag) : mag);
           }
         }
         __syncwarp();
       }
       __syncthreads();
       for (int e = threadIdx.x; e < cg * R3; e += blockDim.x) {
-        const unsigned long long v = sacc[e];
+        const unsigned long long v = ((unsigned long long)sacc_hi[e] << 32) | sacc_lo[e];
         if (v == 0ull) continue;
         const int cc = e / R3, r = e - cc * R3;
         const int rx = r % R, ry = (r / R) % R, rz = r / (R * R);
