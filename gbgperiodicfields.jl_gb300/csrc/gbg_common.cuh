@@ -51,6 +51,28 @@ __device__ __forceinline__ double fma_rn(double a, double b, double c) { return 
 __device__ __forceinline__ float fma_rn(float a, float b, float c) { return fmaf(a, b, c); }
 
 // Julia's integer mod for a positive divisor: the result lies in [0, n).
+// x * 2^e rounded to the nearest integer, ties to even, for finite x with |x| 2^e < 2^63:
+// the value __double2ll_rn(x * 2^e) has wherever x * 2^e is exact in double (e >= 0, or no
+// underflow), formed from the mantissa and exponent bits on the integer pipes instead of a
+// product and a conversion on the FP64 pipe.
+__device__ __forceinline__ long long fixed_rn(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int bexp = (int)((b >> 52) & 0x7ffu);
+  const unsigned long long mant = (b & 0xfffffffffffffull) | (bexp ? (1ull << 52) : 0ull);
+  const int sh = (bexp ? bexp : 1) - 1075 + e;  // x 2^e = mant 2^sh
+  unsigned long long r;
+  if (sh >= 0) {
+    r = mant << sh;
+  } else if (sh < -54) {
+    r = 0ull;  // below 2^-2
+  } else {
+    const int rs = -sh;
+    const unsigned long long q = mant >> rs, rem = mant & ((1ull << rs) - 1ull), halfway = 1ull << (rs - 1);
+    r = q + (unsigned long long)(rem > halfway || (rem == halfway && (q & 1ull)));
+  }
+  return (b >> 63) ? -(long long)r : (long long)r;
+}
+
 // Adds v to a 64-bit integer kept in shared memory as two 32-bit words, lo[i] and hi[i],
 // with native 32-bit atomics: the low word's add returns the old value, whose wrap is the
 // carry into the high word.  Each add wraps the low word at most once, so after all adds

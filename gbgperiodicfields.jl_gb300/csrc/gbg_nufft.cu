@@ -315,7 +315,7 @@ __global__ void __launch_bounds__(kNThreads)
         es_weights<W>(t, beta, half, w);
 #pragma unroll
         for (int i = 0; i < W; ++i)  // w * 2^62, exact to the rounding of one conversion
-          wbuf[(3 * wi + a) * W + i] = ok ? (unsigned long long)__double2ll_rn(ldexp((double)w[i], 62)) : 0ull;
+          wbuf[(3 * wi + a) * W + i] = ok ? (unsigned long long)fixed_rn((double)w[i], 62) : 0ull;
       }
       s[a] = imod(base + (1 - half), g.n[a]);
       first[3 * wi + a] = (int32_t)s[a];
@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(kNThreads)
         if (lane < cg) {
           const int64_t qi = p + m * (c0 + lane);
           const double q = q_f64 ? static_cast<const double *>(qv_)[qi] : (double)static_cast<const float *>(qv_)[qi];
-          sq[warp][lane] = __double2ll_rn(ldexp(q, 62 - sc.eq));
+          sq[warp][lane] = fixed_rn(q, 62 - sc.eq);
         }
         const int ox = (int)(first[3 * (int64_t)wi] - tx), oy = (int)(first[3 * (int64_t)wi + 1] - ty),
                   oz = (int)(first[3 * (int64_t)wi + 2] - tz);

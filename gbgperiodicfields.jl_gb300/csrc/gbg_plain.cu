@@ -431,9 +431,7 @@ __global__ void __launch_bounds__(kThreads)
   int e = 0;
   frexp(qmax, &e);
   const bool finite = isfinite(qmax);
-  // 2^wexp and 2^(62-e) are normal doubles (e <= 1024), so each product rounds once, as
-  // ldexp does; the weight products are exact, then 53-bit integers
-  const double wscale = ldexp(1.0, wexp), qscale = ldexp(1.0, 62 - e);
+  // w 2^wexp and alpha q 2^(62 - e) rounded once to integers (fixed_rn)
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[sl];
@@ -446,11 +444,11 @@ __global__ void __launch_bounds__(kThreads)
       T w[N2];
       axis_weights_fma<T, N2, M2>(sch, ok ? t[d] : quiet_nan<T>(), w);
 #pragma unroll
-      for (int k = 0; k < N2; ++k) dst[d * N2 + k] = ok ? __double2ll_rn((double)w[k] * wscale) : 0ll;
+      for (int k = 0; k < N2; ++k) dst[d * N2 + k] = ok ? fixed_rn((double)w[k], wexp) : 0ll;
     }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);
-      qi[sl * ncomp + c] = finite ? __double2ll_rn((double)v * qscale) : 0ll;
+      qi[sl * ncomp + c] = finite ? fixed_rn((double)v, 62 - e) : 0ll;
     }
   }
 }
