@@ -144,8 +144,8 @@ KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 4, 3>", "gather_quint
 # DRAM bytes (read + write) per launch of those kernels on this workload, from one ncu capture
 # of dram__bytes_read.sum + dram__bytes_write.sum (one pass) on the full-size step (the timed
 # step's launches; the warm-up step's agree to 0.1%).
-NCU_TRAFFIC = {"gather_cubic": 5857477376, "scatter_cubic": 2846136576,
-               "gather_quintic": 6050684928, "scatter_quintic": 5662607872}
+NCU_TRAFFIC = {"gather_cubic": 5867726592, "scatter_cubic": 2899915520,
+               "gather_quintic": 6046056192, "scatter_quintic": 5924986624}
 
 
 def fp64_peak_tflops() -> float:

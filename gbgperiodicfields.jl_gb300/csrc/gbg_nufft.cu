@@ -266,9 +266,9 @@ __global__ void __launch_bounds__(kNThreads)
 
 // The fixed-point scales of a spread.  Weights are w * 2^62 (ES weights lie in [0, 1]);
 // quantities q * 2^(62 - eq) with max|q| < 2^eq; a contribution is
-// hi(hi(hi(Wy, Wz), Wx) >> s, |Q|) = w |q| 2^(56 - eq - s) < 2^(56 - s), the node weight
-// shifted right by s = max(0, em - 6) with M <= 2^em, so that no node's sum of at most M
-// contributions can reach 2^62.  A node's value is its sum times 2^(eq + s - 56).
+// hi(hi(hi(Wy, Wz), Wx), |Q|) = w |q| 2^(56 - eq) < 2^56, shifted right (rounded) by
+// s = max(0, em - 6) with M <= 2^em, so that no node's sum of at most M contributions can
+// reach 2^62.  A node's value is its sum times 2^(eq + s - 56).
 struct SpreadScale {
   int eq, s;
 };
@@ -339,9 +339,9 @@ __global__ void __launch_bounds__(kNThreads)
 
 // Spread, pass 3: a CTA per tile.  For a group of CG components at a time the tile's
 // region ((kTile + W - 1)^3 nodes) is summed in shared memory -- a warp per point, its lanes
-// over the point's W^3 nodes, each contribution hi(hi(Wyz, Wx) >> s, |Q|) formed with
-// integer high products (no FP64 arithmetic per node; the node weight shifted once for all
-// components) and added to the node's 64-bit sum as 32-bit low and high words with a carry
+// over the point's W^3 nodes, each contribution hi(hi(Wyz, Wx), |Q|) formed with integer
+// high products (no FP64 arithmetic per node) and rounded to s bits, then added to the
+// node's 64-bit sum as 32-bit low and high words with a carry
 // (native 32-bit shared atomics) -- then every nonzero node sum is added to the grid's by
 // one global integer atomic.  Integer sums do not depend on the order of the adds.
 constexpr int kMaxGroup = 32;
@@ -363,6 +363,7 @@ __global__ void __launch_bounds__(kNThreads)
   const double qmax = __longlong_as_double((long long)*qmax_bits);
   if (!isfinite(qmax)) return;  // the field is set to NaN by k_nufft_finish
   const SpreadScale sc = spread_scale(*qmax_bits, m);
+  const unsigned long long round = sc.s ? (1ull << (sc.s - 1)) : 0ull;
   const int64_t nxy = g.n[0] * g.n[1], npf = nxy * g.n[2];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -393,11 +394,11 @@ __global__ void __launch_bounds__(kNThreads)
         __syncwarp();
         for (int idx = lane; idx < W * W * W; idx += 32) {
           const int i = idx % W, jk = idx / W, j = jk % W, kk = jk / W;
-          const unsigned long long wxyz = __umul64hi(swyz[warp][jk], swx[warp][i]) >> sc.s;
+          const unsigned long long wxyz = __umul64hi(swyz[warp][jk], swx[warp][i]);
           const int r = ((oz + kk) * R + oy + j) * R + ox + i;
           for (int cc = 0; cc < cg; ++cc) {
             const long long qq = sq[warp][cc];
-            const unsigned long long mag = __umul64hi(wxyz, (unsigned long long)(qq < 0 ? -qq : qq));
+            const unsigned long long mag = (__umul64hi(wxyz, (unsigned long long)(qq < 0 ? -qq : qq)) + round) >> sc.s;
             atomic_add_split64(sacc_lo, sacc_hi, cc * R3 + r, qq < 0 ? (unsigned long long)(-(long long)mag) : mag);
           }
         }

@@ -472,10 +472,14 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
 // w * 2^P (P = 62 - lb, |w| <= 2^lb from the scheme's Bernstein bound) and the
 // quantities q * 2^Q (Q = 62 - e, max|alpha q| < 2^e), both converted once per point;
 // each contribution is the high half of three signed 64 x 64-bit products,
-// hi(hi(hi(wy, wz), wx) >> sh, q) = w1 w2 w3 q * 2^(3P + Q - 192 - sh) (truncated, relative
-// error ~2^-(56 - sh)): the node's weight is shifted right by sh bits, once for all the
-// components, so that the brick's largest node coverage K_max cannot overflow
-// (|contribution| < 2^(56 - sh), sh = max(0, bits(K_max) - 5)).  Integer addition is associative, so the result
+// hi(round(hi(hi(wy, wz), wx) / 2^sh), q) = w1 w2 w3 q * 2^(3P + Q - 192 - sh): the node's
+// weight is shifted right by sh bits (rounded), once for all the components, so that the
+// brick's largest node coverage K_max cannot overflow (with |w 2^P| <= 1.5 * 2^62 and
+// |q 2^Q| < 2^62, |contribution| < 2^(57.76 - sh); sh = max(0, bits(K_max) - 5) keeps a node's
+// sum below 2^62.76).  The last high product floors, so each contribution is low by half a
+// unit on average; the write-back adds that mean back for the node's K contributions (K/2
+// units), which leaves an error within K/2 units, as rounding every contribution would, and
+// unbiased.  Integer addition is associative, so the result
 // does not depend on which thread adds first, and no float atomics are used.  The 64-bit
 // sums are added as two 32-bit words with a carry (atomic_add_split64): native 32-bit
 // shared atomics (with 64-bit shared atomics ncu counted a shared load beside each one).
@@ -622,6 +626,7 @@ __global__ void __launch_bounds__(kThreads)
     int eq = 0;
     frexp(qmax, &eq);
     const int sh = max(0, (32 - __clz((int)kmax)) - 5);
+    const long long wround = sh > 0 ? (1ll << (sh - 1)) : 0ll;  // the node weight's shift rounds
     // value = acc * 2^-(3P + Q - 192 - sh), P = wexp, Q = 62 - eq
     const int vexp = 3 * wexp + (62 - eq) - 192 - sh;
     const bool accumulated = finite && count > 0 && qmax > 0.0;
@@ -676,7 +681,7 @@ __global__ void __launch_bounds__(kThreads)
                 for (int i = 0; i < N2; ++i) {
                   const int lx = lxb + i;
                   if (lx < 0 || lx >= vx) continue;
-                  const long long w = __mul64hi(w1[i], wyz) >> sh;
+                  const long long w = (__mul64hi(w1[i], wyz) + wround) >> sh;
                   for (int c = 0; c < ncomp; ++c)
                     atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + row + lx,
                                        (unsigned long long)__mul64hi(w, __ldg(qv + c)));
@@ -729,7 +734,7 @@ __global__ void __launch_bounds__(kThreads)
               const long long wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
               const long long wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
               if (idx < count) {
-                const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk)) >> sh;
+                const long long w = (__mul64hi(wxi, __mul64hi(wyj, wzk)) + wround) >> sh;
                 const int node = node0 + k * bg.pp + j * bg.p0 + i;
 #pragma unroll
                 for (int r = 0; r < kQReg; ++r)
@@ -755,7 +760,9 @@ __global__ void __launch_bounds__(kThreads)
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
           const int64_t ai = c * bg.slice + lz * bg.pp + ly * bg.p0 + lx;
-          const long long a = (long long)(((unsigned long long)acc_hi[ai] << 32) | acc_lo[ai]);
+          // each of the node's kcnt contributions was floored (the high product), half a
+          // unit low on average: that mean is added back, once
+          const long long a = (long long)(((unsigned long long)acc_hi[ai] << 32) | acc_lo[ai]) + (long long)(kcnt[nl] >> 1);
           const T v = accumulated ? (T)ldexp((double)a, -vexp)
                                   : (finite ? T(0) : quiet_nan<T>());
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
