@@ -277,6 +277,11 @@ def run_gb300(args, rank, world):
             kernel_times[nm].append(a.elapsed_time(b))
     if int(status.item()) != 0:
         raise RuntimeError(f"device status {int(status.item())}")
+    if rank == 0 and not args.no_cpu:
+        # the last timed step's quintic outputs, checked against the oracle after the CPU
+        # baseline has run (oracle_check)
+        _LAST_OUTPUTS.update(field=np.asfortranarray(field.cpu().numpy()), gather=np.asfortranarray(out.cpu().numpy()),
+                             scatter=np.asfortranarray(dep.cpu().numpy()))
 
     ms_total = reduce_max(ms_total, world, dev)
     evals_per_step = 4 * M_POINTS
@@ -753,6 +758,37 @@ def reduce_max(value: float, world: int, device) -> float:
 
 # ----------------------------------------------------------- CPU baseline
 
+_LAST_OUTPUTS: dict = {}
+
+
+def oracle_check(pos_h, q_h):
+    """The last timed step's quintic gather and scatter (all 1e7 points) against the oracle
+    on the same inputs and the same field, run over all host cores: max and RMS error
+    relative to max|oracle|, beside the Float64 bar the parity tests hold (1e-13)."""
+    if not _LAST_OUTPUTS:
+        return None
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle
+    o = _LAST_OUTPUTS
+    g = oracle.grid_dict(N_GRID)
+    coeffs = oracle.lalescu(6)
+    cores = os.cpu_count() or 1
+    p, qq = np.asfortranarray(pos_h), np.asfortranarray(q_h)
+    t0 = time.perf_counter()
+    want_g = oracle.gather(g, o["field"], p, coeffs, nthreads=cores)
+    want_s = oracle.scatter(g, np.zeros(o["field"].shape, order="F"), p, qq, coeffs, 1.0, 0.0, nthreads=cores)
+
+    def rel(got, want):
+        d = got.reshape(want.shape, order="F") - want
+        scale = float(np.abs(want).max())
+        return {"max_rel": float(np.abs(d).max() / scale), "rms_rel": float(np.sqrt(np.mean(d * d)) / scale)}
+
+    res = {"gather_quintic": rel(o["gather"], want_g), "scatter_quintic": rel(o["scatter"], want_s), "bar": 1e-13,
+           "points": M_POINTS, "oracle_seconds": round(time.perf_counter() - t0, 1)}
+    _LAST_OUTPUTS.clear()
+    return res
+
+
 def cpu_sample_rate(pos_h, q_h, field_h, target_seconds: float):
     """Times the reference's CPU path (oracle, OpenMP over all host cores) on a bounded
     sample of the points: the same four transfers per point as a GPU step."""
@@ -921,6 +957,7 @@ def main():
             from gbgperiodicfields_gb300.workloads import spectral_field
             field_h = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device="cpu")
             res["cpu_baseline"] = cpu_sample_rate(pos_h, q_h, field_h, args.cpu_seconds)
+            res["error_vs_oracle"] = oracle_check(pos_h, q_h)
     if rank == 0 and res is not None:
         print(json.dumps(res), flush=True)
     if world > 1:
