@@ -277,10 +277,13 @@ gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_sche
  * Many independent instances of uneven sizes (fields of different grids and component
  * counts, point sets of different sizes, mixed stencil widths) run as ONE persistent
  * gather launch and ONE persistent scatter launch: every (instance, brick) is a unit of
- * work that the CTAs take from a device counter, largest instances first.  The batch
- * holds device copies of each instance's geometry, scheme and TMA descriptor, so
- * gbg_batch_run issues only stream operations and can be captured in a CUDA graph
- * together with the gbg_bins_build calls that precede it. */
+ * work that the CTAs take from a device counter, largest instances first.  Instances of
+ * 1024 points or more run through the single-instance kernels of gbg_interpolate_binned /
+ * gbg_anterpolate_binned instead, which are faster for them (same results: both sums are
+ * formed in an order fixed by the points); every gather still runs before any scatter.
+ * The batch holds device copies of each pooled instance's geometry, scheme and TMA
+ * descriptor, so gbg_batch_run issues only stream operations and can be captured in a
+ * CUDA graph together with the gbg_bins_build calls that precede it. */
 typedef struct gbg_batch_s *gbg_batch;
 typedef struct {
   gbg_field field;    /* gathered from (FP32 resident storage) */

@@ -1,5 +1,6 @@
 """GPU tests of the batched form: instances of uneven sizes (grids, components, point
-counts, stencil widths) in one persistent gather launch and one persistent scatter launch.
+counts, stencil widths) in one persistent gather launch and one persistent scatter launch,
+and beside them instances large enough to run through the single-instance kernels.
 Each instance's batched result must equal its single-instance result bitwise (the same
 arithmetic in the same order) and the FP64 oracle within the precision form's 1e-5; the
 whole step (bins builds + batch) is also replayed from a captured CUDA graph."""
@@ -15,12 +16,13 @@ def relerr(got, want):
     return np.abs(np.asarray(got, np.float64) - want).max() / max(np.abs(want).max(), 1e-300)
 
 
-def make_instances(gbg, oracle, seed=0):
+def make_instances(gbg, oracle, seed=0, specs=None):
     from gbgperiodicfields_gb300 import resident
     rng = np.random.default_rng(seed)
-    specs = [((16, 16, 16), 1, 700, gbg.CatmullRom), ((24, 20, 18), 3, 5000, gbg.LalescuSpline(6)),
-             ((32, 32, 32), 12, 20000, gbg.CatmullRom), ((20, 22, 24), 9, 3000, gbg.CatmullRom),
-             ((18, 18, 18), 3, 1500, gbg.LagrangeSpline(8)), ((28, 16, 20), 4, 9000, gbg.LalescuSpline(6))]
+    if specs is None:
+        specs = [((16, 16, 16), 1, 700, gbg.CatmullRom), ((24, 20, 18), 3, 5000, gbg.LalescuSpline(6)),
+                 ((32, 32, 32), 12, 20000, gbg.CatmullRom), ((20, 22, 24), 9, 3000, gbg.CatmullRom),
+                 ((18, 18, 18), 3, 1500, gbg.LagrangeSpline(8)), ((28, 16, 20), 4, 9000, gbg.LalescuSpline(6))]
     insts = []
     for n, C, M, scheme in specs:
         grid = gbg.Grid3D(n, (TWO_PI,) * 3, origin=(0.1, -0.2, 0.3))
@@ -45,8 +47,17 @@ def dev():
     return torch.device("cuda:0")
 
 
-def test_batch_matches_single_and_oracle(gbg, oracle, dev):
-    resident, insts = make_instances(gbg, oracle)
+def mixed_specs(gbg):
+    """Instances below 1024 points, which share the persistent launches, beside larger
+    ones, which the batch runs through the single-instance kernels."""
+    return [((16, 16, 16), 1, 700, gbg.CatmullRom), ((40, 36, 32), 3, 70000, gbg.LalescuSpline(6)),
+            ((20, 22, 24), 9, 600, gbg.CatmullRom), ((48, 48, 48), 4, 90000, gbg.CatmullRom),
+            ((18, 18, 18), 3, 1500, gbg.LagrangeSpline(8))]
+
+
+@pytest.mark.parametrize("mixed", [False, True], ids=["pooled", "pooled+direct"])
+def test_batch_matches_single_and_oracle(gbg, oracle, dev, mixed):
+    resident, insts = make_instances(gbg, oracle, specs=mixed_specs(gbg) if mixed else None)
     batch = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"], dest=i["dest"],
                                  q=i["qt"], alpha=1.0, beta=0.0) for i in insts])
     status = torch.zeros(1, dtype=torch.int32, device="cuda")
@@ -66,8 +77,9 @@ def test_batch_matches_single_and_oracle(gbg, oracle, dev):
         assert torch.equal(inst["field"].read(), inst["dest"].read())
 
 
-def test_batch_step_in_cuda_graph(gbg, oracle, dev):
-    resident, insts = make_instances(gbg, oracle, seed=5)
+@pytest.mark.parametrize("mixed", [False, True], ids=["pooled", "pooled+direct"])
+def test_batch_step_in_cuda_graph(gbg, oracle, dev, mixed):
+    resident, insts = make_instances(gbg, oracle, seed=5, specs=mixed_specs(gbg) if mixed else None)
     batch = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"], dest=i["dest"],
                                  q=i["qt"]) for i in insts])
 
