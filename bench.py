@@ -147,6 +147,18 @@ KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 4, 3>", "gather_quint
 NCU_TRAFFIC = {"gather_cubic": 5867726592, "scatter_cubic": 2899915520,
                "gather_quintic": 6046056192, "scatter_quintic": 5924986624}
 
+# What bounds those kernels, from the ncu captures summarised in profiles/ (not measured in
+# this run): the scatters run on the integer pipes, the gathers on the FP64 pipe.
+_SCATTER_LIMITER = {"pipe": "integer issue (signed 64-bit high products, shared 32-bit atomics)",
+                    "issue_active_pct": 70.1, "fma_heavy_pct": 56.4, "alu_pct": 53.1, "dram_pct": 2.6,
+                    "source": "ncu --set full, 256^3 x 3, 4e6 clustered points, quintic "
+                              "(profiles/fp64_scatter_k_scatter_fixed64_256cube_c3_4e6_quintic.md)"}
+NCU_LIMITER = {"scatter_cubic": _SCATTER_LIMITER, "scatter_quintic": _SCATTER_LIMITER,
+               "gather_cubic": {"pipe": "FP64", "fp64_pipe_pct": 94.4,
+                                "source": "profiles/fp64_gather_k_gather_plain_256cube_c3_4e6_quintic.md"},
+               "gather_quintic": {"pipe": "FP64", "fp64_pipe_pct": 94.4,
+                                  "source": "profiles/fp64_gather_k_gather_plain_256cube_c3_4e6_quintic.md"}}
+
 
 def fp64_peak_tflops() -> float:
     """FP64 throughput of this GPU, measured: the best of a few cuBLAS DGEMMs."""
@@ -317,7 +329,8 @@ def run_gb300(args, rank, world):
                      "fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                               "frac": fp64_achieved / fp64_peak if fp64_peak else None,
                               "algorithmic_flops": dom_flops,
-                              "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"}},
+                              "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"},
+                     "limiter": NCU_LIMITER.get(dominant)},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
