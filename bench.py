@@ -1,20 +1,29 @@
 #!/usr/bin/env python
 """Benchmark of the particle gather/scatter path on GB300.
 
-Workload (the benchmark's plain-FP64-at-scale configuration): a 256^3 Float64
-3-component velocity field (random Fourier modes |k| <= 64, |k|^(-11/6) spectrum,
-divergence projected out) on [0, 2pi)^3 and 1e7 points, 70% uniform + 30% in 1000
-Gaussian blobs of sigma = 0.05.  One step = build the traversal order, then cubic
-(CatmullRom) gather + scatter and quintic (LalescuSpline(6)) gather + scatter: 4
-particle-evaluations per point per step (one evaluation = one point x one field, all
-components, one transfer).  Inputs are synthetic and seeded; the field (403 MB) and the
-point arrays are larger than L2, so no L2 flush is needed between steps.
+Headline workload (the precision form, the largest configuration that fits one GPU): a
+512^3 field of 3 velocity components plus the 9-component velocity-gradient tensor (random
+Fourier modes |k| <= 64, |k|^(-11/6) spectrum, divergence projected out, the gradient
+computed spectrally), held as one 12-component FP32 resident field; 3.2e7 uniform points
+with FP64 positions (FP64 is kept for the periodic wrap and the cell/fraction split only);
+cubic (CatmullRom) splines.  One step = rebuild the device cell bins from the positions,
+gather the 12 components at every point, scatter 12 quantities per point into a second
+resident field (beta = 0): 2 particle-evaluations per point per step (one evaluation = one
+point x one transfer of the 12-component field).  The caller's particle state is kept in
+binned order (as a particle code re-orders its arrays after moving them), and the bins are
+rebuilt from those positions every step.  Inputs are synthetic and seeded; the field
+(6.6 GB) and the point arrays are larger than L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Prints one JSON line (rank 0).  With --impl reference it times the reference's CPU path
-(the oracle's OpenMP restatement of the reference's KernelAbstractions CPU kernels) on
-the host cores, on a bounded sample of the same workload.
+Prints one JSON line (rank 0).  `e2e` is the same step through the C ABI from host
+buffers: every step uploads the field, the positions and the quantities from pinned host
+memory and reads the gathered values and the deposited field back.  `--impl reference`
+times the reference's CPU path (the oracle's OpenMP restatement of the reference's
+KernelAbstractions CPU kernels: traversal order, gather, atomic scatter) on the host cores,
+each step on a block of the same points against the full FP64 field.  Secondary keys: the
+FP64 drop-in on the same inputs, the plain-FP64-at-scale workload (256^3 x 3, 1e7
+clustered points, cubic + quintic), the batched, served and NUFFT forms, and oracle checks.
 """
 from __future__ import annotations
 
@@ -35,13 +44,28 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "particle-evals/s (gather+scatter) at fixed error vs FP64; serving p50/p99 ms"
 UNIT = "particle-evals/s"
-N_GRID = (256, 256, 256)
-NCOMP = 3
-M_POINTS = 10_000_000
-KMAX = 64
-WORKLOAD = ("256^3 Float64 3-component velocity field (|k|<=64, |k|^-11/6, divergence-free), "
-            "1e7 points (70% uniform + 30% in 1000 Gaussian blobs, sigma=0.05), "
-            "cubic + quintic gather and scatter per step, traversal order rebuilt per step")
+
+# headline: the precision form at full size
+N3 = (512, 512, 512)
+C3 = 12
+M3 = 32_000_000
+KMAX3 = 64
+WORKLOAD = ("512^3 x (3 velocity + 9 velocity-gradient) FP32 resident field (|k|<=64, |k|^-11/6, "
+            "divergence-free), FP64 positions, 3.2e7 uniform points kept in binned order, cubic "
+            "(CatmullRom); per step: bins rebuilt, gather of the 12 components, scatter of 12 "
+            "quantities (beta=0)")
+CONFIG = {"workload": WORKLOAD, "grid": list(N3), "ncomp": C3, "points": M3, "scheme": "CatmullRom",
+          "storage": "f32 field, f64 positions", "evals_per_point_per_step": 2, "parallelism": "replicas",
+          "l2": "inputs larger than L2 (field 6.6 GB), no flush"}
+
+# secondary: plain FP64 at scale
+N2G = (256, 256, 256)
+NCOMP2 = 3
+M2 = 10_000_000
+KMAX2 = 64
+
+# reference arm / CPU baseline: points per step of the CPU port
+CPU_BLOCK = 2_000_000
 
 
 def parse():
@@ -51,14 +75,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and the oracle checks")
+    ap.add_argument("--cpu-block", type=int, default=CPU_BLOCK,
+                    help="points per step of the CPU port (reference arm and CPU baseline)")
     ap.add_argument("--no-forms", action="store_true",
-                    help="skip the precision, batched and served forms (reported beside the headline)")
-    ap.add_argument("--no-peaks", action="store_true",
-                    help="skip the FP64 peak measurement (a cuBLAS DGEMM), e.g. under a profiler's launch list")
+                    help="skip the secondary workloads (FP64 drop-in, plain FP64 at scale, batched, served, NUFFT)")
     ap.add_argument("--case", choices=sorted(PROFILE_CASES),
-                    help="run one small fixed case twice and exit (the inputs of the ncu captures in profiles/)")
+                    help="run one small fixed case twice and exit (the inputs of the committed ncu captures)")
     return ap.parse_args()
 
 
@@ -118,16 +141,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# --------------------------------------------------------------- workload
-
-def make_inputs_host(seed: int = 1):
-    from __graft_entry__ import load_package
-    load_package()
-    from gbgperiodicfields_gb300.workloads import clustered_points
-    pos = clustered_points(M_POINTS, seed=seed + 1)
-    q = np.asfortranarray(np.random.Generator(np.random.PCG64(seed + 2)).standard_normal((M_POINTS, NCOMP)))
-    return pos, q
-
+# --------------------------------------------------------------- inputs
 
 def peaks():
     p = ROOT / "MEASURED_PEAKS.json"
@@ -137,100 +151,89 @@ def peaks():
     return 6800.0, "fallback"
 
 
-# The main kernel of each timed call of the headline step.
-KERNEL_NAMES = {"gather_cubic": "k_gather_plain<double, 4, 4, 3>", "gather_quintic": "k_gather_plain<double, 6, 6, 3>",
-                "scatter_cubic": "k_scatter_fixed64<double, 4>", "scatter_quintic": "k_scatter_fixed64<double, 6>"}
-
-# DRAM bytes (read + write) per launch of those kernels on this workload, from one ncu capture
-# of dram__bytes_read.sum + dram__bytes_write.sum (one pass) on the full-size step (the timed
-# step's launches; the warm-up step's agree to 0.1%).
-NCU_TRAFFIC = {"gather_cubic": 5867726592, "scatter_cubic": 2899915520,
-               "gather_quintic": 6046056192, "scatter_quintic": 5924986624}
-
-# What bounds those kernels, from the ncu captures summarised in profiles/ (not measured in
-# this run): the scatters run on the integer pipes, the gathers on the FP64 pipe.
-_SCATTER_LIMITER = {"pipe": "integer issue (signed 64-bit high products, shared 32-bit atomics)",
-                    "issue_active_pct": 70.1, "fma_heavy_pct": 56.4, "alu_pct": 53.1, "dram_pct": 2.6,
-                    "source": "ncu --set full, 256^3 x 3, 4e6 clustered points, quintic "
-                              "(profiles/fp64_scatter_k_scatter_fixed64_256cube_c3_4e6_quintic.md)"}
-NCU_LIMITER = {"scatter_cubic": _SCATTER_LIMITER, "scatter_quintic": _SCATTER_LIMITER,
-               "gather_cubic": {"pipe": "FP64 (the quintic gather's capture)",
-                                "source": "profiles/fp64_gather_k_gather_plain_256cube_c3_4e6_quintic.md"},
-               "gather_quintic": {"pipe": "FP64", "fp64_pipe_pct": 94.4,
-                                  "source": "profiles/fp64_gather_k_gather_plain_256cube_c3_4e6_quintic.md"}}
-
-
-def fp64_peak_tflops() -> float:
-    """FP64 throughput of this GPU, measured: the best of a few cuBLAS DGEMMs."""
-    import torch
-    n = 8192
-    a = torch.randn((n, n), dtype=torch.float64, device="cuda")
-    b = torch.randn((n, n), dtype=torch.float64, device="cuda")
-    torch.mm(a, b)
-    torch.cuda.synchronize()
-    best = 0.0
-    for _ in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.mm(a, b)
-        e1.record()
-        torch.cuda.synchronize()
-        best = max(best, 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12)
-    del a, b
-    return best
-
-
 def algorithmic_bytes(m: int, ncomp: int, n: int, s: int, beta_nonzero=False) -> dict:
-    """Compulsory traffic per call: every input read once, every output written once."""
-    gather = m * (3 * s + ncomp * s) + n * ncomp * s
-    scatter = m * (3 * s + ncomp * s) + (2 if beta_nonzero else 1) * n * ncomp * s
+    """Compulsory traffic per call: every input read once, every output written once;
+    positions are FP64 (24 B per point), values and quantities s bytes each."""
+    gather = m * (24 + ncomp * s) + n * ncomp * s
+    scatter = m * (24 + ncomp * s) + (2 if beta_nonzero else 1) * n * ncomp * s
     return {"gather": gather, "scatter": scatter}
+
+
+def c3_points_host():
+    """The 3.2e7 uniform FP64 positions, (M, 3) column-major, in generation order."""
+    from __graft_entry__ import load_package
+    load_package()
+    from gbgperiodicfields_gb300.workloads import uniform_points
+    return uniform_points(M3, seed=4)
+
+
+def c3_quantities_host(rows=None):
+    """The scatter's N(0,1) quantities, (M, 12) Float32 in generation order (row blocks of
+    one seeded stream, so a block of rows can be made without the rest)."""
+    out = np.empty((M3, C3), dtype=np.float32, order="F") if rows is None else None
+    blk = 1_000_000
+    lo, hi = (0, M3) if rows is None else rows
+    parts = []
+    for b in range(lo // blk, (hi + blk - 1) // blk):
+        g = np.random.Generator(np.random.PCG64([5, b]))
+        v = g.standard_normal((blk, C3), dtype=np.float32)
+        a, z = max(lo, b * blk), min(hi, (b + 1) * blk)
+        if out is not None:
+            out[a:z] = v[a - b * blk:z - b * blk]
+        else:
+            parts.append(v[a - b * blk:z - b * blk])
+    return out if out is not None else np.asfortranarray(np.concatenate(parts, axis=0))
 
 
 # -------------------------------------------------------------- GB300 arm
 
+def _events(n):
+    import torch
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
+
+
 def run_gb300(args, rank, world):
-    import ctypes
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
+    from gbgperiodicfields_gb300 import autotune, resident
     from gbgperiodicfields_gb300.workloads import spectral_field
 
     local = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     lib = gbg._lib.load()
-    grid = gbg.Grid3D(N_GRID, (2 * np.pi,) * 3)
-    gC = grid.c()
-    cubic, quintic = gbg.CatmullRom, gbg.LalescuSpline(6)
-    schemes = [cubic, quintic]
+    grid = gbg.Grid3D(N3, (2 * np.pi,) * 3)
+    scheme = gbg.CatmullRom
+    peak, peak_kind = peaks()
 
-    pos_h, q_h = make_inputs_host()
-    field = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device=dev)
-    pos = torch.from_numpy(pos_h).to(dev)
-    q = torch.from_numpy(q_h).to(dev)
-    out = gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev)
-    dep = gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev)
-    order = torch.empty(M_POINTS, dtype=torch.int32, device=dev)
+    # inputs: the FP64 field (kept for the FP64 comparison and the oracle), its FP32
+    # resident copy, the points in binned order and their quantities
+    f64 = spectral_field(N3, 3, kmax=KMAX3, seed=3, project=True, gradient=True, device=dev, dtype=torch.float64)
+    field = resident.ResidentField(grid, C3, max_stencil_width=4).load(f64)
+    pos_gen = torch.from_numpy(c3_points_host()).to(dev)
+    bins = resident.PointBins(grid, M3).build(pos_gen)
+    perm = bins.order().long() - 1
+    pos = gbg.colmajor(pos_gen[perm])
+    q_gen = torch.from_numpy(c3_quantities_host()).to(dev)
+    q32 = gbg.colmajor(q_gen[perm])
+    del q_gen
+    perm_h = perm.cpu().numpy()  # binned slot -> generation index
+    del perm, pos_gen
+    torch.cuda.empty_cache()
+    # bin brick and threads per CTA from the autotuner, timed on these points
+    tuned = autotune.tune(grid, C3, scheme, pos, bricks=((11, 8, 8), (7, 8, 8), (15, 8, 8)), reps=1, persist=False)
+    bins = autotune.apply(resident.PointBins(grid, M3, brick=tuned["brick"]).build(pos), tuned)
+    out = gbg.empty_colmajor((M3, C3), torch.float32, dev)
+    dest = resident.ResidentField(grid, C3, max_stencil_width=4)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
-
-    nb = ctypes.c_size_t()
-    gbg._lib.check(lib.gbg_point_traversal_order_workspace_size(gC, M_POINTS, 4, ctypes.byref(nb)))
-    ws_order = torch.empty(nb.value, dtype=torch.uint8, device=dev)
-    need = 0
-    for s in schemes:
-        gbg._lib.check(lib.gbg_anterpolate_workspace_size(gC, gbg._lib.GBG_F64, NCOMP, M_POINTS, s.c(), ctypes.byref(nb)))
-        need = max(need, nb.value)
-    ws_scatter = torch.empty(need, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream(dev)
-    sh = stream.cuda_stream
 
-    # per-call CUDA events on the launching stream, and per call the main kernel alone
-    # (gbg_set_kernel_timing_events: events recorded by the library around that kernel)
-    timings = {"order": [], "gather_cubic": [], "scatter_cubic": [], "gather_quintic": [], "scatter_quintic": []}
-    kernel_times = {k: [] for k in timings if k != "order"}
+    names = ("bins", "gather", "scatter")
+    calls = {k: [] for k in names}
+    kernels = {"gather": [], "scatter": []}
 
-    def timed(kev, fn):
+    def timed_kernel(kev, fn):
         gbg._lib.check(lib.gbg_set_kernel_timing_events(kev[0].cuda_event, kev[1].cuda_event))
         try:
             fn()
@@ -238,30 +241,22 @@ def run_gb300(args, rank, world):
             lib.gbg_set_kernel_timing_events(None, None)
 
     def step(record):
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
-        kev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for k in kernel_times}
+        ev = _events(4)
+        kev = {k: tuple(_events(2)) for k in kernels}
         for a, b in kev.values():  # the handles exist once recorded
             a.record(stream)
             b.record(stream)
         ev[0].record(stream)
-        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M_POINTS, 4,
-                                                     order.data_ptr(), ws_order.data_ptr(), ws_order.numel(), sh))
+        bins.build(pos, status)
         ev[1].record(stream)
-        k = 2
-        for name, s in (("cubic", cubic), ("quintic", quintic)):
-            timed(kev["gather_" + name], lambda: gbg._lib.check(lib.gbg_interpolate(
-                gC, gbg._lib.GBG_F64, NCOMP, field.data_ptr(), pos.data_ptr(), M_POINTS, order.data_ptr(), s.c(),
-                out.data_ptr(), status.data_ptr(), sh)))
-            ev[k].record(stream)
-            timed(kev["scatter_" + name], lambda: gbg._lib.check(lib.gbg_anterpolate(
-                gC, gbg._lib.GBG_F64, NCOMP, dep.data_ptr(), pos.data_ptr(), M_POINTS, q.data_ptr(), None, s.c(),
-                1.0, 0.0, ws_scatter.data_ptr(), ws_scatter.numel(), status.data_ptr(), sh)))
-            ev[k + 1].record(stream)
-            k += 2
+        timed_kernel(kev["gather"], lambda: resident.interpolate_binned(field, bins, scheme, out=out))
+        ev[2].record(stream)
+        timed_kernel(kev["scatter"], lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
+        ev[3].record(stream)
         if record is not None:
             record.append((ev, kev))
 
-    for _ in range(args.warmup):
+    for _ in range(max(3, args.warmup)):
         step(None)
     torch.cuda.synchronize()
     if world > 1:
@@ -271,7 +266,7 @@ def run_gb300(args, rank, world):
     clocks.start()
     time.sleep(0.3)
     evs = []
-    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start, end = _events(2)
     torch.cuda.synchronize()
     start.record(stream)
     for _ in range(args.steps):
@@ -282,66 +277,66 @@ def run_gb300(args, rank, world):
     launches = lib.gbg_kernel_launches() - launches0
     ms_total = start.elapsed_time(end)
     for ev, kev in evs:
-        names = list(timings)
         for i, nm in enumerate(names):
-            timings[nm].append(ev[i].elapsed_time(ev[i + 1]))
+            calls[nm].append(ev[i].elapsed_time(ev[i + 1]))
         for nm, (a, b) in kev.items():
-            kernel_times[nm].append(a.elapsed_time(b))
+            kernels[nm].append(a.elapsed_time(b))
     if int(status.item()) != 0:
         raise RuntimeError(f"device status {int(status.item())}")
-    if rank == 0 and not args.no_cpu:
-        # the last timed step's quintic outputs, checked against the oracle after the CPU
-        # baseline has run (oracle_check)
-        _LAST_OUTPUTS.update(field=np.asfortranarray(field.cpu().numpy()), gather=np.asfortranarray(out.cpu().numpy()),
-                             scatter=np.asfortranarray(dep.cpu().numpy()))
-
     ms_total = reduce_max(ms_total, world, dev)
-    evals_per_step = 4 * M_POINTS
-    value = world * evals_per_step * args.steps / (ms_total / 1e3)
+    value = world * 2 * M3 * args.steps / (ms_total / 1e3)
 
-    # roofline of the dominant kernel (by its own event-timed duration): algorithmic bytes
-    # per launch against the HBM copy peak, and algorithmic FP64 flops (2 * width^3 * C per
-    # point) against the FP64 peak measured here with a cuBLAS DGEMM
-    avg = {k: float(np.mean(v)) for k, v in timings.items()}
-    kavg = {k: float(np.mean(v)) for k, v in kernel_times.items()}
-    peak, peak_kind = peaks()
-    ab = algorithmic_bytes(M_POINTS, NCOMP, int(np.prod(N_GRID)), 8)
+    avg = {k: float(np.mean(v)) for k, v in calls.items()}
+    kavg = {k: float(np.mean(v)) for k, v in kernels.items()}
+    alg = algorithmic_bytes(M3, C3, int(np.prod(N3)), 4)
+    kname = {"gather": "k_gather_staged4<4, 12, float>", "scatter": "k_scatter_nodes<4, 1, 12>"}
+    per_kernel = {k: {"kernel": kname[k], "ms": kavg[k], "algorithmic_bytes": alg[k],
+                      "achieved": alg[k] / (kavg[k] / 1e3) / 1e9,
+                      "frac": alg[k] / (kavg[k] / 1e3) / 1e9 / peak} for k in kavg}
     dominant = max(kavg, key=kavg.get)
-    dom_bytes = ab["scatter"] if dominant.startswith("scatter") else ab["gather"]
-    achieved = dom_bytes / (kavg[dominant] / 1e3) / 1e9
-    width = 6 if dominant.endswith("quintic") else 4
-    dom_flops = 2 * width ** 3 * NCOMP * M_POINTS
-    fp64_peak = None if args.no_peaks else fp64_peak_tflops()
-    fp64_achieved = dom_flops / (kavg[dominant] / 1e3) / 1e12
-
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_total / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "grid": list(N_GRID), "ncomp": NCOMP, "points": M_POINTS,
-                   "schemes": ["CatmullRom", "LalescuSpline(6)"], "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (field 403 MB)"},
+        "warmup": max(3, args.warmup), "ms_per_step": ms_total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 position split)", "data": "synthetic (seeded)",
+        "config": dict(CONFIG),
         "per_call_ms": avg,
         "kernel_ms": kavg,
-        "roofline": {"bound": "hbm", "kernel": KERNEL_NAMES[dominant], "call": dominant, "achieved": achieved,
-                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": NCU_TRAFFIC.get(dominant), "algorithmic_bytes": dom_bytes,
-                     "fp64": {"achieved": fp64_achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                              "frac": fp64_achieved / fp64_peak if fp64_peak else None,
-                              "algorithmic_flops": dom_flops,
-                              "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"},
-                     "limiter": NCU_LIMITER.get(dominant)},
+        "roofline": {"bound": "hbm", "kernel": kname[dominant], "call": dominant,
+                     "achieved": per_kernel[dominant]["achieved"], "peak": peak, "unit": "GB/s",
+                     "frac": per_kernel[dominant]["frac"], "peak_source": peak_kind,
+                     "traffic": None, "algorithmic_bytes": alg[dominant], "per_kernel": per_kernel,
+                     "note": "achieved = algorithmic bytes / the kernel's CUDA-event time on its stream over the "
+                             "timed steps; DRAM traffic per launch is in the committed ncu summaries"},
+        "tuned": {k: tuned[k] for k in ("brick", "gather_threads", "scatter_threads")},
         "clocks": clk,
         "gpu_launches": int(launches),
     }
 
+    # the points of the oracle checks and of the CPU legs: a uniform stride over the slots
+    check_idx = np.arange(0, M3, M3 // 1_000_000)[:1_000_000]
+    if rank == 0 and not args.no_cpu:
+        idx_t = torch.from_numpy(check_idx).to(dev)
+        _LAST.update(gather_rows=out[idx_t].double().cpu().numpy(), check_idx=check_idx, perm_h=perm_h)
+        # the scatter of the same sample on its own (a deposit of all 3.2e7 points cannot
+        # be restated on the host in bench time)
+        sub_pos = gbg.colmajor(pos[idx_t])
+        sub_q = gbg.colmajor(q32[idx_t])
+        sub_bins = resident.PointBins(grid, len(check_idx)).build(sub_pos)
+        sub_dest = resident.ResidentField(grid, C3, max_stencil_width=4)
+        resident.anterpolate_binned(sub_dest, sub_bins, scheme, sub_q, 1.0, 0.0)
+        _LAST.update(scatter_field=sub_dest.read(torch.float32).cpu().numpy(), f64_host=f64.cpu().numpy())
+        del sub_pos, sub_q, sub_bins, sub_dest, idx_t
+
     if not args.no_e2e:
-        result["e2e"] = e2e_gb300(args, gbg, lib, grid, field, pos_h, q_h, dev, stream)
+        result["e2e"] = e2e_c3(args, gbg, grid, scheme, field, dest, bins, pos, q32, f64, dev, stream)
     if not args.no_forms:
-        del field, pos, q, out, dep, ws_scatter, ws_order
-        torch.cuda.empty_cache()
+        result["fp64_dropin_same_inputs"] = fp64_dropin_same_inputs(gbg, lib, grid, scheme, f64, pos, q32, out, dest,
+                                                                     result["ms_per_step"], dev)
+    del field, dest, bins, out, pos, q32, f64
+    torch.cuda.empty_cache()
+    if not args.no_forms:
         launches1 = lib.gbg_kernel_launches()
-        result["precision_form"] = precision_form(gbg, lib, dev, peak)
+        result["plain_fp64_form"] = plain_fp64_form(args, gbg, lib, dev, peak)
         result["batched_form"] = batched_form(gbg, dev)
         result["served_form"] = served_form(gbg, dev)
         result["nufft_form"] = nufft_form(gbg, lib, dev)
@@ -349,75 +344,72 @@ def run_gb300(args, rank, world):
     return result
 
 
-def e2e_gb300(args, gbg, lib, grid, field_dev, pos_h, q_h, dev, stream):
-    """The same step through the C ABI with host buffers: every step copies the inputs
-    from pinned host memory and reads every result back.  The copies run on their own
-    streams, as a caller of the stream-ordered ABI would run them: the uploads on one, the
-    downloads on another, each transfer waiting only for the inputs it reads, and two sets
-    of device buffers so that a step's uploads overlap the previous step's work.  Every byte
-    still crosses inside the timed region."""
+def e2e_c3(args, gbg, grid, scheme, field, dest, bins, pos_dev, q_dev, f64, dev, stream):
+    """The headline step through the C ABI from host buffers.  Every step uploads the
+    field (FP32, the reference's column-major layout), the positions and the quantities
+    from pinned host memory, imports the field into the resident layout, rebuilds the bins,
+    gathers, scatters, exports the deposit to the reference layout and reads the gathered
+    values and the deposit back.  The copies run on their own streams, as a caller of the
+    stream-ordered ABI would run them (uploads on one, downloads on another, each waiting
+    only for what it moves), with two sets of device buffers so that one step's uploads
+    overlap the previous step's work; every byte still crosses inside the timed region."""
     import torch
-    gC = grid.c()
+    from gbgperiodicfields_gb300 import resident
     cs = stream
-    sh = cs.cuda_stream
     up = torch.cuda.Stream(device=dev)
     down = torch.cuda.Stream(device=dev)
-    f_h = field_dev.cpu().pin_memory()  # column-major (Nx,Ny,Nz,3) host copy
-    pos_p = torch.from_numpy(pos_h).pin_memory()
-    q_p = torch.from_numpy(q_h).pin_memory()
-    out_h = [torch.empty((NCOMP, M_POINTS), dtype=torch.float64).pin_memory() for _ in range(2)]
-    dep_h = [torch.empty(f_h.shape[::-1], dtype=torch.float64).pin_memory() for _ in range(2)]
-    schemes = [gbg.CatmullRom, gbg.LalescuSpline(6)]
+    f_h = f64.to(torch.float32).cpu().pin_memory()  # (Nx, Ny, Nz, 12) column-major
+    pos_h = pos_dev.cpu().pin_memory()
+    q_h = q_dev.cpu().pin_memory()
+    out_h = [torch.empty((C3, M3), dtype=torch.float32).pin_memory() for _ in range(2)]
+    dep_h = [torch.empty((C3,) + N3[::-1], dtype=torch.float32).pin_memory() for _ in range(2)]
     sets = []
     for _ in range(2):
-        sets.append({
-            "f": gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev),
-            "pos": gbg.empty_colmajor((M_POINTS, 3), torch.float64, dev),
-            "q": gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev),
-            "order": torch.empty(M_POINTS, dtype=torch.int32, device=dev),
-            "out": [gbg.empty_colmajor((M_POINTS, NCOMP), torch.float64, dev) for _ in range(2)],
-            "dep": [gbg.empty_colmajor(N_GRID + (NCOMP,), torch.float64, dev) for _ in range(2)],
-            "free": torch.cuda.Event(),
-        })
+        sets.append({"f": gbg.empty_colmajor(N3 + (C3,), torch.float32, dev),
+                     "pos": gbg.empty_colmajor((M3, 3), torch.float64, dev),
+                     "q": gbg.empty_colmajor((M3, C3), torch.float32, dev),
+                     "out": gbg.empty_colmajor((M3, C3), torch.float32, dev),
+                     "dep": gbg.empty_colmajor(N3 + (C3,), torch.float32, dev),
+                     "free": torch.cuda.Event()})
         sets[-1]["free"].record(cs)
+    lib = gbg._lib.load()
 
     def step(k):
         S = sets[k & 1]
         ev = {name: torch.cuda.Event() for name in ("pos", "f", "q")}
-        up.wait_event(S["free"])  # this set's previous step is done (its results are read back)
+        up.wait_event(S["free"])  # this set's previous step has been read back
         with torch.cuda.stream(up):
-            S["pos"].copy_(pos_p, non_blocking=True)
+            S["pos"].copy_(pos_h, non_blocking=True)
             ev["pos"].record(up)
             S["f"].copy_(f_h, non_blocking=True)
             ev["f"].record(up)
-            S["q"].copy_(q_p, non_blocking=True)
+            S["q"].copy_(q_h, non_blocking=True)
             ev["q"].record(up)
         cs.wait_event(ev["pos"])
-        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, S["pos"].data_ptr(), M_POINTS, 4,
-                                                     S["order"].data_ptr(), None, 0, sh))
+        bins.build(S["pos"])
         cs.wait_event(ev["f"])
+        field.load(S["f"])
+        resident.interpolate_binned(field, bins, scheme, out=S["out"])
+        g_done = torch.cuda.Event()
+        g_done.record(cs)
         cs.wait_event(ev["q"])
-        for i, s in enumerate(schemes):
-            gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, NCOMP, S["f"].data_ptr(), S["pos"].data_ptr(),
-                                               M_POINTS, S["order"].data_ptr(), s.c(), S["out"][i].data_ptr(), None, sh))
-            g_done = torch.cuda.Event()
-            g_done.record(cs)
-            gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, NCOMP, S["dep"][i].data_ptr(), S["pos"].data_ptr(),
-                                               M_POINTS, S["q"].data_ptr(), None, s.c(), 1.0, 0.0, None, 0, None, sh))
-            s_done = torch.cuda.Event()
-            s_done.record(cs)
-            down.wait_event(g_done)
-            with torch.cuda.stream(down):
-                out_h[i].copy_(S["out"][i].T, non_blocking=True)
-            down.wait_event(s_done)
-            with torch.cuda.stream(down):
-                dep_h[i].copy_(S["dep"][i].permute(3, 2, 1, 0), non_blocking=True)
+        resident.anterpolate_binned(dest, bins, scheme, S["q"], 1.0, 0.0)
+        gbg._lib.check(lib.gbg_field_export(dest.handle, gbg._lib.GBG_F32, S["dep"].data_ptr(), cs.cuda_stream))
+        s_done = torch.cuda.Event()
+        s_done.record(cs)
+        down.wait_event(g_done)
+        with torch.cuda.stream(down):
+            out_h[k & 1].copy_(S["out"].T, non_blocking=True)
+        down.wait_event(s_done)
+        with torch.cuda.stream(down):
+            dep_h[k & 1].copy_(S["dep"].permute(3, 2, 1, 0), non_blocking=True)
         S["free"].record(down)
 
     step(0)
+    step(1)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    n = max(2, args.steps // 2)
+    e0, e1 = _events(2)
+    n = max(3, args.steps // 2)
     e0.record(cs)
     up.wait_stream(cs)
     for k in range(n):
@@ -427,14 +419,46 @@ def e2e_gb300(args, gbg, lib, grid, field_dev, pos_h, q_h, dev, stream):
     e1.record(cs)
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / n
-    h2d = f_h.numel() * 8 + pos_p.numel() * 8 + q_p.numel() * 8
-    d2h = sum(t.numel() * 8 for t in out_h) + sum(t.numel() * 8 for t in dep_h)
-    return {"value": 4 * M_POINTS / (ms / 1e3), "unit": UNIT, "ms_per_step": ms,
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "overlap": "uploads and downloads on their own streams, two buffer sets"}
+    h2d = f_h.numel() * 4 + pos_h.numel() * 8 + q_h.numel() * 4
+    d2h = out_h[0].numel() * 4 + dep_h[0].numel() * 4
+    res = {"value": 2 * M3 / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": n,
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+           "overlap": "uploads and downloads on their own streams, two device buffer sets"}
+    del sets, f_h, pos_h, q_h, out_h, dep_h
+    torch.cuda.empty_cache()
+    return res
 
 
-# ------------------------------------------------- precision / batched / served forms
+def fp64_dropin_same_inputs(gbg, lib, grid, scheme, f64, pos, q32, out32, dest, precision_ms, dev):
+    """The FP64 drop-in (gbg_point_traversal_order + gbg_interpolate + gbg_anterpolate on
+    the reference's layouts, itself pinned to the oracle at 1e-13) on the headline's inputs:
+    its step time beside the precision form's, and the precision form's error against it
+    over every point and every node (max and RMS, relative to max|FP64| and RMS(FP64))."""
+    import torch
+    gC = grid.c()
+    sh = torch.cuda.current_stream().cuda_stream
+    q64 = gbg.colmajor(q32.double())
+    out64 = gbg.empty_colmajor((M3, C3), torch.float64, dev)
+    dep64 = gbg.empty_colmajor(N3 + (C3,), torch.float64, dev)
+    order = torch.empty(M3, dtype=torch.int32, device=dev)
+
+    def plain_step():
+        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M3, 4, order.data_ptr(),
+                                                     None, 0, sh))
+        gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, C3, f64.data_ptr(), pos.data_ptr(), M3,
+                                           order.data_ptr(), scheme.c(), out64.data_ptr(), None, sh))
+        gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, C3, dep64.data_ptr(), pos.data_ptr(), M3,
+                                           q64.data_ptr(), None, scheme.c(), 1.0, 0.0, None, 0, None, sh))
+    t_plain = _time_ms(plain_step, reps=2)
+    res = {"ms_per_step": t_plain, "precision_ms_per_step": precision_ms,
+           "speedup_of_precision_form": t_plain / precision_ms,
+           "precision_error_vs_fp64": {"gather": _rel_errors(out32, out64), "scatter": _rel_errors(dest.read(), dep64)}}
+    del q64, out64, dep64, order
+    torch.cuda.empty_cache()
+    return res
+
+
+# ------------------------------------------------- secondary workloads
 
 def _time_ms(fn, reps=3):
     """Minimum over reps of CUDA-event time (warm-up call first)."""
@@ -443,7 +467,7 @@ def _time_ms(fn, reps=3):
     torch.cuda.synchronize()
     best = float("inf")
     for _ in range(reps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a, b = _events(2)
         a.record()
         fn()
         b.record()
@@ -458,7 +482,7 @@ def _kernel_ms(lib, fn, reps=3):
     import torch
     best = float("inf")
     for _ in range(reps):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a, b = _events(2)
         a.record()
         b.record()
         lib.gbg_set_kernel_timing_events(a.cuda_event, b.cuda_event)
@@ -473,92 +497,98 @@ def _kernel_ms(lib, fn, reps=3):
 
 def _rel_errors(got, want):
     """max and RMS of |got - want|, relative to max|want| and RMS(want)."""
-    import torch
     d = (got.double() - want.double())
     w = want.double()
     return {"max_rel": float(d.abs().max() / w.abs().max().clamp_min(1e-300)),
             "rms_rel": float(d.square().mean().sqrt() / w.square().mean().sqrt().clamp_min(1e-300))}
 
 
-def precision_form(gbg, lib, dev, peak):
-    """512^3 field of 3 + 9 components (velocity and its gradient tensor, stored as one
-    12-component resident FP32 field), 3.2e7 uniform points, cubic gather and scatter
-    through the resident form; errors against the FP64 drop-in path (itself pinned to the
-    oracle at <= 1e-13) and the speed-up over that FP64 path on the same inputs."""
+def plain_fp64_form(args, gbg, lib, dev, peak):
+    """The plain-FP64-at-scale workload through the drop-in C ABI: 256^3 x 3 FP64 velocity
+    field (|k| <= 64, divergence-free), 1e7 points (70% uniform + 30% in 1000 Gaussian
+    blobs, sigma 0.05); per step the traversal order, then cubic and quintic gather and
+    scatter (4 evaluations per point).  The last step's four outputs are kept for the
+    oracle check over all 1e7 points."""
     import torch
-    from gbgperiodicfields_gb300 import resident
-    from gbgperiodicfields_gb300.workloads import spectral_field, uniform_points
-    n, C, M = (512, 512, 512), 12, 32_000_000
-    grid = gbg.Grid3D(n, (2 * np.pi,) * 3)
-    f64 = spectral_field(n, 3, kmax=64, seed=3, project=True, gradient=True, device=dev, dtype=torch.float64)
-    field = resident.ResidentField(grid, C, max_stencil_width=4).load(f64)
-    pos_r = torch.from_numpy(uniform_points(M, seed=4)).to(dev)
-    q64_r = gbg.colmajor(torch.randn((M, C), dtype=torch.float64, device=dev))
-    bins = resident.PointBins(grid, M)
-    out = gbg.empty_colmajor((M, C), torch.float32, dev)
-    dest = resident.ResidentField(grid, C, max_stencil_width=4)
-    scheme = gbg.CatmullRom
-    # points in arrival (random) order: every gathered value lands at a random row
-    q32_r = gbg.colmajor(q64_r.float())
-    random_order = {"bins": _time_ms(lambda: bins.build(pos_r)),
-                    "gather": _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out)),
-                    "scatter": _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32_r, 1.0, 0.0))}
-    # the particle state kept in binned order on the device (re-sorted once, as a
-    # particle code does when it moves its points), the configuration reported
-    perm = bins.order().long() - 1
-    pos = gbg.colmajor(pos_r[perm])
-    q64 = gbg.colmajor(q64_r[perm])
-    q32 = gbg.colmajor(q64.float())
-    del pos_r, q64_r, q32_r, perm
-    # the autotuner picks the bin brick and the threads per CTA for this problem
-    from gbgperiodicfields_gb300 import autotune
-    tuned = autotune.tune(grid, C, scheme, pos, bricks=((11, 8, 8), (7, 8, 8), (15, 8, 8)), reps=1, persist=False)
-    bins = autotune.apply(resident.PointBins(grid, M, brick=tuned["brick"]).build(pos), tuned)
-    t_bins = _time_ms(lambda: bins.build(pos))
-    t_gather = _time_ms(lambda: resident.interpolate_binned(field, bins, scheme, out=out))
-    t_scatter = _time_ms(lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
-    k_gather = _kernel_ms(lib, lambda: resident.interpolate_binned(field, bins, scheme, out=out))
-    k_scatter = _kernel_ms(lib, lambda: resident.anterpolate_binned(dest, bins, scheme, q32, 1.0, 0.0))
-    # the FP64 drop-in on the same inputs: reference values and the speed comparison
+    from gbgperiodicfields_gb300.workloads import clustered_points, spectral_field
+    grid = gbg.Grid3D(N2G, (2 * np.pi,) * 3)
     gC = grid.c()
+    schemes = {"cubic": gbg.CatmullRom, "quintic": gbg.LalescuSpline(6)}
+    pos_h = clustered_points(M2, seed=2)
+    q_h = np.asfortranarray(np.random.Generator(np.random.PCG64(3)).standard_normal((M2, NCOMP2)))
+    field = spectral_field(N2G, NCOMP2, kmax=KMAX2, seed=1, project=True, device=dev)
+    pos = torch.from_numpy(pos_h).to(dev)
+    q = torch.from_numpy(q_h).to(dev)
+    outs = {k: gbg.empty_colmajor((M2, NCOMP2), torch.float64, dev) for k in schemes}
+    deps = {k: gbg.empty_colmajor(N2G + (NCOMP2,), torch.float64, dev) for k in schemes}
+    order = torch.empty(M2, dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
     sh = torch.cuda.current_stream().cuda_stream
-    out64 = gbg.empty_colmajor((M, C), torch.float64, dev)
-    dep64 = gbg.empty_colmajor(n + (C,), torch.float64, dev)
-    order = torch.empty(M, dtype=torch.int32, device=dev)
+    timings = {"order": [], **{f"{c}_{k}": [] for k in schemes for c in ("gather", "scatter")}}
+    kernel = {f"{c}_{k}": [] for k in schemes for c in ("gather", "scatter")}
 
-    def plain_step():
-        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M, 4, order.data_ptr(),
-                                                     None, 0, sh))
-        gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, C, f64.data_ptr(), pos.data_ptr(), M,
-                                           order.data_ptr(), scheme.c(), out64.data_ptr(), None, sh))
-        gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, C, dep64.data_ptr(), pos.data_ptr(), M,
-                                           q64.data_ptr(), None, scheme.c(), 1.0, 0.0, None, 0, None, sh))
-    t_plain = _time_ms(plain_step, reps=1)
-    err_g = _rel_errors(out, out64)
-    err_s = _rel_errors(dest.read(), dep64)
-    alg = algorithmic_bytes(M, C, int(np.prod(n)), 4)
-    step = t_bins + t_gather + t_scatter
-    res = {
-        "workload": "512^3 x (3+9) FP32 resident field (velocity + gradient, |k|<=64), 3.2e7 uniform points "
-                    "kept in binned order, cubic gather + scatter, bins rebuilt per step",
-        "value": 2 * M / (step / 1e3), "unit": UNIT,
-        "per_call_ms": {"bins": t_bins, "gather": t_gather, "scatter": t_scatter},
-        "kernel_ms": {"gather": k_gather, "scatter": k_scatter},
-        "tuned": {k: tuned[k] for k in ("brick", "gather_threads", "scatter_threads")},
-        "random_order_ms": random_order,
-        "roofline": {
-            "gather": {"bound": "hbm", "kernel": "k_gather_staged4<4, 12, float>",
-                       "achieved": alg["gather"] / (k_gather / 1e3) / 1e9, "peak": peak,
-                       "unit": "GB/s", "frac": alg["gather"] / (k_gather / 1e3) / 1e9 / peak,
-                       "algorithmic_bytes": alg["gather"]},
-            "scatter": {"bound": "hbm", "kernel": "k_scatter_nodes<4, 1, 12>",
-                        "achieved": alg["scatter"] / (k_scatter / 1e3) / 1e9, "peak": peak,
-                        "unit": "GB/s", "frac": alg["scatter"] / (k_scatter / 1e3) / 1e9 / peak,
-                        "algorithmic_bytes": alg["scatter"]}},
-        "error_vs_fp64": {"gather": err_g, "scatter": err_s},
-        "plain_fp64_ms": t_plain, "speedup_vs_plain_fp64": t_plain / step,
-    }
-    del f64, field, dest, out64, dep64, q64, q32, pos, bins, out
+    def step():
+        ev = _events(6)
+        ev[0].record()
+        gbg._lib.check(lib.gbg_point_traversal_order(gC, gbg._lib.GBG_F64, pos.data_ptr(), M2, 4,
+                                                     order.data_ptr(), None, 0, sh))
+        ev[1].record()
+        i = 1
+        for k, s in schemes.items():
+            for c in ("gather", "scatter"):
+                a, b = _events(2)
+                a.record()
+                b.record()
+                lib.gbg_set_kernel_timing_events(a.cuda_event, b.cuda_event)
+                try:
+                    if c == "gather":
+                        gbg._lib.check(lib.gbg_interpolate(gC, gbg._lib.GBG_F64, NCOMP2, field.data_ptr(),
+                                                           pos.data_ptr(), M2, order.data_ptr(), s.c(),
+                                                           outs[k].data_ptr(), status.data_ptr(), sh))
+                    else:
+                        gbg._lib.check(lib.gbg_anterpolate(gC, gbg._lib.GBG_F64, NCOMP2, deps[k].data_ptr(),
+                                                           pos.data_ptr(), M2, q.data_ptr(), None, s.c(), 1.0, 0.0,
+                                                           None, 0, status.data_ptr(), sh))
+                finally:
+                    lib.gbg_set_kernel_timing_events(None, None)
+                i += 1
+                ev[i].record()
+                kernel[f"{c}_{k}"].append((a, b))
+        return ev
+
+    step()
+    torch.cuda.synchronize()
+    for v in kernel.values():
+        v.clear()
+    e0, e1 = _events(2)
+    steps = max(3, min(args.steps, 10))
+    evs = []
+    e0.record()
+    for _ in range(steps):
+        evs.append(step())
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    names = list(timings)
+    for ev in evs:
+        for i, nm in enumerate(names):
+            timings[nm].append(ev[i].elapsed_time(ev[i + 1]))
+    kms = {k: float(np.mean([a.elapsed_time(b) for a, b in v])) for k, v in kernel.items()}
+    if int(status.item()) != 0:
+        raise RuntimeError(f"device status {int(status.item())}")
+    alg = algorithmic_bytes(M2, NCOMP2, int(np.prod(N2G)), 8)
+    res = {"workload": "256^3 Float64 3-component velocity field (|k|<=64, |k|^-11/6, divergence-free), 1e7 points "
+                       "(70% uniform + 30% in 1000 Gaussian blobs, sigma=0.05), traversal order + cubic and quintic "
+                       "gather and scatter per step",
+           "value": 4 * M2 / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": steps,
+           "per_call_ms": {k: float(np.mean(v)) for k, v in timings.items()}, "kernel_ms": kms,
+           "hbm_frac": {k: (alg["gather"] if k.startswith("gather") else alg["scatter"]) / (v / 1e3) / 1e9 / peak
+                        for k, v in kms.items()},
+           "fp64_flops_frac_note": "the FP64 kernels are bound by the FP64 pipe (GB300 FP64 is 1/58 of FP32)"}
+    _LAST.update(c2_field=np.asfortranarray(field.cpu().numpy()), c2_pos=pos_h, c2_q=q_h,
+                 c2_out={k: np.asfortranarray(v.cpu().numpy()) for k, v in outs.items()},
+                 c2_dep={k: np.asfortranarray(v.cpu().numpy()) for k, v in deps.items()})
+    del field, pos, q, outs, deps, order
     torch.cuda.empty_cache()
     return res
 
@@ -621,10 +651,9 @@ def nufft_form(gbg, lib, dev, n=128, M=2_000_000, samples=32):
 
 def batched_form(gbg, dev):
     """64 instances of uneven sizes (grids 32^3..256^3, 1/3/9 components, 1e3..1e6
-    points log-uniform, cubic or quintic) as one batch (instances below 1024 points in one
-    persistent gather launch and one persistent scatter launch, the others through the
-    single-instance kernels), the whole step (bins builds + batch) replayed from a CUDA
-    graph; beside it the same work launched instance by instance."""
+    points log-uniform, cubic or quintic) as one batch, the whole step (bins builds +
+    batch) replayed from a CUDA graph; beside it the same work launched instance by
+    instance."""
     import torch
     from gbgperiodicfields_gb300 import autotune, resident
     rng = np.random.default_rng(7)
@@ -660,6 +689,7 @@ def batched_form(gbg, dev):
             resident.anterpolate_binned(i["dest"], i["bins"], i["scheme"], i["q"])
 
     t_seq = _time_ms(seq)
+    t_bins = _time_ms(lambda: [i["bins"].build(i["pos"]) for i in insts])
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -671,10 +701,9 @@ def batched_form(gbg, dev):
         step()
     t_graph = _time_ms(lambda: graph.replay())
     res = {"workload": "64 instances: grids {32,64,128,256}^3, C in {1,3,9}, M log-uniform 1e3..1e6, "
-                       "cubic/quintic, FP32 resident, bricks from the autotuner; bins + the batch (persistent "
-                       "launches below 1024 points, single-instance kernels above), CUDA graph",
+                       "cubic/quintic, FP32 resident, bricks from the autotuner; bins + the batch, CUDA graph",
            "points": int(total), "value": 2 * total / (t_graph / 1e3), "unit": UNIT,
-           "ms_per_step": t_graph, "sequential_ms": t_seq}
+           "ms_per_step": t_graph, "sequential_ms": t_seq, "bins_builds_ms": t_bins}
     del insts, batch, graph
     torch.cuda.empty_cache()
     return res
@@ -770,105 +799,170 @@ def reduce_max(value: float, world: int, device) -> float:
     return float(t.item())
 
 
-# ----------------------------------------------------------- CPU baseline
+# ----------------------------------------------------------- CPU legs
 
-_LAST_OUTPUTS: dict = {}
+_LAST: dict = {}
 
 
-def oracle_check(pos_h, q_h):
-    """The last timed step's quintic gather and scatter (all 1e7 points) against the oracle
-    on the same inputs and the same field, run over all host cores: max and RMS error
-    relative to max|oracle|, beside the Float64 bar the parity tests hold (1e-13)."""
-    if not _LAST_OUTPUTS:
-        return None
+def _oracle():
     sys.path.insert(0, str(ROOT / "oracle"))
     import oracle
-    o = _LAST_OUTPUTS
-    g = oracle.grid_dict(N_GRID)
-    coeffs = oracle.lalescu(6)
-    cores = os.cpu_count() or 1
-    p, qq = np.asfortranarray(pos_h), np.asfortranarray(q_h)
+    return oracle
+
+
+def cpu_transfer_step(oracle, g, field_h, dep_h, pos_h, q_h, lo, hi, coeffs, cores):
+    """The reference's CPU path on points lo..hi-1: its traversal order, the gather of
+    every component at those points, and the atomic scatter of their quantities into the
+    full field (beta = 0, so the field is cleared first, as anterpolate! does).  Returns
+    the wall time."""
+    p = np.asfortranarray(pos_h[lo:hi])
+    qq = np.asfortranarray(q_h[lo:hi].astype(np.float64))
     t0 = time.perf_counter()
-    want_g = oracle.gather(g, o["field"], p, coeffs, nthreads=cores)
-    want_s = oracle.scatter(g, np.zeros(o["field"].shape, order="F"), p, qq, coeffs, 1.0, 0.0, nthreads=cores)
+    trav = oracle.traversal_order(g, p)
+    oracle.gather(g, field_h, p, coeffs, traversal=trav, nthreads=cores)
+    oracle.scatter(g, dep_h, p, qq, coeffs, 1.0, 0.0, traversal=trav, nthreads=cores)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(field_h, block: int, reps: int = 3):
+    """The reference's CPU path (the oracle's OpenMP restatement, all host cores) on the
+    headline workload: blocks of `block` of the 3.2e7 points against the full 512^3 x 12
+    FP64 field, timed per block (the best of `reps`)."""
+    oracle = _oracle()
+    g = oracle.grid_dict(N3)
+    coeffs = oracle.lalescu(4)
+    cores = os.cpu_count() or 1
+    pos_h = c3_points_host()
+    dep_h = np.empty(field_h.shape, order="F")
+    best = float("inf")
+    for r in range(reps):
+        lo = r * block
+        q_h = c3_quantities_host((lo, lo + block))
+        best = min(best, cpu_transfer_step(oracle, g, field_h, dep_h, pos_h[lo:lo + block], q_h, 0, block,
+                                           coeffs, cores))
+    return {"value": 2 * block / best, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{block} of the {M3} points per timed block (traversal order, gather of 12 components, "
+                      f"atomic scatter into the full 512^3 x 12 FP64 field with beta=0), best of {reps}: {best:.2f} s"}
+
+
+def oracle_checks():
+    """The headline's gather (last timed step) at 1e6 points spread over the slots, and the
+    precision-form scatter of those points on their own, against the FP64 oracle on the
+    full FP64 field; the plain-FP64 workload's four outputs over all 1e7 points.  Errors
+    are max and RMS relative to max|oracle|."""
+    if not _LAST:
+        return None
+    oracle = _oracle()
+    cores = os.cpu_count() or 1
+    res = {}
 
     def rel(got, want):
-        d = got.reshape(want.shape, order="F") - want
-        scale = float(np.abs(want).max())
-        return {"max_rel": float(np.abs(d).max() / scale), "rms_rel": float(np.sqrt(np.mean(d * d)) / scale)}
+        # one component (the last axis) at a time, so no full-size temporaries are made
+        got = np.asarray(got).reshape(want.shape, order="F")
+        scale, dmax, dsq = 0.0, 0.0, 0.0
+        for c in range(want.shape[-1]):
+            w = want[..., c]
+            d = got[..., c].astype(np.float64) - w
+            scale = max(scale, float(np.abs(w).max()))
+            dmax = max(dmax, float(np.abs(d).max()))
+            dsq += float(np.sum(d * d))
+        return {"max_rel": dmax / scale, "rms_rel": float(np.sqrt(dsq / want.size)) / scale}
 
-    res = {"gather_quintic": rel(o["gather"], want_g), "scatter_quintic": rel(o["scatter"], want_s), "bar": 1e-13,
-           "points": M_POINTS, "oracle_seconds": round(time.perf_counter() - t0, 1)}
-    _LAST_OUTPUTS.clear()
+    if "gather_rows" in _LAST:
+        t0 = time.perf_counter()
+        g = oracle.grid_dict(N3)
+        c = oracle.lalescu(4)
+        idx = _LAST["check_idx"]
+        gen = _LAST["perm_h"][idx]  # generation indices of the checked slots
+        pos_h = c3_points_host()
+        p = np.asfortranarray(pos_h[gen])
+        del pos_h
+        f = _LAST.pop("f64_host")
+        want_g = oracle.gather(g, f, p, c, nthreads=cores)
+        qall = np.empty((len(gen), C3), dtype=np.float32)
+        order = np.argsort(gen)
+        blk = 1_000_000
+        for b in np.unique(gen // blk):
+            sel = order[(gen[order] // blk) == b]
+            rows = c3_quantities_host((int(b) * blk, int(b) * blk + blk))
+            qall[sel] = rows[gen[sel] - int(b) * blk]
+        want_s = oracle.scatter(g, np.empty(f.shape, order="F"), p, np.asfortranarray(qall.astype(np.float64)), c,
+                                1.0, 0.0, nthreads=cores)
+        del f
+        res["precision_form"] = {"points": int(len(idx)), "bar": 1e-5,
+                                 "gather": rel(_LAST.pop("gather_rows"), want_g),
+                                 "scatter": rel(_LAST.pop("scatter_field"), want_s),
+                                 "oracle_seconds": round(time.perf_counter() - t0, 1)}
+        del want_s
+    if "c2_field" in _LAST:
+        t0 = time.perf_counter()
+        g = oracle.grid_dict(N2G)
+        f, p, qq = _LAST.pop("c2_field"), _LAST.pop("c2_pos"), _LAST.pop("c2_q")
+        outs, deps = _LAST.pop("c2_out"), _LAST.pop("c2_dep")
+        r = {"points": M2, "bar": 1e-13}
+        for name, width in (("cubic", 4), ("quintic", 6)):
+            cf = oracle.lalescu(width)
+            r["gather_" + name] = rel(outs[name], oracle.gather(g, f, p, cf, nthreads=cores))
+            r["scatter_" + name] = rel(deps[name], oracle.scatter(g, np.zeros(f.shape, order="F"), p, qq, cf, 1.0, 0.0,
+                                                                  nthreads=cores))
+        r["oracle_seconds"] = round(time.perf_counter() - t0, 1)
+        res["plain_fp64_form"] = r
+    _LAST.clear()
     return res
 
 
-def cpu_sample_rate(pos_h, q_h, field_h, target_seconds: float):
-    """Times the reference's CPU path (oracle, OpenMP over all host cores) on a bounded
-    sample of the points: the same four transfers per point as a GPU step."""
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import oracle
-    from __graft_entry__ import load_package
-    load_package()
-    g = oracle.grid_dict(N_GRID)
-    cubic, quintic = oracle.lalescu(4), oracle.lalescu(6)
-    cores = os.cpu_count() or 1
-    dep = np.zeros(field_h.shape, order="F")
-
-    def run(m):
-        p = np.asfortranarray(pos_h[:m])
-        qq = np.asfortranarray(q_h[:m])
-        t0 = time.perf_counter()
-        for c in (cubic, quintic):
-            trav = oracle.traversal_order(g, p)
-            oracle.gather(g, field_h, p, c, traversal=trav, nthreads=cores)
-            oracle.scatter(g, dep, p, qq, c, 1.0, 0.0, traversal=trav, nthreads=cores)
-        return time.perf_counter() - t0
-
-    m = 100_000
-    t = run(m)
-    m2 = int(min(M_POINTS, max(m, m * target_seconds / max(t, 1e-3) * 0.8)))
-    t2 = run(m2)
-    return {"value": 4 * m2 / t2, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{m2} of the {M_POINTS} points (all four transfers, traversal order per transfer), "
-                      f"full 256^3x3 field, {t2:.1f} s"}
-
-
 def run_reference(args, rank, world):
+    """The reference arm: the reference's CPU path on the headline workload, on this
+    machine's host cores.  Every step runs the traversal order, the gather and the atomic
+    scatter (into the full FP64 field, cleared first) on the next block of the points; the
+    whole K-step region is timed, and the warm-up steps run first on smaller blocks."""
     if rank != 0:
         return None
     from __graft_entry__ import load_package
     load_package()
     from gbgperiodicfields_gb300.workloads import spectral_field
     import torch
-    torch.set_num_threads(os.cpu_count() or 1)
-    pos_h, q_h = make_inputs_host()
-    field_h = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device="cpu")
-    per_step = max(2.0, args.cpu_seconds / max(1, args.steps))
-    rates = []
-    for _ in range(args.warmup if args.warmup < 1 else 1):
-        cpu_sample_rate(pos_h, q_h, field_h, 1.0)
-    for _ in range(args.steps):
-        rates.append(cpu_sample_rate(pos_h, q_h, field_h, per_step))
-    value = float(np.median([r["value"] for r in rates]))
-    base = rates[-1]
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    oracle = _oracle()
+    g = oracle.grid_dict(N3)
+    coeffs = oracle.lalescu(4)
+    field_h = spectral_field(N3, 3, kmax=KMAX3, seed=3, project=True, gradient=True, device="cpu")
+    pos_h = c3_points_host()
+    dep_h = np.empty(field_h.shape, order="F")
+    block = int(args.cpu_block)
+    wblock = max(1, block // 10)
+    for w in range(args.warmup):
+        lo = (w * wblock) % (M3 - wblock)
+        q_w = c3_quantities_host((lo, lo + wblock))
+        cpu_transfer_step(oracle, g, field_h, dep_h, pos_h[lo:lo + wblock], q_w, 0, wblock, coeffs, cores)
+    qs = [c3_quantities_host(((k * block) % (M3 - block), (k * block) % (M3 - block) + block))
+          for k in range(args.steps)]
+    times = []
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        lo = (k * block) % (M3 - block)
+        times.append(cpu_transfer_step(oracle, g, field_h, dep_h, pos_h[lo:lo + block], qs[k], 0, block, coeffs,
+                                       cores))
+    total = time.perf_counter() - t0
+    value = 2 * block * args.steps / total
+    sample = (f"{block} of the {M3} points per step (the next block each step; traversal order, gather of 12 "
+              f"components, atomic scatter into the full 512^3 x 12 FP64 field with beta=0), {args.steps} steps "
+              f"timed back to back: {total:.1f} s")
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 4 * M_POINTS / value * 1e3, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "grid": list(N_GRID), "ncomp": NCOMP, "points": M_POINTS,
-                       "schemes": ["CatmullRom", "LalescuSpline(6)"], "parallelism": "host threads"},
-            "impl": "reference",
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": base["cores"], "kind": "port",
-                             "sample": base["sample"]},
-            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": dict(CONFIG), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "per_step_s": [round(t, 3) for t in times]}
 
 
 # ------------------------------------------------------- profiling cases
 
 def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), threads=256):
     """256^3 x 12 FP32 resident field (0.85 GB), 4e6 uniform points in binned order,
-    cubic gather and scatter, twice, at the precision form's tuned launch shape (15x8x8
-    bricks, 256 threads for both kernels)."""
+    bins + cubic gather and scatter, twice, at 15x8x8 bricks and 256 threads."""
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
@@ -893,9 +987,8 @@ def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), threads=256):
 
 
 def case_resident_full():
-    """The precision form's step at full size: 512^3 x 12 FP32 resident field, 3.2e7
-    points in binned order, bins + cubic gather + scatter, twice (for a one-pass launch
-    list only)."""
+    """The headline step at full size: 512^3 x 12 FP32 resident field, 3.2e7 points in
+    binned order, bins + cubic gather + scatter, twice (for a one-pass launch list only)."""
     case_resident(n=512, C=12, M=32_000_000)
 
 
@@ -923,9 +1016,9 @@ def case_nufft(n=64, M=500_000):
     torch.cuda.synchronize()
 
 
-def case_plain(n=256, M=4_000_000):
-    """256^3 x 3 FP64 field (403 MB, above L2), 4e6 clustered points, quintic
-    (LalescuSpline(6)) scatter and gather through the drop-in API, twice."""
+def case_plain(n=256, M=4_000_000, width=6):
+    """256^3 x 3 FP64 field (403 MB, above L2), 4e6 clustered points, scatter and gather
+    through the drop-in API (quintic by default), twice."""
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
@@ -936,15 +1029,21 @@ def case_plain(n=256, M=4_000_000):
     q = gbg.VectorPointValues(gbg.colmajor(torch.randn((M, 3), dtype=torch.float64, device=dev)))
     f = gbg.VectorFieldPhysical(gbg.colmajor(torch.randn((n, n, n, 3), dtype=torch.float64, device=dev)), grid)
     order = gbg.point_traversal_order(grid, pts)
-    s = gbg.LalescuSpline(6)
+    s = gbg.LalescuSpline(width) if width != 4 else gbg.CatmullRom
     for _ in range(2):
         gbg.anterpolate_(f, pts, q, s, 1.0, 0.0)
         gbg.interpolate(f, pts, s, traversal=order)
     torch.cuda.synchronize()
 
 
+def case_plain_cubic():
+    """The same as plain_256c3_4e6_quintic with the cubic (CatmullRom) scheme."""
+    case_plain(width=4)
+
+
 PROFILE_CASES = {"resident_256c12_4e6": case_resident, "resident_512c12_3p2e7": case_resident_full,
-                 "plain_256c3_4e6_quintic": case_plain, "nufft_64c3_5e5": case_nufft}
+                 "plain_256c3_4e6_quintic": case_plain, "plain_256c3_4e6_cubic": case_plain_cubic,
+                 "nufft_64c3_5e5": case_nufft}
 
 
 def main():
@@ -967,11 +1066,10 @@ def main():
     else:
         res = run_gb300(args, rank, world)
         if rank == 0 and not args.no_cpu:
-            pos_h, q_h = make_inputs_host()
-            from gbgperiodicfields_gb300.workloads import spectral_field
-            field_h = spectral_field(N_GRID, NCOMP, kmax=KMAX, seed=1, project=True, device="cpu")
-            res["cpu_baseline"] = cpu_sample_rate(pos_h, q_h, field_h, args.cpu_seconds)
-            res["error_vs_oracle"] = oracle_check(pos_h, q_h)
+            f = _LAST.get("f64_host")
+            if f is not None:
+                res["cpu_baseline"] = cpu_baseline(f, min(args.cpu_block, 2_000_000))
+            res["error_vs_oracle"] = oracle_checks()
     if rank == 0 and res is not None:
         print(json.dumps(res), flush=True)
     if world > 1:

@@ -286,9 +286,11 @@ void gbgo_walk(int64_t base, int64_t neighbourhood, int64_t extent, int width, i
     /* Interpolation.jl:1309-1313: beta == 0 overwrites (NaN-safe fill), else data .*= T(beta) */ \
     const int64_t total = npf * ncomp;                                                             \
     if (beta == 0.0) {                                                                             \
+      _Pragma("omp parallel for schedule(static) num_threads(nthreads) if(nthreads > 1)")         \
       for (int64_t i = 0; i < total; ++i) field[i] = (T)0;                                         \
     } else {                                                                                       \
       const T tb = (T)beta;                                                                        \
+      _Pragma("omp parallel for schedule(static) num_threads(nthreads) if(nthreads > 1)")         \
       for (int64_t i = 0; i < total; ++i) field[i] *= tb;                                          \
     }                                                                                              \
     T cT[GBGO_MAX_NODES * GBGO_MAX_POWERS];                                                        \
