@@ -50,13 +50,27 @@ N3 = (512, 512, 512)
 C3 = 12
 M3 = 32_000_000
 KMAX3 = 64
-WORKLOAD = ("512^3 x (3 velocity + 9 velocity-gradient) FP32 resident field (|k|<=64, |k|^-11/6, "
-            "divergence-free), FP64 positions, 3.2e7 uniform points kept in binned order, cubic "
-            "(CatmullRom); per step: bins rebuilt, gather of the 12 components, scatter of 12 "
-            "quantities (beta=0)")
-CONFIG = {"workload": WORKLOAD, "grid": list(N3), "ncomp": C3, "points": M3, "scheme": "CatmullRom",
-          "storage": "f32 field, f64 positions", "evals_per_point_per_step": 2, "parallelism": "replicas",
-          "l2": "inputs larger than L2 (field 6.6 GB), no flush"}
+
+
+def workload_config():
+    """The headline workload's description (the same dict in both arms)."""
+    wl = (f"{N3[0]}^3 x (3 velocity + 9 velocity-gradient) FP32 resident field (|k|<={KMAX3}, |k|^-11/6, "
+          f"divergence-free), FP64 positions, {M3:.1e} uniform points kept in binned order, cubic "
+          "(CatmullRom); per step: bins rebuilt, gather of the 12 components, scatter of 12 quantities (beta=0)")
+    fb = N3[0] * N3[1] * N3[2] * C3 * 4
+    return {"workload": wl, "grid": list(N3), "ncomp": C3, "points": M3, "scheme": "CatmullRom",
+            "storage": "f32 field, f64 positions", "evals_per_point_per_step": 2, "parallelism": "replicas",
+            "l2": f"inputs larger than L2 (field {fb / 1e9:.2f} GB), no flush" if fb > 2 ** 27 else "field within L2"}
+
+
+def shrink_workload(k: int):
+    """Divides the headline grid by k per axis and the points by k^3 (the harness's own CPU
+    tests run the reference arm this way; the line's config records the sizes used)."""
+    global N3, M3, KMAX3
+    if k > 1:
+        N3 = tuple(n // k for n in N3)
+        M3 = M3 // k ** 3
+        KMAX3 = max(2, KMAX3 // k)
 
 # secondary: plain FP64 at scale
 N2G = (256, 256, 256)
@@ -80,6 +94,8 @@ def parse():
                     help="points per step of the CPU port (reference arm and CPU baseline)")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the secondary workloads (FP64 drop-in, plain FP64 at scale, batched, served, NUFFT)")
+    ap.add_argument("--shrink", type=int, default=1,
+                    help="divide the headline grid by K per axis and the points by K^3 (harness tests only)")
     ap.add_argument("--case", choices=sorted(PROFILE_CASES),
                     help="run one small fixed case twice and exit (the inputs of the committed ncu captures)")
     return ap.parse_args()
@@ -171,7 +187,7 @@ def c3_quantities_host(rows=None):
     """The scatter's N(0,1) quantities, (M, 12) Float32 in generation order (row blocks of
     one seeded stream, so a block of rows can be made without the rest)."""
     out = np.empty((M3, C3), dtype=np.float32, order="F") if rows is None else None
-    blk = 1_000_000
+    blk = min(1_000_000, M3)
     lo, hi = (0, M3) if rows is None else rows
     parts = []
     for b in range(lo // blk, (hi + blk - 1) // blk):
@@ -298,7 +314,7 @@ def run_gb300(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": max(3, args.warmup), "ms_per_step": ms_total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 position split)", "data": "synthetic (seeded)",
-        "config": dict(CONFIG),
+        "config": workload_config(),
         "per_call_ms": avg,
         "kernel_ms": kavg,
         "roofline": {"bound": "hbm", "kernel": kname[dominant], "call": dominant,
@@ -313,7 +329,7 @@ def run_gb300(args, rank, world):
     }
 
     # the points of the oracle checks and of the CPU legs: a uniform stride over the slots
-    check_idx = np.arange(0, M3, M3 // 1_000_000)[:1_000_000]
+    check_idx = np.arange(0, M3, max(1, M3 // 1_000_000))[:1_000_000]
     if rank == 0 and not args.no_cpu:
         idx_t = torch.from_numpy(check_idx).to(dev)
         _LAST.update(gather_rows=out[idx_t].double().cpu().numpy(), check_idx=check_idx, perm_h=perm_h)
@@ -930,7 +946,7 @@ def run_reference(args, rank, world):
     field_h = spectral_field(N3, 3, kmax=KMAX3, seed=3, project=True, gradient=True, device="cpu")
     pos_h = c3_points_host()
     dep_h = np.empty(field_h.shape, order="F")
-    block = int(args.cpu_block)
+    block = min(int(args.cpu_block), M3 // 2)
     wblock = max(1, block // 10)
     for w in range(args.warmup):
         lo = (w * wblock) % (M3 - wblock)
@@ -952,7 +968,7 @@ def run_reference(args, rank, world):
     return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": dict(CONFIG), "impl": "reference",
+            "config": workload_config(), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "per_step_s": [round(t, 3) for t in times]}
@@ -1052,6 +1068,7 @@ def main():
         PROFILE_CASES[args.case]()
         print(json.dumps({"case": args.case, "ok": True}))
         return
+    shrink_workload(args.shrink)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if world > 1:
@@ -1068,7 +1085,7 @@ def main():
         if rank == 0 and not args.no_cpu:
             f = _LAST.get("f64_host")
             if f is not None:
-                res["cpu_baseline"] = cpu_baseline(f, min(args.cpu_block, 2_000_000))
+                res["cpu_baseline"] = cpu_baseline(f, min(args.cpu_block, 2_000_000, M3 // 4))
             res["error_vs_oracle"] = oracle_checks()
     if rank == 0 and res is not None:
         print(json.dumps(res), flush=True)

@@ -145,8 +145,8 @@ SIGNATURES = {
     "gbg_bins_permute": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "gbg_bins_build": (_I32, [_P, _I32, _P, _I64, _P, _P]),
     "gbg_bins_order": (_I32, [_P, _P, _P]),
-    "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P]),
-    "gbg_anterpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _D, _D, _P]),
+    "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P, _P]),
+    "gbg_anterpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _D, _D, _P, _P]),
     "gbg_batch_create": (_I32, [ctypes.POINTER(BatchItemC), _I32, ctypes.POINTER(_P)]),
     "gbg_batch_run": (_I32, [_P, _P, _P]),
     "gbg_batch_destroy": (_I32, [_P]),

@@ -244,8 +244,10 @@ struct Scratch {
 
 // Exclusive prefix sum of n uint32 values; tmp must hold scan_temp_elems(n) uint32.
 size_t scan_temp_elems(int64_t n);
+// With gate, every kernel returns at once unless *gate is non-zero (a device-side switch
+// that needs no host synchronization).
 gbg_status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
-                              cudaStream_t stream);
+                              cudaStream_t stream, const uint32_t *gate = nullptr);
 
 // Stable LSD radix sort of (key, value) pairs over the low key_bits bits of the keys.
 // vals_in == nullptr means the identity 0..n-1.  Results land in keys_out / vals_out;
@@ -253,7 +255,17 @@ gbg_status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint
 size_t radix_sort_temp_bytes(int64_t n);
 gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
                             uint32_t *vals_out, int64_t n, int key_bits, void *temp,
-                            cudaStream_t stream);
+                            cudaStream_t stream, const uint32_t *gate = nullptr);
+
+// Stable sort of point indices by key from a counting pass: rank[p] is what an atomic count
+// of keys[p] returned and starts[] the exclusive scan of those counts (starts[k+1] -
+// starts[k] points per key).  perm[s] = the point in slot s, points of one key in index
+// order -- the order the stable radix sort gives.  *big must be zero on entry; a key with
+// more than 1024 points sets it and the radix sort (gated on it) redoes the order, writing
+// skeys too.  temp holds radix_sort_temp_bytes(n) bytes.
+gbg_status stable_counting_sort(const uint32_t *keys, const uint32_t *rank, const uint32_t *starts, int64_t n,
+                                int key_bits, uint32_t *perm, uint32_t *skeys, uint32_t *big, void *temp,
+                                cudaStream_t stream);
 
 // Grid-stride launch shape: a multiple of the SM count.
 int launch_blocks(int64_t work, int threads, int per_sm = 8);

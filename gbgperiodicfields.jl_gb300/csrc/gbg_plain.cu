@@ -6,12 +6,13 @@
 //   gbg_validate_traversal      PointTraversalOrder     Interpolation.jl:560-589
 //
 // The gather is one thread per work item, as in the reference, contracting the x
-// direction first for every component of the chunk.  The scatter is
-// not the reference's atomic push: points are sorted by brick and cell with a stable
-// device radix sort, and each brick's nodes are accumulated in shared memory as int64
-// fixed-point sums (or, for a stencil wider than the grid, every node pulls its
-// contributions).  No float atomics are used, so the scatter is bitwise reproducible and
-// independent of any traversal order.
+// direction first for every component of the chunk.  The scatter is not the reference's
+// atomic push: points are sorted by brick and cell (a stable device counting sort), and each
+// brick's nodes are accumulated in shared memory as 128-bit integer sums on a scale local to
+// the brick (or, for a stencil wider than the grid, every node pulls its contributions).  No
+// float atomics are used, so the scatter is bitwise reproducible and independent of any
+// traversal order, and each node keeps the accuracy of an FP64 sum of its own
+// contributions.
 #include <mutex>
 #include <string>
 
@@ -256,7 +257,7 @@ __global__ void __launch_bounds__(kThreads)
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_cell_keys(GridT<T> g, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
-                uint32_t *__restrict__ counts, int32_t *status) {
+                uint32_t *__restrict__ counts, uint32_t *__restrict__ rank, int32_t *status) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t b[3];
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t key =
         (uint32_t)(imod(b[0], g.nx) + g.nx * (imod(b[1], g.ny) + g.ny * imod(b[2], g.nz)));
     keys[p] = key;
-    atomicAdd(counts + key, 1u);
+    rank[p] = atomicAdd(counts + key, 1u);  // the point's rank within its cell, in no order
   }
 }
 
@@ -357,13 +358,75 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// The same pull for a compile-time width: the cells of a node's x walk are computed once,
+// the x loop is unrolled; the order of every sum is the one above (z, y, x cells, then each
+// cell's points in slot order), so the results are the same bits.
+template <typename T, int N2, int CC>
+__global__ void __launch_bounds__(kThreads)
+    k_scatter_pull_n(GridT<T> g, int ncomp, const uint32_t *__restrict__ cell_start, const T *__restrict__ rec,
+                     const T *__restrict__ qs, T *__restrict__ field, T beta, int beta_zero) {
+  constexpr int nb = (N2 - 2) / 2;
+  const int64_t nxny = g.nx * g.ny;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < g.npf;
+       n += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = n % g.nx;
+    const int64_t yz = n / g.nx;
+    const int64_t y = yz % g.ny;
+    const int64_t z = yz / g.ny;
+    int64_t cxs[N2];
+    {
+      int64_t cx = imod(x + nb, g.nx);
+#pragma unroll
+      for (int i = 0; i < N2; ++i) {
+        cxs[i] = cx;
+        cx = step_down(cx, g.nx);
+      }
+    }
+    const int64_t cy0 = imod(y + nb, g.ny), cz0 = imod(z + nb, g.nz);
+    for (int c0 = 0; c0 < ncomp; c0 += CC) {
+      T acc[CC];
+#pragma unroll
+      for (int c = 0; c < CC; ++c) acc[c] = T(0);
+      int64_t cz = cz0;
+#pragma unroll 1
+      for (int k = 0; k < N2; ++k) {
+        int64_t cy = cy0;
+#pragma unroll 1
+        for (int j = 0; j < N2; ++j) {
+          const int64_t rowoff = g.nx * cy + nxny * cz;
+#pragma unroll
+          for (int i = 0; i < N2; ++i) {
+            const int64_t cell = cxs[i] + rowoff;
+            const uint32_t s0 = __ldg(cell_start + cell), s1 = __ldg(cell_start + cell + 1);
+#pragma unroll 1
+            for (uint32_t sl = s0; sl < s1; ++sl) {
+              const T *r = rec + (int64_t)sl * (3 * N2);
+              const T wv = mul_rn(mul_rn(__ldg(r + N2 + j), __ldg(r + 2 * N2 + k)), __ldg(r + i));
+              const T *qv = qs + (int64_t)sl * ncomp + c0;
+#pragma unroll
+              for (int c = 0; c < CC; ++c) acc[c] = fma_rn(wv, __ldg(qv + c), acc[c]);
+            }
+          }
+          cy = step_down(cy, g.ny);
+        }
+        cz = step_down(cz, g.nz);
+      }
+#pragma unroll
+      for (int c = 0; c < CC; ++c) {
+        T *f = field + n + g.npf * (c0 + c);
+        *f = beta_zero ? acc[c] : add_rn(mul_rn(beta, *f), acc[c]);
+      }
+    }
+  }
+}
+
 // ------------------------------------------------------ brick scatter
 //
 // The default scatter.  Points are sorted by brick and by cell within the brick (a stable
-// radix sort, so the order is fixed).  A CTA owns one brick of nodes and accumulates, in
+// counting sort, so the order is fixed).  A CTA owns one brick of nodes and accumulates, in
 // shared memory, every contribution of the points in the cells whose stencils reach the
-// brick (the extended region) as an integer, so the sum does not depend on the order
-// in which threads add.  Each node is written to HBM once.
+// brick (the extended region) as a 128-bit integer, so the sum does not depend on the
+// order in which threads add.  Each node is written to HBM once.
 
 struct BrickGeo {
   int32_t b[3];
@@ -378,15 +441,29 @@ struct BrickGeo {
   int32_t nseg = 1;
 };
 
-// One pass over the points in their own order: the locate, the brick-major key and the
-// cell count, and max|alpha q|.
+// Binary exponents of the quantities, biased so that 0 means "no non-zero quantity" and
+// kENonFinite (above every finite one) a NaN or an infinity: a non-zero finite v has
+// 2^(e-1) <= |v| < 2^e and is stored as e + kEBias.
+constexpr int kEBias = 2048;
+constexpr int kENonFinite = 4095;
+
+__device__ __forceinline__ int biased_exponent(double v) {
+  if (v == 0.0) return 0;
+  if (!isfinite(v)) return kENonFinite;
+  int e = 0;
+  frexp(v, &e);
+  return e + kEBias;
+}
+
+// One pass over the points in their own order: the locate, the brick-major key, the cell
+// count (the atomic's value is the point's rank in its cell, for the counting sort), and
+// per brick and component the largest exponent of the finite non-zero alpha*q.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
     k_brick_keys(GridT<T> g, BrickGeo bg, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
-                 uint32_t *__restrict__ counts, const T *__restrict__ q, int ncomp, T alpha,
-                 unsigned long long *__restrict__ qmax_bits, int32_t *status) {
+                 uint32_t *__restrict__ counts, uint32_t *__restrict__ rank, const T *__restrict__ q, int ncomp,
+                 T alpha, uint32_t *__restrict__ ebrick, int32_t *status) {
   const int64_t n[3] = {g.nx, g.ny, g.nz};
-  unsigned long long mx = 0ull;  // largest |alpha q| as ordered double bits (NaN above all)
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t b[3];
@@ -402,36 +479,30 @@ __global__ void __launch_bounds__(kThreads)
     }
     const uint32_t key = (uint32_t)(brick * bg.bvol + local);
     keys[p] = key;
-    atomicAdd(counts + key, 1u);
+    rank[p] = atomicAdd(counts + key, 1u);
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);  // quantity = T(alpha)*q
-      const unsigned long long bits = (unsigned long long)__double_as_longlong(fabs((double)v));
-      mx = bits > mx ? bits : mx;
+      const int e = biased_exponent((double)v);
+      if (e == kENonFinite) {
+        if (status) atomicOr(status, GBG_DEV_NONFINITE);
+      } else if (e) {
+        atomicMax(ebrick + brick * ncomp + c, (uint32_t)e);
+      }
     }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long other = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = other > mx ? other : mx;
-  }
-  if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
 // In sorted order, slot by slot: the point's three axes' stencil weights (the reference's
 // Horner with fused multiply-adds, once per point) as 64-bit fixed point w * 2^wexp, and
-// alpha*q as 64-bit fixed point q * 2^(62 - e) with max|alpha q| < 2^e (one scale for all
-// points).  The weights are evaluated here, from the position read through the
-// permutation, rather than in the key pass, so they are written once, already sorted.
+// each alpha*q in floating form of its own: a 64-bit mantissa q * 2^(62 - e) (exact for
+// every double) beside its biased exponent e.  The weights are evaluated here, from the
+// position read through the permutation, rather than in the key pass, so they are written
+// once, already sorted.
 template <typename T, int N2, int M2>
 __global__ void __launch_bounds__(kThreads)
     k_brick_order(GridT<T> g, SchemeT<T, N2> sch, const T *__restrict__ pos, const uint32_t *__restrict__ perm,
                   int64_t m, int wexp, long long *__restrict__ wts, const T *__restrict__ q, int ncomp, T alpha,
-                  const unsigned long long *__restrict__ qmax_bits, long long *__restrict__ qi) {
-  const double qmax = __longlong_as_double((long long)*qmax_bits);
-  int e = 0;
-  frexp(qmax, &e);
-  const bool finite = isfinite(qmax);
-  // w 2^wexp and alpha q 2^(62 - e) rounded once to integers (fixed_rn)
+                  long long *__restrict__ qi, int32_t *__restrict__ qe) {
   for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < m;
        sl += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[sl];
@@ -448,9 +519,62 @@ __global__ void __launch_bounds__(kThreads)
     }
     for (int c = 0; c < ncomp; ++c) {
       const T v = mul_rn(alpha, q[p + m * c]);
-      qi[sl * ncomp + c] = finite ? fixed_rn((double)v, 62 - e) : 0ll;
+      const int e = biased_exponent((double)v);
+      qi[sl * ncomp + c] = (e && e != kENonFinite) ? fixed_rn((double)v, 62 - (e - kEBias)) : 0ll;
+      qe[sl * ncomp + c] = e;
     }
   }
+}
+
+// Adds the 128-bit integer (hi:lo) to the sum kept in shared memory as four 32-bit words
+// w0 (lowest) .. w3, with native 32-bit atomics: each word's add returns the old value,
+// whose wrap is the carry into the next word.  Each add wraps a word at most once, so
+// after all adds the words hold the exact 128-bit sum (mod 2^128) in any order, as the
+// two-word form atomic_add_split64 does for 64 bits.
+__device__ __forceinline__ void atomic_add_split128(uint32_t *w0, uint32_t *w1, uint32_t *w2, uint32_t *w3, int i,
+                                                    unsigned long long lo, unsigned long long hi) {
+  const uint32_t v0 = (uint32_t)lo, v1 = (uint32_t)(lo >> 32), v2 = (uint32_t)hi, v3 = (uint32_t)(hi >> 32);
+  const uint32_t o0 = atomicAdd(w0 + i, v0);
+  const uint32_t c1 = (uint32_t)(o0 + v0 < v0);
+  const uint32_t s1 = v1 + c1;  // wraps only when v1 == 2^32 - 1 and c1 == 1 (then s1 == 0)
+  const uint32_t o1 = atomicAdd(w1 + i, s1);
+  const uint32_t c2 = (uint32_t)(s1 < c1) + (uint32_t)(o1 + s1 < s1);
+  const uint32_t s2 = v2 + c2;
+  const uint32_t o2 = atomicAdd(w2 + i, s2);
+  const uint32_t c3 = (uint32_t)(s2 < c2) + (uint32_t)(o2 + s2 < s2);
+  atomicAdd(w3 + i, v3 + c3);
+}
+
+// One contribution: the node weight wn (64-bit fixed point) times the quantity's mantissa
+// mq (exact signed 64 x 64 -> 128-bit product), shifted right by d with rounding (half up),
+// added to the node's 128-bit sum.  d >= 127 leaves nothing to add.
+__device__ __forceinline__ void add_contribution(uint32_t *a0, uint32_t *a1, uint32_t *a2, uint32_t *a3, int i,
+                                                 long long wn, long long mq, int d) {
+  if (mq == 0 || wn == 0 || d >= 127) return;
+  unsigned long long lo = (unsigned long long)wn * (unsigned long long)mq;
+  long long hi = __mul64hi(wn, mq);
+  if (d > 0) {
+    // + 2^(d-1), then an arithmetic shift right by d
+    if (d <= 64) {
+      const unsigned long long h = 1ull << (d - 1);
+      const unsigned long long s = lo + h;
+      hi += (long long)(s < lo);
+      lo = s;
+    } else {
+      hi += (long long)(1ull << (d - 65));
+    }
+    if (d < 64) {
+      lo = (lo >> d) | ((unsigned long long)hi << (64 - d));
+      hi >>= d;
+    } else if (d == 64) {
+      lo = (unsigned long long)hi;
+      hi = hi < 0 ? -1ll : 0ll;
+    } else {
+      lo = (unsigned long long)(hi >> (d - 64));
+      hi = hi < 0 ? -1ll : 0ll;
+    }
+  }
+  atomic_add_split128(a0, a1, a2, a3, i, lo, (unsigned long long)hi);
 }
 
 template <int N, typename T>
@@ -462,27 +586,30 @@ __device__ __forceinline__ T pick_t(const T (&w)[N], int q) {
   return v;
 }
 
-// The default scatter (deterministic, FP64-grade).  A CTA owns one brick of nodes.  It
-// lists the points of every cell whose stencil reaches the brick (the extended region),
-// gives each warp a point (its lanes cover the point's nodes inside the brick), and adds
-// every contribution w1*w2*w3*alpha*q to an int64 accumulator in shared memory.
+// The default scatter (deterministic, FP64-grade per node).  A CTA owns one brick of
+// nodes.  It lists the points of every cell whose stencil reaches the brick (the extended
+// region), gives each warp a point (its lanes cover the point's nodes inside the brick),
+// and adds every contribution w1*w2*w3*alpha*q to a 128-bit integer accumulator in shared
+// memory.
 //
 // The arithmetic is integer: GB300's FP64 rate is 1/58 of its FP32 rate, while 64-bit
-// integer products run on the integer pipes.  The weights are 64-bit fixed point
-// w * 2^P (P = 62 - lb, |w| <= 2^lb from the scheme's Bernstein bound) and the
-// quantities q * 2^Q (Q = 62 - e, max|alpha q| < 2^e), both converted once per point;
-// each contribution is the high half of three signed 64 x 64-bit products,
-// hi(round(hi(hi(wy, wz), wx) / 2^sh), q) = w1 w2 w3 q * 2^(3P + Q - 192 - sh): the node's
-// weight is shifted right by sh bits (rounded), once for all the components, so that the
-// brick's largest node coverage K_max cannot overflow (with |w 2^P| <= 1.5 * 2^62 and
-// |q 2^Q| < 2^62, |contribution| < 2^(57.76 - sh); sh = max(0, bits(K_max) - 5) keeps a node's
-// sum below 2^62.76).  The last high product floors, so each contribution is low by half a
-// unit on average; the write-back adds that mean back for the node's K contributions (K/2
-// units), which leaves an error within K/2 units, as rounding every contribution would, and
-// unbiased.  Integer addition is associative, so the result
-// does not depend on which thread adds first, and no float atomics are used.  The 64-bit
-// sums are added as two 32-bit words with a carry (atomic_add_split64): native 32-bit
-// shared atomics (with 64-bit shared atomics ncu counted a shared load beside each one).
+// integer products run on the integer pipes.  The weights are 64-bit fixed point w * 2^P
+// (P = 62 - lb, |w| <= 1.5 * 2^lb from the scheme's Bernstein bound), converted once per
+// point; a node's weight is hi(wx, hi(wy, wz)), the high halves of two signed 64 x 64-bit
+// products (w1 w2 w3 * 2^(3P - 128), to 2^-58 of itself).  Each quantity keeps its own
+// binary exponent e_p beside an exact 64-bit mantissa q * 2^(62 - e_p), and every
+// component of the brick's region has a scale: the largest exponent e_r among its points.
+// A contribution is the exact 128-bit product of the node weight and the mantissa, shifted
+// right (rounded) by (e_r - e_p) + sh onto that common scale; sh = max(0, bits(K_max) - 5),
+// K_max the brick's largest node coverage, keeps the sum of a node's contributions below
+// 2^127 (each is below 3.375 * 2^(120 - sh)).  The largest contribution keeps about
+// 120 - sh significant bits and one 2^-k of it keeps 120 - sh - k, so a node's sum has the
+// accuracy of an FP64 sum of its own contributions unless the region spans more than about
+// 2^60 in magnitude: the scale is local to the brick, not global.  Integer addition is
+// associative, so the result does not depend on which thread adds first; the 128-bit sums
+// are added as four 32-bit words with carries (atomic_add_split128).  A non-finite quantity
+// marks every node its stencil reaches, which is written as NaN (the reference's 0 * NaN
+// included).
 constexpr int kFlatChunk = 1024;
 // the scatter's static shared memory: one count per warp for the block scan
 constexpr int kScanSlots = 32;
@@ -491,20 +618,21 @@ constexpr int kQReg = 4;
 
 template <typename T, int N2>
 __global__ void __launch_bounds__(kThreads)
-    k_scatter_fixed64(GridT<T> g, BrickGeo bg, int ncomp,
-                      const uint32_t *__restrict__ cell_start, const long long *__restrict__ wts,
-                      const long long *__restrict__ qi, const unsigned long long *__restrict__ qmax_bits, int wexp,
-                      T *__restrict__ field, T beta, int beta_zero, int32_t *status) {
+    k_scatter_fixed128(GridT<T> g, BrickGeo bg, int ncomp,
+                       const uint32_t *__restrict__ cell_start, const long long *__restrict__ wts,
+                       const long long *__restrict__ qi, const int32_t *__restrict__ qe,
+                       const uint32_t *__restrict__ ebrick, int wexp, T *__restrict__ field, T beta, int beta_zero) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int half = N2 / 2;
   const int E0 = bg.b[0] + N2 - 1, E1 = bg.b[1] + N2 - 1, E2 = bg.b[2] + N2 - 1;
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)bg.bvol;
-  // ncomp * slice 64-bit accumulators, comp-major and pitched, as a plane of low words and
-  // a plane of high words (atomic_add_split64)
-  uint32_t *acc_lo = reinterpret_cast<uint32_t *>(smem_raw);
-  uint32_t *acc_hi = acc_lo + (size_t)bg.slice * ncomp;
-  uint32_t *off = acc_hi + (size_t)bg.slice * ncomp;                         // ecount: exclusive prefix
+  // ncomp * slice 128-bit accumulators, comp-major and pitched, as four planes of 32-bit
+  // words, lowest first (atomic_add_split128)
+  const size_t plane = (size_t)bg.slice * ncomp;
+  uint32_t *acc0 = reinterpret_cast<uint32_t *>(smem_raw);
+  uint32_t *acc1 = acc0 + plane, *acc2 = acc1 + plane, *acc3 = acc2 + plane;
+  uint32_t *off = acc3 + plane;                                              // ecount: exclusive prefix
   // along a row of the region, cells whose keys are consecutive hold consecutive slots, so
   // one base (first slot - prefix) serves each such run of cells (segment)
   uint32_t *segbase = off + ecount;                                          // E1*E2*nseg: slot bases
@@ -514,9 +642,10 @@ __global__ void __launch_bounds__(kThreads)
   uint32_t *kcnt = kz + E2;                                                   // bvol coverage counts + max
   uint32_t *segx = kcnt + bvol + 1;                                          // E0: segment of each x
   uint32_t *segfirst = segx + E0;                                            // nseg: first x of each
+  int32_t *ereg = reinterpret_cast<int32_t *>(segfirst + bg.nseg);           // ncomp: region scales
+  uint32_t *poison = reinterpret_cast<uint32_t *>(ereg + ncomp);             // slice: NaN marks
   __shared__ uint32_t warp_tot[kScanSlots];
   const int lane = (int)threadIdx.x & 31, warp = (int)threadIdx.x >> 5, nwarps = (int)blockDim.x >> 5;
-  const double qmax = __longlong_as_double((long long)*qmax_bits);
   const int64_t nbricks = bg.nb[0] * bg.nb[1] * bg.nb[2];
   const int n[3] = {(int)g.nx, (int)g.ny, (int)g.nz};
   const int nb0 = (int)bg.nb[0], nb1 = (int)bg.nb[1];
@@ -571,8 +700,8 @@ __global__ void __launch_bounds__(kThreads)
     // coverage of every node (points whose stencil reaches it): window sums of the cell
     // counts, over x and y into the accumulators as scratch, then over z
     if (threadIdx.x == 0) kcnt[bvol] = 0u;
-    uint32_t *scratch = acc_lo;
-    if (E2 <= 2 * bg.b[2] * ncomp) {
+    uint32_t *scratch = acc0;
+    if (E2 <= 4 * bg.b[2] * ncomp) {
       for (int o = threadIdx.x; o < B0 * B1 * E2; o += blockDim.x) {
         const int lx = o % B0, r = o / B0, ly = r % B1, ez = r / B1;
         uint32_t sum = 0;
@@ -608,7 +737,19 @@ __global__ void __launch_bounds__(kThreads)
       mx = __reduce_max_sync(0xffffffffu, mx);
       if ((threadIdx.x & 31) == 0) atomicMax(kcnt + bvol, mx);
     }
-    for (int i = threadIdx.x; i < 2 * (int)bg.slice * ncomp; i += blockDim.x) acc_lo[i] = 0u;
+    for (int i = threadIdx.x; i < 4 * (int)plane; i += blockDim.x) acc0[i] = 0u;
+    for (int i = threadIdx.x; i < (int)bg.slice; i += blockDim.x) poison[i] = 0u;
+    // each component's scale: the largest exponent in the 27 bricks around this one (the
+    // region lies within them; periodic wrap)
+    for (int c = threadIdx.x; c < ncomp; c += blockDim.x) {
+      uint32_t e = 0;
+      for (int d = 0; d < 27; ++d) {
+        const int64_t x = (bc[0] + d % 3 - 1 + nb0) % nb0, y = (bc[1] + (d / 3) % 3 - 1 + nb1) % nb1,
+                      z = (bc[2] + d / 9 - 1 + bg.nb[2]) % bg.nb[2];
+        e = max(e, __ldg(ebrick + ((z * nb1 + y) * nb0 + x) * ncomp + c));
+      }
+      ereg[c] = (int32_t)e;
+    }
     __syncthreads();
     const uint32_t kmax = kcnt[bvol];
     const uint32_t count = block_scan_counts(off, ecount, warp_tot);
@@ -621,15 +762,10 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
     __syncthreads();
-    const bool finite = isfinite(qmax);
-    if (!finite && threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_NONFINITE);
-    int eq = 0;
-    frexp(qmax, &eq);
     const int sh = max(0, (32 - __clz((int)kmax)) - 5);
-    const long long wround = sh > 0 ? (1ll << (sh - 1)) : 0ll;  // the node weight's shift rounds
-    // value = acc * 2^-(3P + Q - 192 - sh), P = wexp, Q = 62 - eq
-    const int vexp = 3 * wexp + (62 - eq) - 192 - sh;
-    const bool accumulated = finite && count > 0 && qmax > 0.0;
+    // a contribution of exponent e_p lands on the component's scale: d = (e_r - e_p) + sh;
+    // value = sum * 2^(66 + e_r + sh - 3P) (e_r unbiased), P = wexp
+    const bool accumulated = count > 0;
     if (accumulated) {
       for (uint32_t c0 = 0; c0 < count; c0 += kFlatChunk) {
         const uint32_t c1 = min(count, c0 + kFlatChunk);
@@ -681,10 +817,13 @@ __global__ void __launch_bounds__(kThreads)
                 for (int i = 0; i < N2; ++i) {
                   const int lx = lxb + i;
                   if (lx < 0 || lx >= vx) continue;
-                  const long long w = (__mul64hi(w1[i], wyz) + wround) >> sh;
-                  for (int c = 0; c < ncomp; ++c)
-                    atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + row + lx,
-                                       (unsigned long long)__mul64hi(w, __ldg(qv + c)));
+                  const long long w = __mul64hi(w1[i], wyz);
+                  for (int c = 0; c < ncomp; ++c) {
+                    const int ep = __ldg(qe + (int64_t)sl * ncomp + c);
+                    if (ep == kENonFinite) atomicOr(poison + row + lx, 1u << (c & 31));
+                    else if (ep) add_contribution(acc0, acc1, acc2, acc3, c * (int)bg.slice + row + lx, w,
+                                                  __ldg(qv + c), ereg[c] - ep + sh);
+                  }
                 }
               }
             }
@@ -699,20 +838,28 @@ __global__ void __launch_bounds__(kThreads)
           uint32_t t = c0 + warp;
           uint32_t sl_n = 0, packed_n = 0;
           long long wl_n = 0ll, q_n[kQReg];
+          int e_n[kQReg];
           auto fetch = [&](uint32_t tt) {
             sl_n = pslot[tt - c0];
             packed_n = pxyz[tt - c0];
             wl_n = lane < 3 * N2 ? __ldg(wts + (int64_t)sl_n * (3 * N2) + lane) : 0ll;
 #pragma unroll
-            for (int r = 0; r < kQReg; ++r) q_n[r] = r < ncomp ? __ldg(qi + (int64_t)sl_n * ncomp + r) : 0ll;
+            for (int r = 0; r < kQReg; ++r) {
+              q_n[r] = r < ncomp ? __ldg(qi + (int64_t)sl_n * ncomp + r) : 0ll;
+              e_n[r] = r < ncomp ? __ldg(qe + (int64_t)sl_n * ncomp + r) : 0;
+            }
           };
           if (t < c1) fetch(t);
           for (; t < c1; t += nwarps) {
             const uint32_t sl = sl_n, packed = packed_n;
             const long long wl = wl_n;
             long long qr[kQReg];
+            int er[kQReg];
 #pragma unroll
-            for (int r = 0; r < kQReg; ++r) qr[r] = q_n[r];
+            for (int r = 0; r < kQReg; ++r) {
+              qr[r] = q_n[r];
+              er[r] = e_n[r];
+            }
             if (t + nwarps < c1) fetch(t + nwarps);
             const int ex = (int)(packed & 0xffu), ey = (int)((packed >> 8) & 0xffu), ez = (int)(packed >> 16);
             const int i0 = max(0, N2 - 1 - ex), i1 = min(N2, vx + N2 - 1 - ex);
@@ -721,6 +868,7 @@ __global__ void __launch_bounds__(kThreads)
             const int nx = i1 - i0, ny = j1 - j0, nz = k1 - k0;
             if (nx <= 0 || ny <= 0 || nz <= 0) continue;  // warp-uniform
             const long long *qv = qi + (int64_t)sl * ncomp;
+            const int32_t *ev = qe + (int64_t)sl * ncomp;
             const int count = nx * ny * nz;
             // idx -> (ii, jj, kk) by multiply-shift division: exact for idx < 4096, divisors <= 8
             const uint32_t rnx = (65536u + nx - 1) / nx, rny = (65536u + ny - 1) / ny;
@@ -734,16 +882,21 @@ __global__ void __launch_bounds__(kThreads)
               const long long wyj = __shfl_sync(0xffffffffu, wl, N2 + j);
               const long long wzk = __shfl_sync(0xffffffffu, wl, 2 * N2 + k);
               if (idx < count) {
-                const long long w = (__mul64hi(wxi, __mul64hi(wyj, wzk)) + wround) >> sh;
+                const long long w = __mul64hi(wxi, __mul64hi(wyj, wzk));
                 const int node = node0 + k * bg.pp + j * bg.p0 + i;
 #pragma unroll
                 for (int r = 0; r < kQReg; ++r)
-                  if (r < ncomp)
-                    atomic_add_split64(acc_lo, acc_hi, r * (int)bg.slice + node,
-                                       (unsigned long long)__mul64hi(w, qr[r]));
-                for (int c = kQReg; c < ncomp; ++c)
-                  atomic_add_split64(acc_lo, acc_hi, c * (int)bg.slice + node,
-                                     (unsigned long long)__mul64hi(w, __ldg(qv + c)));
+                  if (r < ncomp) {
+                    if (er[r] == kENonFinite) atomicOr(poison + node, 1u << (r & 31));
+                    else if (er[r]) add_contribution(acc0, acc1, acc2, acc3, r * (int)bg.slice + node, w, qr[r],
+                                                     ereg[r] - er[r] + sh);
+                  }
+                for (int c = kQReg; c < ncomp; ++c) {
+                  const int ep = __ldg(ev + c);
+                  if (ep == kENonFinite) atomicOr(poison + node, 1u << (c & 31));
+                  else if (ep) add_contribution(acc0, acc1, acc2, acc3, c * (int)bg.slice + node, w, __ldg(qv + c),
+                                                ereg[c] - ep + sh);
+                }
               }
             }
           }
@@ -759,12 +912,13 @@ __global__ void __launch_bounds__(kThreads)
         if (lx < vx && ly < vy && lz < vz) {
           const int64_t x = (int64_t)bc[0] * B0 + lx, y = (int64_t)bc[1] * B1 + ly, z = (int64_t)bc[2] * bg.b[2] + lz;
           T *f = field + x + g.nx * (y + g.ny * z) + g.npf * c;
-          const int64_t ai = c * bg.slice + lz * bg.pp + ly * bg.p0 + lx;
-          // each of the node's kcnt contributions was floored (the high product), half a
-          // unit low on average: that mean is added back, once
-          const long long a = (long long)(((unsigned long long)acc_hi[ai] << 32) | acc_lo[ai]) + (long long)(kcnt[nl] >> 1);
-          const T v = accumulated ? (T)ldexp((double)a, -vexp)
-                                  : (finite ? T(0) : quiet_nan<T>());
+          const int64_t ni = lz * bg.pp + ly * bg.p0 + lx, ai = c * bg.slice + ni;
+          // the 128-bit sum as a double (one rounding of the high part, one of the sum)
+          const long long hi = (long long)(((unsigned long long)acc3[ai] << 32) | acc2[ai]);
+          const unsigned long long lo = ((unsigned long long)acc1[ai] << 32) | acc0[ai];
+          const double sum = fma((double)hi, 18446744073709551616.0, (double)lo);
+          T v = (accumulated && ereg[c] > 0) ? (T)ldexp(sum, 66 + (ereg[c] - kEBias) + sh - 3 * wexp) : T(0);
+          if ((poison[ni] >> (c & 31)) & 1u) v = quiet_nan<T>();
           *f = beta_zero ? v : add_rn(mul_rn(beta, *f), v);
         }
         lx += lsx;
@@ -986,15 +1140,18 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   if (e0 > 32) wide_enough = false;  // the kernel finds the x segments with one warp
   p.bg.nseg = brick_segments(p.bg, g.n[0], n2);
   // shared memory besides the accumulators: region offsets and segment bases, the point
-  // chunk, the key tables, the coverage counts, the segment of each x and first x of each
+  // chunk, the key tables, the coverage counts, the segment of each x and first x of each,
+  // the components' scales and the NaN marks (one word per node of the padded slice, at
+  // most the accumulators' slice: bvol words plus the padding counted with the slice)
   const size_t rest = sizeof(uint32_t) * ecount + sizeof(uint32_t) * (size_t)e1 * e2 * p.bg.nseg +
                       2 * sizeof(uint32_t) * kFlatChunk + sizeof(uint32_t) * (size_t)(e0 + e1 + e2) +
-                      sizeof(uint32_t) * (size_t)(p.bg.bvol + 1) + sizeof(uint32_t) * (size_t)(e0 + p.bg.nseg);
+                      sizeof(uint32_t) * (size_t)(p.bg.bvol + 1) + sizeof(uint32_t) * (size_t)(e0 + p.bg.nseg) +
+                      sizeof(int32_t) * (size_t)ncomp;
   {
     // accumulator pitches that keep the unpadded layout's CTAs per SM (228 KB per SM, 1 KB
     // reserved per CTA by the runtime, the kernel's static scan slots) and its 200 KB cap;
     // they depend on the brick, the width and the components alone, so each is searched once
-    const size_t per_node = (size_t)ncomp * sizeof(unsigned long long), sm = 228 * 1024,
+    const size_t per_node = (size_t)ncomp * 16 + sizeof(uint32_t), sm = 228 * 1024,
                  reserve = 1024 + kScanSlots * sizeof(uint32_t);
     const size_t unpadded = (size_t)p.bg.bvol * per_node + rest;
     const size_t ctas = std::max<size_t>(1, sm / (unpadded + reserve));
@@ -1014,7 +1171,7 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
       p.bg.slice = (int64_t)p.bg.b[2] * p.bg.pp;
     }
   }
-  p.smem = (size_t)p.bg.slice * ncomp * sizeof(unsigned long long) + rest;
+  p.smem = (size_t)p.bg.slice * (ncomp * 16 + sizeof(uint32_t)) + rest;
   (void)esize;
   if (ecount > 65535) wide_enough = false;
   p.bricked = wide_enough && p.smem <= 200 * 1024 && nbricks * p.bg.bvol < (int64_t(1) << 32) - 1;
@@ -1022,30 +1179,37 @@ ScatterPlan plan_scatter(const gbg_grid &g, int ncomp, size_t esize, int n2) {
   return p;
 }
 
+// The scatter's workspace: keys, per-cell counts (then slot starts), ranks within a cell
+// (then the fallback sort's keys), the permutation, the counting sort's long-run flag and
+// scratch, the scan's scratch, per sorted slot the three axes' weights (64-bit fixed point
+// for the brick scatter) and the quantities (for the brick scatter as mantissas and
+// exponents, with per brick the largest exponent of every component).
 struct ScatterLayout {
-  uint32_t *keys, *counts, *skeys, *perm;
+  uint32_t *keys, *counts, *rank, *perm, *flag;
   void *sort_tmp;
   uint32_t *scan_tmp;
   void *rec, *qs;
-  long long *qi;  // alpha*q in 64-bit fixed point (brick scatter)
-  unsigned long long *qmax_bits;
+  long long *qi;
+  int32_t *qe;
+  uint32_t *ebrick;
 };
 
 ScatterLayout scatter_layout(Arena &a, int64_t m, const ScatterPlan &P, int ncomp, int n2, size_t esize) {
   ScatterLayout L;
   L.keys = a.take<uint32_t>((size_t)m);
   L.counts = a.take<uint32_t>((size_t)P.nkeys + 1);
-  L.skeys = a.take<uint32_t>((size_t)m);
+  L.rank = a.take<uint32_t>((size_t)m);
   L.perm = a.take<uint32_t>((size_t)m);
+  L.flag = a.take<uint32_t>(4);
   L.sort_tmp = a.take<char>(radix_sort_temp_bytes(m));
   L.scan_tmp = a.take<uint32_t>(scan_temp_elems(P.nkeys + 1));
-  // the three axes' weights per point, in sorted order (64-bit fixed point for the brick
-  // scatter, which keeps its quantities in qi and needs no qs)
   const size_t rec_bytes = 3 * (size_t)n2 * (P.bricked ? sizeof(long long) : esize);
   L.rec = a.take<char>((size_t)m * rec_bytes);
   L.qs = P.bricked ? nullptr : a.take<char>((size_t)m * ncomp * esize);
   L.qi = P.bricked ? a.take<long long>((size_t)m * ncomp) : nullptr;
-  L.qmax_bits = a.take<unsigned long long>(4);
+  L.qe = P.bricked ? a.take<int32_t>((size_t)m * ncomp) : nullptr;
+  const int64_t nbricks = P.bricked ? P.bg.nb[0] * P.bg.nb[1] * P.bg.nb[2] : 0;
+  L.ebrick = P.bricked ? a.take<uint32_t>((size_t)nbricks * ncomp) : nullptr;
   return L;
 }
 
@@ -1062,20 +1226,22 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   const SchemeT<T, N2> s = make_scheme<T, N2>(sch);
   const int wexp = fixed_weight_exp(sch);
   const int blocks_m = launch_blocks(m, kThreads);
-  GBG_CUDA_TRY(cudaMemsetAsync(L.qmax_bits, 0, sizeof(unsigned long long), st));
-  k_brick_keys<T><<<blocks_m, kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, q, ncomp, T(alpha),
-                                                 L.qmax_bits, status);
-  note_launch();
-  GBG_CUDA_TRY(cudaGetLastError());
-  GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(P.nkeys - 1)), L.sort_tmp, st));
-  GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
-  k_brick_order<T, N2, FIXED ? N2 : 0><<<blocks_m, kThreads, 0, st>>>(
-      g, s, x, L.perm, m, wexp, static_cast<long long *>(L.rec), q, ncomp, T(alpha), L.qmax_bits, L.qi);
-  note_launch();
-  GBG_CUDA_TRY(cudaGetLastError());
-  auto kernel = k_scatter_fixed64<T, N2>;
-  GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
   const int64_t nbricks = P.bg.nb[0] * P.bg.nb[1] * P.bg.nb[2];
+  GBG_CUDA_TRY(cudaMemsetAsync(L.ebrick, 0, sizeof(uint32_t) * (size_t)nbricks * ncomp, st));
+  GBG_CUDA_TRY(cudaMemsetAsync(L.flag, 0, sizeof(uint32_t), st));
+  k_brick_keys<T><<<blocks_m, kThreads, 0, st>>>(g, P.bg, x, m, L.keys, L.counts, L.rank, q, ncomp, T(alpha),
+                                                 L.ebrick, status);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  GBG_TRY(exclusive_scan_u32(L.counts, L.counts, P.nkeys + 1, L.scan_tmp, st));
+  GBG_TRY(stable_counting_sort(L.keys, L.rank, L.counts, m, bits_for((uint64_t)(P.nkeys - 1)), L.perm, L.rank,
+                               L.flag, L.sort_tmp, st));
+  k_brick_order<T, N2, FIXED ? N2 : 0><<<blocks_m, kThreads, 0, st>>>(
+      g, s, x, L.perm, m, wexp, static_cast<long long *>(L.rec), q, ncomp, T(alpha), L.qi, L.qe);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  auto kernel = k_scatter_fixed128<T, N2>;
+  GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P.smem));
   int dev = 0, sms = 1, per_sm = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1084,7 +1250,7 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   BrickGeo bg = P.bg;
   size_t smem = P.smem;
   if (bg.slice != bg.bvol) {
-    const size_t flat = smem - (size_t)(bg.slice - bg.bvol) * ncomp * sizeof(unsigned long long);
+    const size_t flat = smem - (size_t)(bg.slice - bg.bvol) * (ncomp * 16 + sizeof(uint32_t));
     int flat_per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&flat_per_sm, kernel, kThreads, flat);
     if (flat_per_sm > per_sm) {
@@ -1098,13 +1264,18 @@ gbg_status launch_bricked(const GridT<T> &g, const ScatterPlan &P, const gbg_sch
   const int blocks = (int)std::min<int64_t>(nbricks, (int64_t)sms * std::max(per_sm, 1));
   mark_main_start(st);
   kernel<<<blocks, kThreads, smem, st>>>(g, bg, ncomp, L.counts, static_cast<const long long *>(L.rec), L.qi,
-                                         L.qmax_bits, wexp, field, T(beta), beta == 0.0, status);
+                                         L.qe, L.ebrick, wexp, field, T(beta), beta == 0.0);
   mark_main_stop(st);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
 }
 
+
+// The deterministic scatter.  The brick push (128-bit integer sums, FP64-grade per node)
+// whenever every axis is at least a stencil wide and a brick's accumulators fit in shared
+// memory; otherwise the node pull (points sorted by cell, one thread per node summing its
+// contributions in T in a fixed order), which also takes a stencil wider than the grid.
 template <typename T>
 gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int ncomp, void *field,
                             const void *pos, int64_t m, const void *q, double alpha, double beta,
@@ -1126,14 +1297,15 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
     GBG_BRICKED(8);
 #undef GBG_BRICKED
   }
-  const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
   const int64_t ncells = g.npf;
-  k_cell_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, x, m, L.keys, L.counts, status);
+  GBG_CUDA_TRY(cudaMemsetAsync(L.flag, 0, sizeof(uint32_t), st));
+  const SchemeT<T, GBG_MAX_NODES> s = make_scheme<T, GBG_MAX_NODES>(sch);
+  k_cell_keys<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(g, x, m, L.keys, L.counts, L.rank, status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
-  GBG_TRY(radix_sort_pairs(L.keys, nullptr, L.skeys, L.perm, m, bits_for((uint64_t)(ncells - 1)),
-                           L.sort_tmp, st));
   GBG_TRY(exclusive_scan_u32(L.counts, L.counts, ncells + 1, L.scan_tmp, st));
+  GBG_TRY(stable_counting_sort(L.keys, L.rank, L.counts, m, bits_for((uint64_t)(ncells - 1)), L.perm, L.rank,
+                               L.flag, L.sort_tmp, st));
   T *rec = static_cast<T *>(L.rec);
   T *qs = static_cast<T *>(L.qs);
   k_scatter_prep<T><<<launch_blocks(m, kThreads), kThreads, 0, st>>>(
@@ -1143,11 +1315,24 @@ gbg_status dispatch_scatter(const gbg_grid &grid, const gbg_scheme &sch, int nco
   const int blocks = launch_blocks(ncells, kThreads);
   const int bz = beta == 0.0;
   const int n2 = sch.stencil_width;
-  switch (chunk_for(ncomp)) {
-    case 9: k_scatter_pull<T, 9><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
-    case 3: k_scatter_pull<T, 3><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
-    default: k_scatter_pull<T, 1><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); note_launch(); break;
+  const int cc = chunk_for(ncomp);
+  mark_main_start(st);
+#define GBG_PULL_N(W)                                                                                                  \
+  if (n2 == W) {                                                                                                       \
+    if (cc == 9) k_scatter_pull_n<T, W, 9><<<blocks, kThreads, 0, st>>>(g, ncomp, L.counts, rec, qs, f, T(beta), bz);  \
+    else if (cc == 3) k_scatter_pull_n<T, W, 3><<<blocks, kThreads, 0, st>>>(g, ncomp, L.counts, rec, qs, f, T(beta), bz); \
+    else k_scatter_pull_n<T, W, 1><<<blocks, kThreads, 0, st>>>(g, ncomp, L.counts, rec, qs, f, T(beta), bz);          \
+  } else
+  GBG_PULL_N(2) GBG_PULL_N(4) GBG_PULL_N(6) GBG_PULL_N(8) {
+    switch (cc) {
+      case 9: k_scatter_pull<T, 9><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+      case 3: k_scatter_pull<T, 3><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+      default: k_scatter_pull<T, 1><<<blocks, kThreads, 0, st>>>(g, n2, ncomp, L.counts, rec, qs, f, T(beta), bz); break;
+    }
   }
+#undef GBG_PULL_N
+  mark_main_stop(st);
+  note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
 }
@@ -1317,7 +1502,8 @@ gbg_status gbg_anterpolate_noalloc(const gbg_grid *grid, gbg_dtype dtype, int32_
     void *scratch = nullptr;
     if (need > 0) GBG_TRY(noalloc_scratch(&scratch));
     // The shared path: with a caller workspace it allocates nothing, and it clears the
-    // per-cell counts (the only buffer that must start at zero) before every use.
+    // per-cell counts and the sort's flag (the only words that must start at zero) before
+    // every use.
     const gbg_status st = gbg_anterpolate(grid, dtype, ncomp, field, positions, npoints, quantities, nullptr,
                                           scheme, alpha, beta, scratch, GBG_NOALLOC_SCRATCH_BYTES,
                                           device_status, stream);

@@ -324,13 +324,14 @@ __device__ __forceinline__ void unpack_local(float w, int &lx, int &ly, int &lz)
   lz = (int)(loc >> 16);
 }
 
-// Keys, counts and per-point records of the bins; with DISP the positions are first
+// Keys, counts (each point keeps the count its atomic returned, its rank within the key
+// in no particular order) and per-point records of the bins; with DISP the positions are first
 // displaced (and wrapped) from `disp`, written to disp.dst, and binned in the same pass.
 template <typename T, bool DISP = false>
 __global__ void __launch_bounds__(kThreads)
     k_bin_keys(BinGeom g, const T *__restrict__ pos, int64_t m, uint32_t *__restrict__ keys,
-               uint32_t *__restrict__ counts, float4 *__restrict__ rec_user, int32_t *status,
-               DisplaceArgs<T> disp = {}) {
+               uint32_t *__restrict__ counts, uint32_t *__restrict__ rank, float4 *__restrict__ rec_user,
+               int32_t *status, DisplaceArgs<T> disp = {}) {
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < m;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t c[3];
@@ -357,7 +358,7 @@ __global__ void __launch_bounds__(kThreads)
     const uint32_t local = (lz * (uint32_t)g.b[1] + ly) * (uint32_t)g.b[0] + lx;
     const uint32_t key = (uint32_t)(((bz * g.nb[1] + by) * g.nb[0] + bx) * g.bvol + local);
     keys[p] = key;
-    atomicAdd(counts + key, 1u);
+    rank[p] = atomicAdd(counts + key, 1u);
     rec_user[p] = make_float4(t[0], t[1], t[2], __uint_as_float(pack_local(lx, ly, lz)));
   }
 }
@@ -1259,7 +1260,8 @@ StagedGeo staged_geo(const gbg_field_s *f, const gbg_bins_s *b, int width) {
 }
 
 template <int N2, int M2, typename TO>
-gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, TO *out, cudaStream_t st) {
+gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, TO *out, int32_t *status,
+                                cudaStream_t st) {
   CUtensorMap *map = nullptr;
   GBG_TRY(tensor_map_for(f, N2, b->b, &map));
   const StagedGeo g = staged_geo(f, b, N2);
@@ -1271,7 +1273,6 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
   int sms = 0, dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int32_t *status = nullptr;
   const int threads = b->gather_threads ? b->gather_threads : (N2 == 4 ? kGatherThreads : kThreads);
   auto go = [&](auto kernel) -> gbg_status {
     // Double-buffer the tile when that leaves as many CTAs per SM as a single buffer
@@ -1927,7 +1928,8 @@ gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, i
                            cudaStream_t st, const DisplaceArgs<T> *disp) {
   b->npoints = npoints;
   GBG_CUDA_TRY(cudaMemsetAsync(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1), st));
-  GBG_CUDA_TRY(cudaMemsetAsync(b->lists_n, 0, sizeof(uint32_t) * 2, st));
+  // the two work-list lengths and the counting sort's long-run flag
+  GBG_CUDA_TRY(cudaMemsetAsync(b->lists_n, 0, sizeof(uint32_t) * 3, st));
   if (npoints == 0) return GBG_OK;
   BinGeom g;
   for (int d = 0; d < 3; ++d) {
@@ -1942,18 +1944,23 @@ gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, i
   }
   g.bvol = b->bvol;
   const int blocks = launch_blocks(npoints, kThreads);
+  // the rank of each point within its key goes to skeys (free until the fallback sort)
   if (disp)
-    k_bin_keys<T, true><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->rec_user,
-                                                     device_status, *disp);
+    k_bin_keys<T, true><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->skeys,
+                                                     b->rec_user, device_status, *disp);
   else
-    k_bin_keys<T, false><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->rec_user,
-                                                      device_status);
+    k_bin_keys<T, false><<<blocks, kThreads, 0, st>>>(g, positions, npoints, b->keys, b->cell_start, b->skeys,
+                                                      b->rec_user, device_status);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   int bits = 0;
   while (bits < 32 && ((uint64_t)(b->nkeys - 1) >> bits) != 0) ++bits;
-  GBG_TRY(radix_sort_pairs(b->keys, nullptr, b->skeys, b->perm, npoints, bits, b->sort_tmp, st));
+  // one counting pass: the scan of the counts gives every cell its slots, the atomic ranks
+  // place the points, and a per-cell pass puts each cell's points in index order (the
+  // stable order; a cell of more than 1024 points sends the whole sort to the radix sort)
   GBG_TRY(exclusive_scan_u32(b->cell_start, b->cell_start, b->nkeys + 1, b->scan_tmp, st));
+  GBG_TRY(stable_counting_sort(b->keys, b->skeys, b->cell_start, npoints, bits, b->perm, b->skeys, b->lists_n + 2,
+                               b->sort_tmp, st));
   k_gather_records<<<blocks, kThreads, 0, st>>>(b->rec_user, b->perm, npoints, b->rec);
   note_launch();
   k_brick_lists<<<launch_blocks(b->nbricks, kThreads), kThreads, 0, st>>>(
@@ -2055,7 +2062,7 @@ gbg_status gbg_bins_order(gbg_bins b, int32_t *order, void *stream) {
 }
 
 gbg_status gbg_interpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *scheme, gbg_dtype out_dtype,
-                                  void *out, void *stream) {
+                                  void *out, int32_t *device_status, void *stream) {
   clear_error();
   GBG_TRY(check_field_bins(f, b, scheme));
   if (out_dtype != GBG_F32 && out_dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
@@ -2065,15 +2072,15 @@ gbg_status gbg_interpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   auto run = [&](auto *o) -> gbg_status {
     switch (scheme->stencil_width) {
       // compile-time (width, powers) for the common schemes, guarded Horner otherwise
-      case 2: return scheme->num_powers == 2 ? launch_staged_gather<2, 2>(f, b, *scheme, o, st)
-                                             : launch_staged_gather<2, 0>(f, b, *scheme, o, st);
-      case 4: return scheme->num_powers == 4 ? launch_staged_gather<4, 4>(f, b, *scheme, o, st)
-                                             : launch_staged_gather<4, 0>(f, b, *scheme, o, st);
-      case 6: return scheme->num_powers == 6 ? launch_staged_gather<6, 6>(f, b, *scheme, o, st)
-                     : scheme->num_powers == 4 ? launch_staged_gather<6, 4>(f, b, *scheme, o, st)
-                                               : launch_staged_gather<6, 0>(f, b, *scheme, o, st);
-      default: return scheme->num_powers == 8 ? launch_staged_gather<8, 8>(f, b, *scheme, o, st)
-                                              : launch_staged_gather<8, 0>(f, b, *scheme, o, st);
+      case 2: return scheme->num_powers == 2 ? launch_staged_gather<2, 2>(f, b, *scheme, o, device_status, st)
+                                             : launch_staged_gather<2, 0>(f, b, *scheme, o, device_status, st);
+      case 4: return scheme->num_powers == 4 ? launch_staged_gather<4, 4>(f, b, *scheme, o, device_status, st)
+                                             : launch_staged_gather<4, 0>(f, b, *scheme, o, device_status, st);
+      case 6: return scheme->num_powers == 6 ? launch_staged_gather<6, 6>(f, b, *scheme, o, device_status, st)
+                     : scheme->num_powers == 4 ? launch_staged_gather<6, 4>(f, b, *scheme, o, device_status, st)
+                                               : launch_staged_gather<6, 0>(f, b, *scheme, o, device_status, st);
+      default: return scheme->num_powers == 8 ? launch_staged_gather<8, 8>(f, b, *scheme, o, device_status, st)
+                                              : launch_staged_gather<8, 0>(f, b, *scheme, o, device_status, st);
     }
   };
   if (out_dtype == GBG_F64) return run(static_cast<double *>(out));
@@ -2081,7 +2088,7 @@ gbg_status gbg_interpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
 }
 
 gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *scheme, gbg_dtype q_dtype,
-                                  const void *q, double alpha, double beta, void *stream) {
+                                  const void *q, double alpha, double beta, int32_t *device_status, void *stream) {
   clear_error();
   GBG_TRY(check_field_bins(f, b, scheme));
   if (q_dtype != GBG_F32 && q_dtype != GBG_F64) return set_error(GBG_EARG, "bad dtype");
@@ -2105,17 +2112,17 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   const bool fixed = scheme->num_powers == w;
   gbg_status s;
   if (w == 2)
-    s = fixed ? launch_staged_scatter<2, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-              : launch_staged_scatter<2, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<2, true>(f, b, *scheme, beta, b->qmax_bits, device_status, st)
+              : launch_staged_scatter<2, false>(f, b, *scheme, beta, b->qmax_bits, device_status, st);
   else if (w == 4)
-    s = fixed ? launch_staged_scatter<4, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-              : launch_staged_scatter<4, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<4, true>(f, b, *scheme, beta, b->qmax_bits, device_status, st)
+              : launch_staged_scatter<4, false>(f, b, *scheme, beta, b->qmax_bits, device_status, st);
   else if (w == 6)
-    s = fixed ? launch_staged_scatter<6, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-              : launch_staged_scatter<6, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<6, true>(f, b, *scheme, beta, b->qmax_bits, device_status, st)
+              : launch_staged_scatter<6, false>(f, b, *scheme, beta, b->qmax_bits, device_status, st);
   else
-    s = fixed ? launch_staged_scatter<8, true>(f, b, *scheme, beta, b->qmax_bits, nullptr, st)
-              : launch_staged_scatter<8, false>(f, b, *scheme, beta, b->qmax_bits, nullptr, st);
+    s = fixed ? launch_staged_scatter<8, true>(f, b, *scheme, beta, b->qmax_bits, device_status, st)
+              : launch_staged_scatter<8, false>(f, b, *scheme, beta, b->qmax_bits, device_status, st);
   GBG_TRY(s);
   const int64_t total = ghost_count(f->px, f->py, f->pz, f->grid.n[0], f->grid.n[1], f->grid.n[2]);
   k_fill_ghosts<<<launch_blocks(total, kThreads), kThreads, 0, st>>>(f->data, f->cp, f->px, f->py, f->pz, f->halo,
@@ -2500,7 +2507,7 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
     }
   }
   for (const gbg_batch_item &it : bt->direct)
-    if (it.out) GBG_TRY(gbg_interpolate_binned(it.field, it.bins, &it.scheme, GBG_F32, it.out, stream));
+    if (it.out) GBG_TRY(gbg_interpolate_binned(it.field, it.bins, &it.scheme, GBG_F32, it.out, device_status, stream));
   if (pooled && bt->nswork > 0) {
     GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)bt->scatter_smem));
@@ -2521,7 +2528,7 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
     GBG_CUDA_TRY(cudaGetLastError());
   }
   for (const gbg_batch_item &it : bt->direct)
-    if (it.dest) GBG_TRY(gbg_anterpolate_binned(it.dest, it.bins, &it.scheme, GBG_F32, it.q, it.alpha, it.beta, stream));
+    if (it.dest) GBG_TRY(gbg_anterpolate_binned(it.dest, it.bins, &it.scheme, GBG_F32, it.q, it.alpha, it.beta, device_status, stream));
   return GBG_OK;
 }
 

@@ -49,7 +49,8 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *w
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_block_sums(const uint32_t *in, int64_t n,
-                                                             uint32_t *sums) {
+                                                             uint32_t *sums, const uint32_t *gate) {
+  if (gate && __ldg(gate) == 0u) return;
   __shared__ uint32_t ws[32];
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
   uint32_t s = 0;
@@ -66,7 +67,9 @@ __global__ void __launch_bounds__(kScanThreads) k_block_sums(const uint32_t *in,
 // Scans one tile (coalesced through shared memory) and adds offsets[blockIdx.x] if given.
 // in may equal out: a block only reads and writes its own tile.
 __global__ void __launch_bounds__(kScanThreads) k_scan_tile(const uint32_t *in, uint32_t *out,
-                                                            int64_t n, const uint32_t *offsets) {
+                                                            int64_t n, const uint32_t *offsets,
+                                                            const uint32_t *gate) {
+  if (gate && __ldg(gate) == 0u) return;
   __shared__ uint32_t tile[kScanTile];
   __shared__ uint32_t ws[32];
   const int64_t base = (int64_t)blockIdx.x * kScanTile;
@@ -99,7 +102,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tile(const uint32_t *in, 
 }
 
 __global__ void __launch_bounds__(kRsThreads) k_rs_hist(const uint32_t *keys, int64_t n, int shift,
-                                                        uint32_t *hist, int64_t nb) {
+                                                        uint32_t *hist, int64_t nb, const uint32_t *gate) {
+  if (gate && __ldg(gate) == 0u) return;
   __shared__ uint32_t h[kRsWarps][kRsBins];
   for (int i = threadIdx.x; i < kRsWarps * kRsBins; i += kRsThreads) (&h[0][0])[i] = 0u;
   __syncthreads();
@@ -127,8 +131,9 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const uint32_t *keys_
                                                            const uint32_t *vals_in, int64_t n,
                                                            int shift, const uint32_t *offsets,
                                                            int64_t nb, uint32_t *keys_out,
-                                                           uint32_t *vals_out) {
+                                                           uint32_t *vals_out, const uint32_t *gate) {
   static_assert(kRsThreads == kRsBins, "one thread per digit in the tile's digit scan");
+  if (gate && __ldg(gate) == 0u) return;
   __shared__ uint32_t wh[kRsWarps][kRsBins];
   __shared__ uint32_t sbase[kRsBins], goff[kRsBins], ws[32];
   __shared__ uint32_t skey[kRsTile], sval[kRsTile];
@@ -205,6 +210,41 @@ int sm_count_cached() {
   return cached[dev];
 }
 
+// Counting placement.  Every point p already holds rank[p], the value an atomic count of
+// its key returned (unique within the key, but in no particular order), and starts[] is the
+// exclusive scan of the counts: the slot starts[key] + rank is free for it.
+__global__ void k_place_unstable(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ rank,
+                                 const uint32_t *__restrict__ starts, int64_t n, uint32_t *__restrict__ perm_u) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
+    perm_u[__ldg(starts + __ldg(keys + p)) + __ldg(rank + p)] = (uint32_t)p;
+}
+
+// Makes the placement stable: the point in slot s moves to the position, within its key's
+// run of slots, given by the number of the run's points with a smaller index.  Runs longer
+// than kPlaceMaxRun are left alone and raise *big instead (the radix sort then redoes the
+// whole order), so no thread does more than kPlaceMaxRun steps.
+constexpr uint32_t kPlaceMaxRun = 1024;
+__global__ void k_place_stable(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ starts,
+                               const uint32_t *__restrict__ perm_u, int64_t n, uint32_t *__restrict__ perm,
+                               uint32_t *big) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = __ldg(perm_u + s);
+    const uint32_t k = __ldg(keys + p);
+    const uint32_t a = __ldg(starts + k), c = __ldg(starts + k + 1) - a;
+    if (c == 1u) {
+      perm[s] = p;
+      continue;
+    }
+    if (c > kPlaceMaxRun) {
+      atomicOr(big, 1u);
+      continue;
+    }
+    uint32_t r = 0;
+    for (uint32_t t = 0; t < c; ++t) r += __ldg(perm_u + a + t) < p ? 1u : 0u;
+    perm[a + r] = p;
+  }
+}
+
 }  // namespace
 
 int launch_blocks(int64_t work, int threads, int per_sm) {
@@ -225,22 +265,22 @@ size_t scan_temp_elems(int64_t n) {
 }
 
 gbg_status exclusive_scan_u32(const uint32_t *in, uint32_t *out, int64_t n, uint32_t *tmp,
-                              cudaStream_t stream) {
+                              cudaStream_t stream, const uint32_t *gate) {
   if (n <= 0) return GBG_OK;
   const int64_t nb = (n + kScanTile - 1) / kScanTile;
   if (nb == 1) {
-    k_scan_tile<<<1, kScanThreads, 0, stream>>>(in, out, n, nullptr);
+    k_scan_tile<<<1, kScanThreads, 0, stream>>>(in, out, n, nullptr, gate);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   }
   uint32_t *sums = tmp;
   uint32_t *rest = tmp + nb + 64;
-  k_block_sums<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, n, sums);
+  k_block_sums<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, n, sums, gate);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
-  GBG_TRY(exclusive_scan_u32(sums, sums, nb, rest, stream));
-  k_scan_tile<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, out, n, sums);
+  GBG_TRY(exclusive_scan_u32(sums, sums, nb, rest, stream, gate));
+  k_scan_tile<<<(unsigned)nb, kScanThreads, 0, stream>>>(in, out, n, sums, gate);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return GBG_OK;
@@ -258,7 +298,7 @@ size_t radix_sort_temp_bytes(int64_t n) {
 
 gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, uint32_t *keys_out,
                             uint32_t *vals_out, int64_t n, int key_bits, void *temp,
-                            cudaStream_t stream) {
+                            cudaStream_t stream, const uint32_t *gate) {
   if (n <= 0) return GBG_OK;
   if (n > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "radix sort: more than 2^31-1 points");
   const int64_t nb = (n + kRsTile - 1) / kRsTile;
@@ -276,17 +316,35 @@ gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, ui
     const bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t *kout = to_out ? keys_out : kt;
     uint32_t *vout = to_out ? vals_out : vt;
-    k_rs_hist<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, n, 8 * p, hist, nb);
+    k_rs_hist<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, n, 8 * p, hist, nb, gate);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
-    GBG_TRY(exclusive_scan_u32(hist, hist, kRsBins * nb, scan_tmp, stream));
-    k_rs_scatter<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, vin, n, 8 * p, hist, nb, kout, vout);
+    GBG_TRY(exclusive_scan_u32(hist, hist, kRsBins * nb, scan_tmp, stream, gate));
+    k_rs_scatter<<<(unsigned)nb, kRsThreads, 0, stream>>>(kin, vin, n, 8 * p, hist, nb, kout, vout, gate);
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
     kin = kout;
     vin = vout;
   }
   return GBG_OK;
+}
+
+
+gbg_status stable_counting_sort(const uint32_t *keys, const uint32_t *rank, const uint32_t *starts, int64_t n,
+                                int key_bits, uint32_t *perm, uint32_t *skeys, uint32_t *big, void *temp,
+                                cudaStream_t stream) {
+  if (n <= 0) return GBG_OK;
+  if (n > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "counting sort: more than 2^31-1 points");
+  // the unstable placement lives at the start of the radix sort's scratch, which only the
+  // fallback (after the stable pass has read it) writes
+  uint32_t *perm_u = static_cast<uint32_t *>(temp);
+  const int blocks = launch_blocks(n, 256);
+  k_place_unstable<<<blocks, 256, 0, stream>>>(keys, rank, starts, n, perm_u);
+  note_launch();
+  k_place_stable<<<blocks, 256, 0, stream>>>(keys, starts, perm_u, n, perm, big);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return radix_sort_pairs(keys, nullptr, skeys, perm, n, key_bits, temp, stream, big);
 }
 
 }  // namespace gbg

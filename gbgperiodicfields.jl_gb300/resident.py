@@ -137,18 +137,21 @@ class PointBins:
 
 
 def interpolate_binned(field: ResidentField, bins: PointBins, scheme, out: torch.Tensor | None = None,
-                       dtype=torch.float32) -> torch.Tensor:
+                       dtype=torch.float32, status: torch.Tensor | None = None) -> torch.Tensor:
     if out is None:
         out = empty_colmajor((bins.npoints, field.ncomp), dtype, "cuda")
     _lib.check(_lib.load().gbg_interpolate_binned(field.handle, bins.handle, scheme.c(), _DTYPE_CODE[out.dtype],
-                                                  out.data_ptr(), _stream()), "gbg_interpolate_binned")
+                                                  out.data_ptr(), status.data_ptr() if status is not None else None,
+                                                  _stream()), "gbg_interpolate_binned")
     return out
 
 
-def anterpolate_binned(field: ResidentField, bins: PointBins, scheme, q: torch.Tensor, alpha=1.0, beta=0.0):
+def anterpolate_binned(field: ResidentField, bins: PointBins, scheme, q: torch.Tensor, alpha=1.0, beta=0.0,
+                       status: torch.Tensor | None = None):
     q = colmajor(q)
     _lib.check(_lib.load().gbg_anterpolate_binned(field.handle, bins.handle, scheme.c(), _DTYPE_CODE[q.dtype],
-                                                  q.data_ptr(), float(alpha), float(beta), _stream()),
+                                                  q.data_ptr(), float(alpha), float(beta),
+                                                  status.data_ptr() if status is not None else None, _stream()),
                "gbg_anterpolate_binned")
     return field
 

@@ -260,17 +260,20 @@ gbg_status gbg_bins_build(gbg_bins bins, gbg_dtype pos_dtype, const void *positi
 gbg_status gbg_bins_order(gbg_bins bins, int32_t *order, void *stream);
 
 /* Gather of a resident field at binned points into out (M, ncomp) of out_dtype, in the
- * points' own order.  scheme width must not exceed the field's max_stencil_width. */
+ * points' own order.  scheme width must not exceed the field's max_stencil_width.  A
+ * bounded wait on a staged tile that gives up sets GBG_DEV_TIMEOUT in device_status (may
+ * be NULL) and leaves that tile's points unwritten. */
 gbg_status gbg_interpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
-                                  gbg_dtype out_dtype, void *out, void *stream);
+                                  gbg_dtype out_dtype, void *out, int32_t *device_status, void *stream);
 /* Deterministic scatter of q (M, ncomp) of q_dtype at binned points into a resident
  * field: field = alpha * W^T q + beta * field.  No atomics: each node's sum is formed
  * by one thread in a fixed order (the node's rows of cells, within a row the points in
  * binned order), so the result is bitwise reproducible and independent of the launch
- * shape; the ghost layer is refreshed. */
+ * shape; the ghost layer is refreshed.  A non-finite quantity sets GBG_DEV_NONFINITE in
+ * device_status (may be NULL). */
 gbg_status gbg_anterpolate_binned(gbg_field field, gbg_bins bins, const gbg_scheme *scheme,
                                   gbg_dtype q_dtype, const void *q, double alpha, double beta,
-                                  void *stream);
+                                  int32_t *device_status, void *stream);
 
 /* ------------------------------------------------------------ batched form
  *

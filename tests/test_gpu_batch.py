@@ -145,3 +145,18 @@ def test_autotune_persists_and_keeps_results(gbg, oracle, dev, tmp_path, monkeyp
         assert torch.equal(d2.read(), ref)
         assert torch.equal(resident.interpolate_binned(field, bins, gbg.CatmullRom),
                            torch.from_numpy(got).cuda())
+
+
+def test_batch_reports_nonfinite_from_a_direct_instance(gbg, oracle, dev):
+    """An instance large enough to run through the single-instance kernels inside the batch
+    still reports a non-finite quantity in the batch's status word."""
+    resident, insts = make_instances(gbg, oracle, seed=3, specs=mixed_specs(gbg))
+    big = insts[1]
+    assert big["pos"].shape[0] >= 1024
+    big["qt"][17, 1] = float("nan")
+    batch = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"], dest=i["dest"],
+                                 q=i["qt"], alpha=1.0, beta=0.0) for i in insts])
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    batch.run(status)
+    torch.cuda.synchronize()
+    assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE

@@ -119,3 +119,32 @@ def test_nonfinite_position_flagged(gbg, oracle, dev):
     resident.PointBins(grid, 2).build(pos, status)
     torch.cuda.synchronize()
     assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE
+
+
+def test_bins_order_with_a_crowded_cell(gbg, oracle, dev):
+    """A cell holding more than 1024 points sends the counting sort to the radix sort: the
+    order is still the stable brick sort."""
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (20, 18, 16), 3, 3000, 41, brick=(11, 8, 8))
+    rng = np.random.default_rng(42)
+    crowd = np.asfortranarray(np.vstack([pos, np.full((2500, 3), 0.5) + 0.01 * rng.random((2500, 3))]))
+    bins = resident.PointBins(grid, len(crowd), brick=(11, 8, 8)).build(torch.from_numpy(crowd).cuda())
+    order = bins.order().cpu().numpy()
+    n = np.array(grid.grid_size)
+    b = np.array([11, 8, 8])
+    nb = -(-n // b)
+    c = np.mod(np.floor((crowd - np.array(grid.origin)) * (n / np.array(grid.domain_size))).astype(np.int64), n)
+    br = c // b
+    loc = c - br * b
+    key = ((br[:, 2] * nb[1] + br[:, 1]) * nb[0] + br[:, 0]) * b.prod() + (loc[:, 2] * b[1] + loc[:, 1]) * b[0] + loc[:, 0]
+    assert np.array_equal(order, np.argsort(key, kind="stable") + 1)
+
+
+def test_nonfinite_quantity_is_reported(gbg, oracle, dev):
+    """A NaN quantity in the binned scatter sets GBG_DEV_NONFINITE in the status word."""
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (16, 16, 16), 3, 2000, 51)
+    q = q.copy(order="F")
+    q[100, 1] = np.nan
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    resident.anterpolate_binned(field, bins, gbg.CatmullRom, torch.from_numpy(q).cuda(), 1.0, 0.0, status=status)
+    torch.cuda.synchronize()
+    assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE

@@ -332,3 +332,84 @@ def test_config1_parity(gbg, oracle, dev):
     lhs = torch.dot(got, torch.from_numpy(q).to(dev)).item()
     rhs = torch.sum(torch.from_numpy(f).to(dev) * dep).item()
     assert abs(lhs - rhs) / (got.norm().item() * np.linalg.norm(q)) <= 1e-13
+
+
+def _abs_scatter(coeffs, n, pos, q, dx):
+    """Per node and component, sum over points of |w_x w_y w_z| |q| (numpy, FP64): the
+    magnitude that bounds the rounding error of any FP64 sum of the node's contributions."""
+    n2 = coeffs.shape[0]
+    half = n2 // 2
+    ci = pos / dx
+    base = np.floor(ci).astype(np.int64)
+    t = ci - base
+    w = []
+    for d in range(3):
+        # Horner over the powers, every node at once: w[p, i] = sum_r c[i, r] t_p^r
+        acc = np.zeros((len(pos), n2))
+        for r in range(coeffs.shape[1] - 1, -1, -1):
+            acc = acc * t[:, d:d + 1] + coeffs[:, r][None, :]
+        w.append(np.abs(acc))
+    A = np.zeros(tuple(n) + (q.shape[1],))
+    for i in range(n2):
+        for j in range(n2):
+            for k in range(n2):
+                wt = w[0][:, i] * w[1][:, j] * w[2][:, k]
+                ix = np.mod(base[:, 0] - half + 1 + i, n[0])
+                iy = np.mod(base[:, 1] - half + 1 + j, n[1])
+                iz = np.mod(base[:, 2] - half + 1 + k, n[2])
+                for c in range(q.shape[1]):
+                    np.add.at(A[..., c], (ix, iy, iz), wt * np.abs(q[:, c]))
+    return A
+
+
+@pytest.mark.parametrize("width", [4, 6])
+def test_scatter_per_node_accuracy_across_magnitudes(gbg, oracle, dev, width):
+    """Quantities spanning eight decades by region (1, 1e-3, 1e-6, 1e-8 by z slab), one
+    component all zero and one scaled by 1e-4: every node of the FP64 scatter is within
+    1e-12 of the sum of its contributions' magnitudes, as any FP64 sum of that node's
+    contributions is (the reference's atomic adds included) -- not only relative to the
+    largest value in the field -- and the zero component is exactly zero."""
+    n = (24, 20, 32)
+    grid, g = make(gbg, oracle, n=n)
+    rng = np.random.default_rng(300 + width)
+    M = 30000
+    pos = np.asfortranarray(TWO_PI * rng.random((M, 3)))
+    slab = np.minimum((pos[:, 2] / TWO_PI * 4).astype(int), 3)
+    q = rng.standard_normal((M, 3)) * np.array([1.0, 1e-3, 1e-6, 1e-8])[slab][:, None]
+    q[:, 1] = 0.0
+    q[:, 2] *= 1e-4
+    q = np.asfortranarray(q)
+    scheme = gbg.CatmullRom if width == 4 else gbg.LalescuSpline(6)
+    points = gbg.PointSet(to_dev(pos, dev))
+    got = gbg.anterpolate(grid, points, gbg.VectorPointValues(to_dev(q, dev)), scheme).data.cpu().numpy()
+    want = oracle.scatter(g, np.zeros(n + (3,), order="F"), pos, q, scheme.coefficients)
+    A = _abs_scatter(np.asarray(scheme.coefficients), n, pos, q, TWO_PI / np.array(n))
+    assert np.all(got[..., 1] == 0.0)
+    err = np.abs(got - want)
+    assert np.all(err <= 1e-12 * A), float(np.max(err / np.maximum(A, 1e-300)))
+    # nodes reached only by the smallest slab's points (z cells 24..31): relative error per
+    # node where the sum is not a cancellation
+    half = width // 2
+    zn = np.arange(n[2])
+    small = (zn >= 3 * n[2] // 4 + half) & (zn <= n[2] - half)
+    sel = np.abs(want[:, :, small, 0]) > 1e-3 * A[:, :, small, 0]
+    rel = np.abs(got[:, :, small, 0] - want[:, :, small, 0])[sel] / np.abs(want[:, :, small, 0])[sel]
+    assert rel.size > 100 and rel.max() <= 1e-11
+
+
+def test_scatter_exact_zeros_on_nodes(gbg, oracle, dev):
+    """Points exactly on grid nodes reach their other stencil nodes with weight 0: every
+    node the reference leaves exactly zero stays exactly zero, for either precision."""
+    n = (12, 10, 8)
+    for dtype in (np.float64, np.float32):
+        grid, g = make(gbg, oracle, n=n, dtype=dtype)
+        rng = np.random.default_rng(11)
+        cells = rng.integers(0, 8, size=(200, 3))
+        pos = np.asfortranarray((cells * (TWO_PI / np.array(n))).astype(dtype))
+        q = np.asfortranarray(rng.standard_normal((200, 3)).astype(dtype))
+        points = gbg.PointSet(to_dev(pos, dev))
+        got = gbg.anterpolate(grid, points, gbg.VectorPointValues(to_dev(q, dev)), gbg.CatmullRom).data.cpu().numpy()
+        want = oracle.scatter(g, np.zeros(n + (3,), dtype, order="F"), pos, q, gbg.CatmullRom.coefficients)
+        assert (want == 0).sum() > 0.5 * want.size
+        assert np.all(got[want == 0] == 0)
+        assert relerr(got, want) <= TOL[dtype]

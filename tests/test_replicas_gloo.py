@@ -54,7 +54,8 @@ def test_reference_arm_under_torchrun():
     env = dict(os.environ, OMP_NUM_THREADS="2")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.5"]
+           "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "1", "--shrink", "8",
+           "--cpu-block", "20000"]
     r = subprocess.run(cmd, cwd=ROOT, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -62,3 +63,4 @@ def test_reference_arm_under_torchrun():
     res = json.loads(lines[0])
     assert res["impl"] == "reference" and res["n_gpus"] == 2 and res["value"] > 0
     assert res["cpu_baseline"]["kind"] == "port" and res["e2e"]["h2d_bytes_per_step"] == 0
+    assert res["config"]["grid"] == [64, 64, 64] and res["config"]["points"] == 32_000_000 // 512
