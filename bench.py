@@ -323,7 +323,9 @@ def run_gb300(args, rank, world):
                      "traffic": None, "algorithmic_bytes": alg[dominant], "per_kernel": per_kernel,
                      "note": "achieved = algorithmic bytes / the kernel's CUDA-event time on its stream over the "
                              "timed steps; DRAM traffic per launch is in the committed ncu summaries"},
-        "tuned": {k: tuned[k] for k in ("brick", "gather_threads", "scatter_threads")},
+        "tuned": {**{k: tuned[k] for k in ("brick", "gather_threads", "scatter_threads")},
+                  "trials": [{k: (round(v, 3) if isinstance(v, float) else v) for k, v in t.items()}
+                             for t in tuned["trials"]]},
         "clocks": clk,
         "gpu_launches": int(launches),
     }

@@ -63,10 +63,16 @@ struct gbg_bins_s {
   size_t bytes = 0;
   bool async = false;  // block from cudaMallocAsync (serving loop)
   int32_t gather_threads = 0, scatter_threads = 0;  // 0: the defaults (gbg_bins_set_launch)
+  int32_t compensated = 1;  // the scatter's compensated summation (gbg_bins_set_compensated)
+  uint32_t wait_polls = 0;  // the gather's tile-wait limit, 0: the default (gbg_bins_set_wait_limit)
   // work lists rebuilt with the bins: bricks holding a point (gathers), bricks a point's
   // stencil reaches (scatters with beta == 1; valid when reach_ok), and their lengths
   uint32_t *active = nullptr, *reach = nullptr, *lists_n = nullptr;
   bool reach_ok = false;
+  // corrections of the compensated scatter's regions of several chunks: one slot of
+  // bvol * 12 floats per scatter CTA; the scatter launches at most cslots CTAs
+  float *cscratch = nullptr;
+  int32_t cslots = 1;
 };
 
 namespace gbg {
@@ -86,6 +92,7 @@ inline void bins_layout(Arena &a, gbg_bins_s *b) {
   b->active = a.take<uint32_t>((size_t)b->nbricks);
   b->reach = a.take<uint32_t>((size_t)b->nbricks);
   b->lists_n = a.take<uint32_t>(4);
+  b->cscratch = a.take<float>((size_t)b->cslots * b->bvol * 12);
 }
 }  // namespace gbg
 
@@ -93,6 +100,16 @@ namespace gbg {
 namespace {
 
 constexpr int kThreads = 256;
+// scatter CTAs per SM that a launch may use at most: each owns a slot of the compensated
+// scatter's correction scratch
+constexpr int kScatterSlotsPerSM = 4;
+
+int device_sms() {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) cudaGetLastError();
+  return sms > 0 ? sms : 1;
+}
 
 int padded_components(int ncomp) { return ncomp <= 4 ? 4 : 12; }
 
@@ -408,6 +425,7 @@ struct StagedGeo {
   int32_t box_off;  // halo - n: padded coordinate of a brick's first tile node, less b*brick
   int64_t nbricks, bvol, m;
   int32_t ncomp;
+  uint32_t wait_polls;  // polls of a tile's mbarrier before the wait gives up (kWaitPolls by default)
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -423,16 +441,30 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
-// Bounded wait on a phase of an mbarrier; false if it did not complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Bounded wait on a phase of an mbarrier; false if it did not complete within `polls`
+// tries.  A try of the default limit (kWaitPolls) is mbarrier.try_wait, which may suspend
+// the thread for a while before it answers; below the default every try is the
+// non-blocking mbarrier.test_wait, so that a small limit gives up after about that many
+// polls.  The waits on a tile use the launch's limit; the drain of copies still in flight
+// after a wait gave up always uses the full kWaitPolls, so no copy outlives the CTA.
+constexpr uint32_t kWaitPolls = 1u << 22;
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t polls = kWaitPolls) {
   const uint32_t a = smem_addr(bar);
-  for (int iter = 0; iter < (1 << 22); ++iter) {
+  const bool block = polls >= kWaitPolls;
+  for (uint32_t iter = 0; iter < polls; ++iter) {
     uint32_t done;
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
+    if (block)
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(a), "r"(parity)
+          : "memory");
+    else
+      asm volatile(
+          "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+          : "=r"(done)
+          : "r"(a), "r"(parity)
+          : "memory");
     if (done) return true;
   }
   return false;
@@ -543,9 +575,11 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
   uint32_t phase[2] = {0, 0};
   bool failed = false;
 
+  bool pending[2] = {false, false};  // thread 0's copies issued and not yet waited for
   auto issue = [&](int64_t b, int buf) {
     int64_t bx, by, bz;
     brick_coords(g, b, bx, by, bz);
+    pending[buf] = true;
     mbar_expect_tx(bars + buf, box_bytes);
     tma_load_tile(smem + buf * tile_bytes, &tmap, 0, (int)(bx * g.b[0]) + g.box_off,
                   (int)(by * g.b[1]) + g.box_off, (int)(bz * g.b[2]) + g.box_off, bars + buf);
@@ -564,12 +598,13 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
-      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
+      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf], g.wait_polls))) {
         failed = true;
         if (threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_TIMEOUT);
         break;
       }
       phase[buf] ^= 1;
+      pending[buf] = false;
       const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
       uint32_t sl = s0 + qw;
       float4 r_next = sl < s1 ? __ldg(rec + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -655,9 +690,11 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     __syncthreads();  // every lane is done with this buffer before it is refilled
     if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
   }
-  if (failed) {
-    // a copy that never completed: give any other in-flight copy a bounded chance to land
-    for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
+  if (failed && threadIdx.x == 0) {
+    // a copy that did not complete in time: let every copy still in flight land (with the
+    // full limit) before the CTA's shared memory is released
+    for (int i = 0; i < nbuf; ++i)
+      if (pending[i]) mbar_wait(bars + i, phase[i]);
   }
 }
 
@@ -678,9 +715,11 @@ __global__ void __launch_bounds__(kThreads, 1)
   __syncthreads();
   uint32_t phase[2] = {0, 0};
   bool failed = false;
+  bool pending[2] = {false, false};  // thread 0's copies issued and not yet waited for
   auto issue = [&](int64_t b, int buf) {
     int64_t bx, by, bz;
     brick_coords(g, b, bx, by, bz);
+    pending[buf] = true;
     mbar_expect_tx(bars + buf, box_bytes);
     tma_load_tile(smem + buf * tile_bytes, &tmap, 0, (int)(bx * g.b[0]) + g.box_off,
                   (int)(by * g.b[1]) + g.box_off, (int)(bz * g.b[2]) + g.box_off, bars + buf);
@@ -698,12 +737,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
-      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf]))) {
+      if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf], g.wait_polls))) {
         failed = true;
         if (threadIdx.x == 0 && status) atomicOr(status, GBG_DEV_TIMEOUT);
         break;
       }
       phase[buf] ^= 1;
+      pending[buf] = false;
       const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
       for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += blockDim.x) {
         const float4 r = __ldg(rec + sl);
@@ -750,8 +790,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncthreads();
     if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
   }
-  if (failed)
-    for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
+  if (failed && threadIdx.x == 0)
+    for (int i = 0; i < nbuf; ++i)
+      if (pending[i]) mbar_wait(bars + i, phase[i]);
 }
 
 // ------------------------------------------------------------ staged scatter
@@ -782,6 +823,15 @@ __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__rest
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
+// One compensated step (Knuth's TwoSum, every operation rounded on its own): s + x into
+// the pair (s, c), c collecting the exact rounding error of each addition.
+__device__ __forceinline__ void twosum_add(float &s, float &c, float x) {
+  const float t = __fadd_rn(s, x);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(x, z)));
+  s = t;
+}
+
 struct FixGeo {
   int32_t b[3];
   int32_t nb[3];
@@ -793,6 +843,9 @@ struct FixGeo {
   int32_t neighbour_skip;  // every brick edge >= width/2: the region lies in the 27 neighbouring bricks
   int32_t chunk;           // points staged in shared memory at a time (a multiple of 4)
   int32_t chunk1;          // the same when the region's points fit at once (no running sums kept)
+  int32_t comp;            // compensated: chunk partial sums folded into (sum, correction) by TwoSum
+  float *cscratch;         // corrections of regions of several chunks: one slot per CTA
+  int64_t cstride;         // floats per slot (>= bvol * CP)
 };
 
 // All N2 weights from coefficients in memory ([q + N2*p], M2 == N2 powers).
@@ -820,7 +873,8 @@ __device__ __forceinline__ void weights_rt(const float *c, int m2, float t, floa
 // Shared memory of one scatter CTA, in this order: the brick's running sums (CP floats per
 // node), one chunk of the region's points (CP quantities and 3*N2+4 weights each), the
 // region's per-cell point offsets (+ the total) and first slots, the per-axis key tables
-// of the region's cells, and the points' region x cells.
+// of the region's cells, and the points' region x cells.  (With compensation, a region of
+// several chunks keeps its sums' corrections in the CTA's own slot of a global scratch.)
 size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
   const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
   return sizeof(float) * (size_t)g.bvol * cp + sizeof(uint32_t) * (2 * ecount + 1 + (size_t)(g.e[0] + g.e[1] + g.e[2])) +
@@ -890,6 +944,9 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   const int bvol = (int)g.bvol;
   // [running sums | chunk: quantities, weights] [offsets, first slots, key tables] [x cells]
   float *sacc = reinterpret_cast<float *>(smem);
+  // compensation terms of the running sums (regions of several chunks only): this CTA's slot
+  // of the global scratch
+  float *scmp = g.cscratch + (size_t)blockIdx.x * g.cstride;
   uint32_t *off = reinterpret_cast<uint32_t *>(sacc + bvol * CP + g.chunk * (CP + kScatterWStride<N2>));
   uint32_t *r0s = off + ecount + 1;
   uint32_t *kx = r0s + ecount, *ky = kx + E0, *kz = ky + E1;
@@ -1057,7 +1114,10 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
 #pragma unroll
         for (int v = 0; v < CP / 4; ++v) {
           float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
-          if (!first && mine) s4 = reinterpret_cast<const float4 *>(sacc + (((lz + bb) * B1 + ly + a) * B0 + lx) * CP)[v];
+          // plain sums carry the running sum from chunk to chunk; compensated ones start each
+          // chunk at zero and fold it in at the chunk's end
+          if (!first && mine && !g.comp)
+            s4 = reinterpret_cast<const float4 *>(sacc + (((lz + bb) * B1 + ly + a) * B0 + lx) * CP)[v];
           acc[n][4 * v] = s4.x;
           acc[n][4 * v + 1] = s4.y;
           acc[n][4 * v + 2] = s4.z;
@@ -1172,6 +1232,22 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
         const int a = n % BY, bb = n / BY;
         const int ny = ly + a, nz = lz + bb;
         if (ny >= B1 || nz >= g.b[2]) continue;  // past the brick (odd edge)
+        if (g.comp && !first) {
+          // fold this chunk's partial sums into the node's (sum, correction)
+          float *sp = sacc + ((nz * B1 + ny) * B0 + lx) * CP, *cp2 = scmp + ((nz * B1 + ny) * B0 + lx) * CP;
+#pragma unroll
+          for (int c = 0; c < CP; ++c) {
+            float sum = sp[c], cor = cp2[c];
+            twosum_add(sum, cor, acc[n][c]);
+            if (last) {
+              acc[n][c] = __fadd_rn(sum, cor);
+            } else {
+              sp[c] = sum;
+              cp2[c] = cor;
+            }
+          }
+          if (!last) continue;
+        }
         if (last) {
           if (lx >= vx || ny >= vy || nz >= vz) continue;  // past the grid (last brick)
           const int64_t x = (int64_t)bx * B0 + lx, y = (int64_t)by * B1 + ny, z = (int64_t)bz * g.b[2] + nz;
@@ -1191,9 +1267,11 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
           }
         } else {
 #pragma unroll
-          for (int v = 0; v < CP / 4; ++v)
+          for (int v = 0; v < CP / 4; ++v) {
             reinterpret_cast<float4 *>(sacc + ((nz * B1 + ny) * B0 + lx) * CP)[v] =
                 make_float4(acc[n][4 * v], acc[n][4 * v + 1], acc[n][4 * v + 2], acc[n][4 * v + 3]);
+            if (g.comp) reinterpret_cast<float4 *>(scmp + ((nz * B1 + ny) * B0 + lx) * CP)[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+          }
         }
       }
     }
@@ -1256,6 +1334,7 @@ StagedGeo staged_geo(const gbg_field_s *f, const gbg_bins_s *b, int width) {
   g.bvol = b->bvol;
   g.m = b->npoints;
   g.ncomp = f->ncomp;
+  g.wait_polls = b->wait_polls ? b->wait_polls : kWaitPolls;
   return g;
 }
 
@@ -1332,6 +1411,9 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     g.e[d] = b->b[d] + N2 - 1;
   }
   g.neighbour_skip = neighbour_skip_ok(b->b, b->nb, f->grid.n, N2);
+  g.comp = b->compensated;
+  g.cscratch = b->cscratch;
+  g.cstride = b->bvol * 12;
   g.nbricks = b->nbricks;
   g.bvol = b->bvol;
   g.px = f->px;
@@ -1355,7 +1437,7 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-    const int blocks = (int)std::min<int64_t>(b->nbricks, (int64_t)sms * std::max(per_sm, 1));
+    const int blocks = (int)std::min<int64_t>(b->cslots, (int64_t)sms * std::max(per_sm, 1));
     mark_main_start(st);
     const bool reach = beta == 1.0 && b->reach_ok;
     kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
@@ -1597,8 +1679,9 @@ __global__ void __launch_bounds__(kBatchGatherThreads, 1)
       buf ^= 1;
     }
   }
-  if (failed)
-    for (int i = 0; i < nbuf; ++i) mbar_wait(bars + i, phase[i]);
+  if (failed && threadIdx.x == 0)
+    for (int i = 0; i < nbuf; ++i)
+      if (s_issued[i]) mbar_wait(bars + i, phase[i]);
 }
 
 // The scatter of every listed brick of every instance: units taken from the device counter.
@@ -1717,6 +1800,7 @@ gbg_status bins_plan(const gbg_grid &grid, int64_t max_points, const int32_t *br
   b->nkeys = b->nbricks * b->bvol;
   if (b->nkeys >= (int64_t(1) << 32) - 1) return set_error(GBG_EUNSUPPORTED, "bins: 2^32 or more cells");
   b->reach_ok = neighbour_skip_ok(b->b, b->nb, grid.n, 8) != 0;
+  b->cslots = (int32_t)std::min<int64_t>(b->nbricks, (int64_t)kScatterSlotsPerSM * device_sms());
   Arena a;
   bins_layout(a, b);
   b->bytes = a.used + 256;
@@ -1869,6 +1953,20 @@ gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32
   bins_carve(b);
   cudaMemset(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1));
   *out = b;
+  return GBG_OK;
+}
+
+gbg_status gbg_bins_set_wait_limit(gbg_bins b, uint32_t polls) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  b->wait_polls = polls;
+  return GBG_OK;
+}
+
+gbg_status gbg_bins_set_compensated(gbg_bins b, int32_t compensated) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  b->compensated = compensated ? 1 : 0;
   return GBG_OK;
 }
 
@@ -2160,6 +2258,11 @@ struct gbg_batch_s {
   void *block = nullptr;  // the device tables, one allocation
   size_t bytes = 0;
   bool async = false;     // block from cudaMallocAsync (serving loop)
+  // corrections of the pooled scatter's compensated regions of several chunks: cslots
+  // slots of cstride floats, one per scatter CTA (a separate allocation, never staged)
+  float *cscratch = nullptr;
+  int64_t cstride = 0;
+  int32_t cslots = 0;
 };
 
 namespace gbg {
@@ -2295,6 +2398,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
         d.fg.e[k] = b->b[k] + w - 1;
       }
       d.fg.neighbour_skip = neighbour_skip_ok(b->b, b->nb, ds->grid.n, w);
+      d.fg.comp = b->compensated;
       d.fg.nbricks = b->nbricks;
       d.fg.bvol = b->bvol;
       d.fg.px = ds->px;
@@ -2304,6 +2408,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
       d.fg.ncomp = ds->ncomp;
       scatter_nodes_chunk(d.fg, ds->cp, w, scatter_nodes_budget(scat_fa.numRegs, kThreads, d.fg, ds->cp, w));
       scat_max = std::max(scat_max, scatter_nodes_smem(d.fg, ds->cp, w));
+      bt->cstride = std::max<int64_t>(bt->cstride, b->bvol * 12);
       if (d.fg.e[0] > 255) return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");
       h.qptrs[i] = it.q;
       h.qs_out[i] = b->qs;
@@ -2361,6 +2466,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   if (bt->gather_smem > 227 * 1024 || bt->scatter_smem > 227 * 1024)
     return set_error(GBG_EUNSUPPORTED, "batch: a brick's tile does not fit in shared memory");
   bt->bytes = batch_layout(count).bytes;
+  bt->cslots = ns ? (int32_t)std::min<uint64_t>(ns, (uint64_t)kScatterSlotsPerSM * device_sms()) : 0;
   return GBG_OK;
 }
 
@@ -2387,7 +2493,14 @@ void batch_fill(gbg_batch_s *bt, const BatchHost &h, char *image) {
   put(bt->qmax_out, L.qmax_out, h.qmax_out.data(), sizeof(unsigned *) * n);
   put(bt->alphas, L.alphas, h.alphas.data(), sizeof(float) * n);
   put(bt->qoff, L.qoff, h.qoff.data(), sizeof(int64_t) * (n + 1));
+  BatchDev *items = reinterpret_cast<BatchDev *>(image + L.items);
+  for (int32_t i = 0; i < n; ++i) {
+    items[i].fg.cscratch = bt->cscratch;
+    items[i].fg.cstride = bt->cstride;
+  }
 }
+
+size_t batch_scratch_bytes(const gbg_batch_s *bt) { return sizeof(float) * (size_t)bt->cslots * bt->cstride; }
 
 gbg_status batch_create_async(const gbg_batch_item *items, int32_t count, cudaStream_t stream, void *pinned,
                               size_t pinned_bytes, gbg_batch *out) {
@@ -2414,10 +2527,17 @@ gbg_status batch_create_async(const gbg_batch_item *items, int32_t count, cudaSt
     return set_error(GBG_ENOMEM, "batch: cudaMallocAsync failed");
   }
   bt->async = true;
+  if (bt->cslots && cudaMallocAsync(&bt->cscratch, batch_scratch_bytes(bt), stream) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFreeAsync(bt->block, stream);
+    delete bt;
+    return set_error(GBG_ENOMEM, "batch: cudaMallocAsync of the scatter scratch failed");
+  }
   batch_fill(bt, h, static_cast<char *>(pinned));
   const cudaError_t e = cudaMemcpyAsync(bt->block, pinned, bt->bytes, cudaMemcpyHostToDevice, stream);
   if (e != cudaSuccess) {
     cudaFreeAsync(bt->block, stream);
+    if (bt->cscratch) cudaFreeAsync(bt->cscratch, stream);
     delete bt;
     return set_error(GBG_ECUDA, std::string("batch: copy failed: ") + cudaGetErrorString(e));
   }
@@ -2429,7 +2549,11 @@ size_t batch_table_bytes(int32_t count) { return batch_layout(count).bytes; }
 
 gbg_status batch_destroy_async(gbg_batch bt, cudaStream_t stream) {
   if (!bt) return GBG_OK;
-  const cudaError_t e = !bt->block ? cudaSuccess : bt->async ? cudaFreeAsync(bt->block, stream) : cudaFree(bt->block);
+  cudaError_t e = !bt->block ? cudaSuccess : bt->async ? cudaFreeAsync(bt->block, stream) : cudaFree(bt->block);
+  if (bt->cscratch) {
+    const cudaError_t e2 = bt->async ? cudaFreeAsync(bt->cscratch, stream) : cudaFree(bt->cscratch);
+    if (e == cudaSuccess) e = e2;
+  }
   delete bt;
   if (e != cudaSuccess) return set_error(GBG_ECUDA, std::string("freeing the batch: ") + cudaGetErrorString(e));
   return GBG_OK;
@@ -2463,11 +2587,18 @@ gbg_status gbg_batch_create(const gbg_batch_item *items, int32_t count, gbg_batc
     delete bt;
     return set_error(GBG_ENOMEM, "batch: cudaMalloc failed");
   }
+  if (bt->cslots && cudaMalloc(&bt->cscratch, batch_scratch_bytes(bt)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(bt->block);
+    delete bt;
+    return set_error(GBG_ENOMEM, "batch: cudaMalloc of the scatter scratch failed");
+  }
   std::vector<char> image(bt->bytes);
   batch_fill(bt, h, image.data());
   const cudaError_t e = cudaMemcpy(bt->block, image.data(), bt->bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     cudaFree(bt->block);
+    if (bt->cscratch) cudaFree(bt->cscratch);
     delete bt;
     return set_error(GBG_ECUDA, std::string("batch: copy failed: ") + cudaGetErrorString(e));
   }
@@ -2514,7 +2645,7 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
     GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_scatter, kThreads, bt->scatter_smem);
-    const int blocks = (int)std::min<uint32_t>(bt->nswork, (uint32_t)(std::max(per_sm, 1) * sms));
+    const int blocks = (int)std::min<uint32_t>((uint32_t)bt->cslots, (uint32_t)(std::max(per_sm, 1) * sms));
     k_batch_scatter<<<blocks, kThreads, bt->scatter_smem, st>>>(bt->items, bt->soff, bt->sidx, bt->ns,
                                                                 bt->counters + 1, device_status);
     note_launch();

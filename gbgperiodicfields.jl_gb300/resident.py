@@ -130,6 +130,18 @@ class PointBins:
                                                 out.data_ptr(), _stream()), "gbg_bins_permute")
         return out
 
+    def set_compensated(self, on: bool = True):
+        """Compensated summation of chunk partial sums in the binned scatter (the default) or
+        one plain FP32 running sum per node (gbg_bins_set_compensated)."""
+        _lib.check(_lib.load().gbg_bins_set_compensated(self.handle, int(bool(on))), "gbg_bins_set_compensated")
+        return self
+
+    def set_wait_limit(self, polls: int = 0):
+        """Polls of a staged tile's barrier before the binned gather gives up on it (0 = the
+        default; gbg_bins_set_wait_limit)."""
+        _lib.check(_lib.load().gbg_bins_set_wait_limit(self.handle, int(polls)), "gbg_bins_set_wait_limit")
+        return self
+
     def order(self) -> torch.Tensor:
         o = torch.empty(self.npoints, dtype=torch.int32, device="cuda")
         _lib.check(_lib.load().gbg_bins_order(self.handle, o.data_ptr(), _stream()), "gbg_bins_order")

@@ -249,6 +249,20 @@ gbg_status gbg_bins_permute(gbg_bins bins, gbg_dtype dtype, int32_t ncols, const
  * the brick edges.  Each CTA works through whole bricks; the grid is sized from the
  * occupancy the choice allows.  No counterpart in the reference. */
 gbg_status gbg_bins_set_launch(gbg_bins bins, int32_t gather_threads, int32_t scatter_threads);
+/* Compensated summation in gbg_anterpolate_binned on these bins: 1 (the default) sums each
+ * node in FP32 over every chunk of at most 1024 of its brick region's points and folds the
+ * chunk sums into a running (sum, correction) pair by TwoSum (the corrections live in a
+ * per-CTA slot of the bins' device block); 0 carries one plain FP32 running sum.  A region
+ * that fits in one chunk is summed the same way either way.  No counterpart in the
+ * reference, whose scatter sums in its field's own precision. */
+gbg_status gbg_bins_set_compensated(gbg_bins bins, int32_t compensated);
+/* Polls of a staged tile's mbarrier before gbg_interpolate_binned gives up on it (0 = the
+ * default, 2^22 suspending polls; a smaller limit polls without suspending): the wait then
+ * sets GBG_DEV_TIMEOUT, the CTA lets its copies land (always with the full limit) and
+ * returns, leaving that tile's points unwritten.  A failure-path control with no
+ * counterpart in the reference; a tiny limit makes the wait run out on purpose, which is
+ * how the timeout path is tested. */
+gbg_status gbg_bins_set_wait_limit(gbg_bins bins, uint32_t polls);
 /* Bins the points: each position is wrapped periodically and split into a cell index
  * and a fractional offset in the positions' own precision (FP64 positions keep FP64
  * for this step), then the points are stably sorted by brick and cell on the device.

@@ -148,3 +148,62 @@ def test_nonfinite_quantity_is_reported(gbg, oracle, dev):
     resident.anterpolate_binned(field, bins, gbg.CatmullRom, torch.from_numpy(q).cuda(), 1.0, 0.0, status=status)
     torch.cuda.synchronize()
     assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE
+
+
+def test_compensated_scatter_at_high_coverage(gbg, oracle, dev):
+    """Thousands of points per cell (400000 points in eight neighbouring cells): every node
+    sums of order 10^5 contributions of one sign.  One plain FP32 running sum per node
+    drifts with the number of terms; compensated summation of the chunk sums stays at the
+    FP32 rounding of the weights and quantities.  Errors against the FP64 oracle, relative
+    to max|oracle| (the precision form's bar is 1e-5)."""
+    from gbgperiodicfields_gb300 import resident
+    grid = gbg.Grid3D((16, 16, 16), (TWO_PI,) * 3)
+    g = oracle.grid_dict(grid.grid_size, grid.domain_size, grid.origin)
+    rng = np.random.default_rng(31)
+    m = 400_000
+    h = TWO_PI / 16
+    cells = rng.integers(6, 8, size=(m, 3))
+    pos = np.asfortranarray((cells + rng.random((m, 3))) * h)
+    q = np.asfortranarray(1.0 + 0.1 * rng.standard_normal((m, 3)))
+    want = oracle.scatter(g, np.zeros((16, 16, 16, 3), order="F"), pos, q, gbg.CatmullRom.coefficients)
+    field = resident.ResidentField(grid, 3, max_stencil_width=4)
+    bins = resident.PointBins(grid, m).build(torch.from_numpy(pos).cuda())
+    qt = torch.from_numpy(q).cuda()
+    errs = {}
+    for comp in (True, False):
+        bins.set_compensated(comp)
+        resident.anterpolate_binned(field, bins, gbg.CatmullRom, qt, 1.0, 0.0)
+        errs[comp] = relerr(field.read().cpu().numpy(), want)
+    assert errs[True] <= 1e-6, errs
+    assert errs[True] * 10 <= errs[False], errs
+
+
+def test_compensation_leaves_single_chunk_regions_unchanged(gbg, oracle, dev):
+    """At ordinary densities every brick region fits in one chunk: the compensated and the
+    plain scatter give the same bits."""
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (32, 24, 20), 12, 3000, 61)
+    qt = torch.from_numpy(q).cuda()
+    out = []
+    for comp in (True, False):
+        bins.set_compensated(comp)
+        resident.anterpolate_binned(field, bins, gbg.CatmullRom, qt, 1.0, 0.0)
+        out.append(field.read())
+    assert torch.equal(out[0], out[1])
+
+
+def test_bounded_tile_wait_reports_timeout(gbg, oracle, dev):
+    """A staged gather whose tile wait is allowed a single poll gives up on tiles still in
+    flight: the status word says GBG_DEV_TIMEOUT, the call returns, and the context stays
+    usable -- with the default limit the next gather matches the oracle."""
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (48, 40, 32), 12, 40000, 71)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    bins.set_wait_limit(1)
+    resident.interpolate_binned(field, bins, gbg.CatmullRom, status=status)
+    torch.cuda.synchronize()
+    assert int(status.item()) & gbg._lib.GBG_DEV_TIMEOUT
+    bins.set_wait_limit(0)
+    status.zero_()
+    got = resident.interpolate_binned(field, bins, gbg.CatmullRom, dtype=torch.float64, status=status).cpu().numpy()
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert relerr(got, oracle.gather(g, f, pos, gbg.CatmullRom.coefficients)) <= 1e-5
