@@ -15,9 +15,12 @@ from .api import (AbstractFieldPhysical, AbstractPointValues, Grid3D, LagrangeSp
                   field_data, field_grid, interpolate, interpolate_, npoints, point_positions,
                   point_traversal_order, point_traversal_order_, point_values, sample_field, wrap_,
                   zeros_colmajor)
-from .nufft import (NUFFT, AbstractFieldSpectral, FieldTransformPlans, RealFourierLayout, ScalarFieldSpectral,
-                    TensorFieldSpectral, VectorFieldSpectral, field_layout, field_spectral_shape, to_physical,
-                    to_spectral)
+from .nufft import (NUFFT, AbstractFieldSpectral, DirectDFT, FieldTransformPlans, RealFourierLayout,
+                    ScalarFieldSpectral, TensorFieldSpectral, VectorFieldSpectral, field_layout, field_spectral_shape,
+                    to_physical, to_spectral)
+from .checkpoint import (read_field, read_field_, read_points, read_scheme, write_field, write_points,
+                         write_scheme)
+from .h5 import h5open
 
 
 def __getattr__(name):

@@ -509,7 +509,7 @@ def interpolate_(out: AbstractPointValues, field: AbstractFieldPhysical, points:
     """interpolate! (Interpolation.jl:1181-1198): out = field sampled at points.  A
     field in spectral representation with a NUFFT scheme goes to the NUFFT path."""
     from . import nufft as _nufft
-    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+    if isinstance(scheme, (_nufft.NUFFT, _nufft.DirectDFT)) or isinstance(field, _nufft.AbstractFieldSpectral):
         return _nufft.dispatch_interpolate_(out, field, points, scheme, traversal)
     if out.tensor_order != field.tensor_order:
         raise ArgumentError(f"output tensor order {out.tensor_order} must equal field tensor order {field.tensor_order}")
@@ -536,7 +536,7 @@ def interpolate(field: AbstractFieldPhysical, points: PointSet, scheme,
                 traversal: Optional[PointTraversalOrder] = None) -> AbstractPointValues:
     """Allocating form of interpolate! (Interpolation.jl:1212-1217)."""
     from . import nufft as _nufft
-    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+    if isinstance(scheme, (_nufft.NUFFT, _nufft.DirectDFT)) or isinstance(field, _nufft.AbstractFieldSpectral):
         return _nufft.dispatch_interpolate(field, points, scheme, traversal)
     data = empty_colmajor((points.npoints,) + (3,) * field.tensor_order, field.data.dtype, points.device)
     return interpolate_(AbstractPointValues(data, field.tensor_order), field, points, scheme, traversal)
@@ -551,7 +551,7 @@ def anterpolate_(field: AbstractFieldPhysical, points: PointSet, quantities: Abs
     if alpha is None:
         alpha, beta = 1.0, 0.0
     from . import nufft as _nufft
-    if isinstance(scheme, _nufft.NUFFT) or isinstance(field, _nufft.AbstractFieldSpectral):
+    if isinstance(scheme, (_nufft.NUFFT, _nufft.DirectDFT)) or isinstance(field, _nufft.AbstractFieldSpectral):
         return _nufft.dispatch_anterpolate_(field, points, quantities, scheme, alpha, beta, traversal)
     if field.tensor_order != quantities.tensor_order:
         raise ArgumentError(f"field tensor order {field.tensor_order} must equal quantities tensor order {quantities.tensor_order}")

@@ -1463,27 +1463,18 @@ gbg_status gbg_anterpolate(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
 //
 // The scratch of gbg_anterpolate_noalloc: one fixed array per device, part of this
 // library's device image, so the entry point never allocates.  Host code must not pass
-// the array's name to a kernel (on the host it names a host-side stand-in); its device
-// address is looked up once per device with that device current.
+// the array's name to a kernel (on the host it names a host-side stand-in).  Its device
+// address is looked up on every call, in the context current at the call: an address
+// kept from an earlier call would be stale after a device reset or in another context.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[GBG_NOALLOC_SCRATCH_BYTES];
 
 static gbg_status noalloc_scratch(void **out) {
-  constexpr int kMaxDevices = 64;
-  static std::mutex mu;
-  static void *addr[kMaxDevices] = {};
-  int dev = 0;
-  GBG_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return set_error(GBG_EUNSUPPORTED, "device ordinal above 63");
-  std::lock_guard<std::mutex> lock(mu);
-  if (!addr[dev]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return set_error(GBG_ECUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
-                                      cudaGetErrorString(e));
-    addr[dev] = p;
-  }
-  *out = addr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return set_error(GBG_ECUDA, std::string("cudaGetSymbolAddress of the static scratch failed: ") +
+                                    cudaGetErrorString(e));
+  *out = p;
   return GBG_OK;
 }
 

@@ -419,6 +419,38 @@ def anterpolate_nufft(grid: Grid3D, points: PointSet, quantities: AbstractPointV
                               traversal=traversal)
 
 
+# ------------------------------------------------ the exact spectral scheme, as a record
+
+
+class DirectDFT:
+    """The reference's exact spectral transfer scheme (src/Interpolation.jl:1382-1433), a
+    parameterless singleton.  This package carries it as a scheme record -- it round-trips
+    through write_scheme/read_scheme, so checkpoints that name it stay readable -- but the
+    exact O(N*M) Fourier transfer itself is outside the accelerated path: a transfer with
+    it raises MethodError (NUFFT is the fast transfer for spectral fields)."""
+    _instance = None
+
+    def __new__(cls):
+        if cls._instance is None:
+            cls._instance = super().__new__(cls)
+        return cls._instance
+
+    def __eq__(self, other):
+        return isinstance(other, DirectDFT)
+
+    def __hash__(self):
+        return hash("DirectDFT")
+
+    def __repr__(self):
+        return "DirectDFT()"
+
+
+def _refuse_direct_dft(scheme):
+    if isinstance(scheme, DirectDFT):
+        raise MethodError("DirectDFT, the exact O(N*M) Fourier transfer, is not provided by this package; "
+                          "use a NUFFT scheme for a field in spectral representation")
+
+
 # ------------------------------------------------ dispatch from the generic entry points
 
 
@@ -428,18 +460,21 @@ def _refuse_mixed():
 
 
 def dispatch_interpolate_(out, field, points, scheme, traversal):
+    _refuse_direct_dft(scheme)
     if not (isinstance(field, AbstractFieldSpectral) and isinstance(scheme, NUFFT)):
         _refuse_mixed()
     return interpolate_nufft_(out, field, points, scheme, traversal)
 
 
 def dispatch_interpolate(field, points, scheme, traversal):
+    _refuse_direct_dft(scheme)
     if not (isinstance(field, AbstractFieldSpectral) and isinstance(scheme, NUFFT)):
         _refuse_mixed()
     return interpolate_nufft(field, points, scheme, traversal)
 
 
 def dispatch_anterpolate_(field, points, quantities, scheme, alpha, beta, traversal):
+    _refuse_direct_dft(scheme)
     if not (isinstance(field, AbstractFieldSpectral) and isinstance(scheme, NUFFT)):
         _refuse_mixed()
     return anterpolate_nufft_(field, points, quantities, scheme, alpha, beta, traversal)

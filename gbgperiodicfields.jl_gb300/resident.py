@@ -72,6 +72,10 @@ class PointBins:
         self.handle = h
         self.npoints = 0
         self.status = None
+        # the configuration a checkpoint records (the binned order itself is derived data)
+        self.brick = tuple(int(v) for v in brick) if brick is not None else None
+        self.gather_threads = self.scatter_threads = 0
+        self.compensated = True
 
     def __del__(self):
         h = getattr(self, "handle", None)
@@ -134,6 +138,7 @@ class PointBins:
         """Compensated summation of chunk partial sums in the binned scatter (the default) or
         one plain FP32 running sum per node (gbg_bins_set_compensated)."""
         _lib.check(_lib.load().gbg_bins_set_compensated(self.handle, int(bool(on))), "gbg_bins_set_compensated")
+        self.compensated = bool(on)
         return self
 
     def set_wait_limit(self, polls: int = 0):

@@ -156,11 +156,12 @@ gbg_status gbg_anterpolate_workspace_size(const gbg_grid *grid, gbg_dtype dtype,
  * GPU's memory up front through its own pool, and a caller held to the reference's
  * in-place contract that anterpolate! allocates nothing (test/allocations.jl:335-361).
  * A problem whose scratch (gbg_anterpolate_workspace_size) exceeds the array is
- * refused with GBG_EUNSUPPORTED.  The first call on a device looks up the array's
- * device address (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  Every call shares the one array: calls that overlap on
- * the GPU (different streams, or different host threads, on the same device) race and
- * must be serialized by the caller. */
+ * refused with GBG_EUNSUPPORTED.  Every call looks up the array's device address
+ * (cudaGetSymbolAddress) in the context current at the call, so the address is never
+ * stale after a device reset; the first call on a device may load the library's device
+ * image, so make it before any stream capture.  Every call shares the one array: calls
+ * that overlap on the GPU (different streams, or different host threads, on the same
+ * device) race and must be serialized by the caller. */
 #define GBG_NOALLOC_SCRATCH_BYTES ((size_t)64 << 20)
 gbg_status gbg_anterpolate_noalloc(const gbg_grid *grid, gbg_dtype dtype, int32_t ncomp,
                                    void *field, const void *positions, int64_t npoints,
