@@ -903,18 +903,19 @@ void scatter_nodes_chunk(FixGeo &g, int cp, int n2, size_t budget) {
   g.chunk1 = g.chunk + (int32_t)(((size_t)g.bvol * cp * sizeof(float) / per) & ~size_t(3));
 }
 
-// Shared memory per scatter CTA: the SM's share for as many CTAs as the kernel's registers
-// allow (at most 4), less the block's reserved and static share -- but never so little
-// that a region of 512 points needs more than one chunk (a brick's region holds a few
-// hundred at the usual densities, and each extra chunk re-stages and re-walks the rows;
-// a single chunk may also use the running sums' space).
-size_t scatter_nodes_budget(int regs, int threads, const FixGeo &g, int cp, int n2) {
+// Shared memory per scatter CTA: half an SM's (two CTAs per SM) less the block's reserved
+// and static share, or more when a region of 512 points would not fit one chunk (a brick's
+// region holds a few hundred at the usual densities, and each extra chunk re-stages and
+// re-walks the rows; a single chunk may also use the running sums' space).  It depends on
+// the brick's geometry alone, never on the launch shape: the chunks are where the
+// compensated summation folds its partial sums, so the same chunks for every launch keep
+// the results bitwise independent of the threads per CTA and of batching.
+size_t scatter_nodes_budget(const FixGeo &g, int cp, int n2) {
   const size_t per = sizeof(float) * (cp + scatter_wstride(n2)) + 1;
   const size_t sums = sizeof(float) * (size_t)g.bvol * cp;
   const size_t want = scatter_nodes_fixed(g, cp) + (512 * per > sums ? 512 * per - sums : 0) + 4 * per;
-  int ctas = std::max(1, std::min(4, 65536 / std::max(1, regs * threads)));
-  while (ctas > 1 && 228 * 1024 / ctas - 4096 < want) --ctas;
-  return std::min<size_t>(200 * 1024, 228 * 1024 / ctas - 4096);
+  const size_t half = 228 * 1024 / 2 - 4096;
+  return want <= half ? half : std::min<size_t>(200 * 1024, 228 * 1024 - 4096);
 }
 
 // Deterministic scatter, output-driven.  A CTA owns a brick's nodes and a thread owns a
@@ -1428,9 +1429,7 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int threads = b->scatter_threads ? b->scatter_threads : kThreads;
   auto go = [&](auto kernel) -> gbg_status {
-    cudaFuncAttributes fa{};
-    GBG_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
-    scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(fa.numRegs, threads, g, f->cp, N2));
+    scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(g, f->cp, N2));
     const size_t smem = scatter_nodes_smem(g, f->cp, N2);
     if (smem > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared memory");
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2358,8 +2357,6 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   std::vector<double> cost(count);
   uint32_t buf_max = 0;
   size_t scat_max = 0;
-  cudaFuncAttributes scat_fa{};
-  cudaFuncGetAttributes(&scat_fa, k_batch_scatter);
   for (int32_t i = 0; i < count; ++i) {
     const gbg_batch_item &it = items[i];
     gbg_field_s *f = it.field;
@@ -2406,7 +2403,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
       d.fg.halo = ds->halo;
       d.fg.cp = ds->cp;
       d.fg.ncomp = ds->ncomp;
-      scatter_nodes_chunk(d.fg, ds->cp, w, scatter_nodes_budget(scat_fa.numRegs, kThreads, d.fg, ds->cp, w));
+      scatter_nodes_chunk(d.fg, ds->cp, w, scatter_nodes_budget(d.fg, ds->cp, w));
       scat_max = std::max(scat_max, scatter_nodes_smem(d.fg, ds->cp, w));
       bt->cstride = std::max<int64_t>(bt->cstride, b->bvol * 12);
       if (d.fg.e[0] > 255) return set_error(GBG_EUNSUPPORTED, "batch: brick too large for the scatter");

@@ -191,6 +191,25 @@ def test_compensation_leaves_single_chunk_regions_unchanged(gbg, oracle, dev):
     assert torch.equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("comp", [True, False], ids=["compensated", "plain"])
+def test_multi_chunk_scatter_is_independent_of_the_launch_shape(gbg, oracle, dev, comp):
+    """Dense points make every brick region span several chunks; the chunks, and so where
+    the compensated summation folds, depend on the brick alone, so every threads-per-CTA
+    choice gives the same bits -- and both stay within the precision form's bar."""
+    resident, grid, g, f, pos, q, field, bins = setup(gbg, oracle, (24, 20, 16), 12, 120000, 83)
+    bins.set_compensated(comp)
+    qt = torch.from_numpy(q).cuda()
+    outs = []
+    for threads in (0, 64, 128, 256):
+        bins.set_launch(0, threads)
+        resident.anterpolate_binned(field, bins, gbg.CatmullRom, qt, 1.0, 0.0)
+        outs.append(field.read())
+    for o in outs[1:]:
+        assert torch.equal(o, outs[0])
+    want = oracle.scatter(g, np.zeros(grid.grid_size + (12,), order="F"), pos, q, gbg.CatmullRom.coefficients)
+    assert relerr(outs[0].cpu().numpy(), want) <= 1e-5
+
+
 def test_bounded_tile_wait_reports_timeout(gbg, oracle, dev):
     """A staged gather whose tile wait is allowed a single poll gives up on tiles still in
     flight: the status word says GBG_DEV_TIMEOUT, the call returns, and the context stays
