@@ -539,6 +539,87 @@ __device__ __forceinline__ void brick_coords(const StagedGeo &g, int64_t b, int6
   bz = b / (g.nb[0] * g.nb[1]);
 }
 
+// One point of a width-4 gather by its quarter-warp: this lane's x node qi and y nodes
+// 2jj, 2jj+1 over all four z nodes, then a reduce-scatter of the CP sums over the eight
+// lanes.  The nodes are base[(origin + x + y*sy + z*sz) * CP] at stencil-relative
+// x, y, z: a brick's tile in shared memory (origin 0) or the field itself; both give the
+// same bits.
+template <int M2, int CP, typename TO, typename I>
+__device__ __forceinline__ void gather4_point(const SchemeT<float, 4> &s, const float (&cx)[M2 > 0 ? M2 : 1],
+                                              const float (&cya)[M2 > 0 ? M2 : 1], const float (&cyb)[M2 > 0 ? M2 : 1],
+                                              int qi, int jj, int sub, unsigned seg_mask, float4 r, int64_t pt,
+                                              const float *base, I sy, I sz, I origin, TO *out, int64_t m, int ncomp) {
+  int lx, ly, lz;
+  unpack_local(r.w, lx, ly, lz);
+  float w1, w2a, w2b, w3[4];
+  if constexpr (M2 > 0) {
+    // only the weights this lane uses: its x node, its two y nodes, all four z nodes
+    w1 = cx[M2 - 1];
+    w2a = cya[M2 - 1];
+    w2b = cyb[M2 - 1];
+#pragma unroll
+    for (int p = M2 - 2; p >= 0; --p) {
+      w1 = fmaf(w1, r.x, cx[p]);
+      w2a = fmaf(w2a, r.y, cya[p]);
+      w2b = fmaf(w2b, r.y, cyb[p]);
+    }
+    weights_all<4, M2>(s, r.z, w3);
+  } else {
+    float wx[4], wy[4];
+    weights_all<4, M2>(s, r.x, wx);
+    weights_all<4, M2>(s, r.y, wy);
+    weights_all<4, M2>(s, r.z, w3);
+    w1 = pick(wx, qi);
+    w2a = pick(wy, 2 * jj);
+    w2b = pick(wy, 2 * jj + 1);
+  }
+  float acc[CP];
+#pragma unroll
+  for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
+  const I node0 = origin + lz * sz + (ly + 2 * jj) * sy + lx + qi;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+#pragma unroll
+    for (int jp = 0; jp < 2; ++jp) {
+      const float w = w1 * (jp ? w2b : w2a) * w3[k];
+      const float4 *p = reinterpret_cast<const float4 *>(base + (node0 + k * sz + jp * sy) * CP);
+#pragma unroll
+      for (int q4 = 0; q4 < CP / 4; ++q4) {
+        const float4 v = p[q4];
+        acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
+        acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
+        acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
+        acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
+      }
+    }
+  }
+  // reduce-scatter over the 8 lanes: halves by lane bit 2, then bit 1, then sum bit 0
+  constexpr int H = CP / 2, Q = CP / 4;
+  const bool up2 = sub & 4, up1 = sub & 2;
+  float h[H];
+#pragma unroll
+  for (int v = 0; v < H; ++v) {
+    const float keep = up2 ? acc[H + v] : acc[v];
+    const float give = up2 ? acc[v] : acc[H + v];
+    h[v] = keep + __shfl_xor_sync(seg_mask, give, 4, 8);
+  }
+  float qv[Q];
+#pragma unroll
+  for (int v = 0; v < Q; ++v) {
+    const float keep = up1 ? h[Q + v] : h[v];
+    const float give = up1 ? h[v] : h[Q + v];
+    qv[v] = keep + __shfl_xor_sync(seg_mask, give, 2, 8);
+  }
+#pragma unroll
+  for (int v = 0; v < Q; ++v) qv[v] += __shfl_xor_sync(seg_mask, qv[v], 1, 8);
+  if ((sub & 1) == 0) {
+    const int cbase = (up2 ? H : 0) + (up1 ? Q : 0);
+#pragma unroll
+    for (int v = 0; v < Q; ++v)
+      if (cbase + v < ncomp) store_out(out, pt + m * (cbase + v), qv[v]);
+  }
+}
+
 // Gather: width-4 stencils, a point per quarter-warp, 512 threads (64 quarter-warps) per
 // CTA; each quarter-warp loads its next point's record and index while it computes.
 constexpr int kGatherThreads = 512;
@@ -605,7 +686,6 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
       }
       phase[buf] ^= 1;
       pending[buf] = false;
-      const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
       uint32_t sl = s0 + qw;
       float4 r_next = sl < s1 ? __ldg(rec + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
       uint32_t p_next = sl < s1 ? __ldg(perm + sl) : 0u;
@@ -616,75 +696,9 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
           r_next = __ldg(rec + sl + nqw);
           p_next = __ldg(perm + sl + nqw);
         }
-        int lx, ly, lz;
-        unpack_local(r.w, lx, ly, lz);
-        float w1, w2a, w2b, w3[4];
-        if constexpr (M2 > 0) {
-          // only the weights this lane uses: its x node, its two y nodes, all four z nodes
-          w1 = cx[M2 - 1];
-          w2a = cya[M2 - 1];
-          w2b = cyb[M2 - 1];
-#pragma unroll
-          for (int p = M2 - 2; p >= 0; --p) {
-            w1 = fmaf(w1, r.x, cx[p]);
-            w2a = fmaf(w2a, r.y, cya[p]);
-            w2b = fmaf(w2b, r.y, cyb[p]);
-          }
-          weights_all<4, M2>(s, r.z, w3);
-        } else {
-          float wx[4], wy[4];
-          weights_all<4, M2>(s, r.x, wx);
-          weights_all<4, M2>(s, r.y, wy);
-          weights_all<4, M2>(s, r.z, w3);
-          w1 = pick(wx, qi);
-          w2a = pick(wy, 2 * jj);
-          w2b = pick(wy, 2 * jj + 1);
-        }
-        float acc[CP];
-#pragma unroll
-        for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
-        const int node0 = (lz * g.w[1] + ly + 2 * jj) * g.w[0] + lx + qi;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-#pragma unroll
-          for (int jp = 0; jp < 2; ++jp) {
-            const float w = w1 * (jp ? w2b : w2a) * w3[k];
-            const float4 *p = reinterpret_cast<const float4 *>(tile + (node0 + (k * g.w[1] + jp) * g.w[0]) * CP);
-#pragma unroll
-            for (int q4 = 0; q4 < CP / 4; ++q4) {
-              const float4 v = p[q4];
-              acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
-              acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
-              acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
-              acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
-            }
-          }
-        }
-        // reduce-scatter over the 8 lanes: halves by lane bit 2, then bit 1, then sum bit 0
-        constexpr int H = CP / 2, Q = CP / 4;
-        const bool up2 = sub & 4, up1 = sub & 2;
-        float h[H];
-#pragma unroll
-        for (int v = 0; v < H; ++v) {
-          const float keep = up2 ? acc[H + v] : acc[v];
-          const float give = up2 ? acc[v] : acc[H + v];
-          h[v] = keep + __shfl_xor_sync(seg_mask, give, 4, 8);
-        }
-        float qv[Q];
-#pragma unroll
-        for (int v = 0; v < Q; ++v) {
-          const float keep = up1 ? h[Q + v] : h[v];
-          const float give = up1 ? h[v] : h[Q + v];
-          qv[v] = keep + __shfl_xor_sync(seg_mask, give, 2, 8);
-        }
-#pragma unroll
-        for (int v = 0; v < Q; ++v) qv[v] += __shfl_xor_sync(seg_mask, qv[v], 1, 8);
-        if ((sub & 1) == 0) {
-          const int cbase = (up2 ? H : 0) + (up1 ? Q : 0);
-#pragma unroll
-          for (int v = 0; v < Q; ++v)
-            if (cbase + v < g.ncomp) store_out(out, p + g.m * (cbase + v), qv[v]);
-        }
+        gather4_point<M2, CP>(s, cx, cya, cyb, qi, jj, sub, seg_mask, r, p,
+                              reinterpret_cast<const float *>(smem + buf * tile_bytes), g.w[0], g.w[0] * g.w[1], 0,
+                              out, g.m, g.ncomp);
       }
     }
     __syncthreads();  // every lane is done with this buffer before it is refilled
@@ -696,6 +710,50 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     for (int i = 0; i < nbuf; ++i)
       if (pending[i]) mbar_wait(bars + i, phase[i]);
   }
+}
+
+// One point of a gather of another width, by one thread over its N2^3 stencil; the nodes
+// are base[(origin + x + y*sy + z*sz) * CP] as for the width-4 gather.
+template <int N2, int M2, int CP, typename TO, typename I>
+__device__ __forceinline__ void gather_point(const SchemeT<float, N2> &s, float4 r, int64_t pt, const float *base, I sy,
+                                             I sz, I origin, TO *out, int64_t m, int ncomp) {
+  int lx, ly, lz;
+  unpack_local(r.w, lx, ly, lz);
+  float w1[N2], w2[N2], w3[N2];
+  weights_all<N2, M2>(s, r.x, w1);
+  weights_all<N2, M2>(s, r.y, w2);
+  weights_all<N2, M2>(s, r.z, w3);
+  float acc[CP];
+#pragma unroll
+  for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
+#pragma unroll 1
+  for (int k = 0; k < N2; ++k) {
+    float w3k = w3[0];
+#pragma unroll
+    for (int q = 1; q < N2; ++q)
+      if (q == k) w3k = w3[q];
+#pragma unroll
+    for (int j = 0; j < N2; ++j) {
+      const float wyz = w2[j] * w3k;
+      const float *row = base + (origin + (lz + k) * sz + (ly + j) * sy + lx) * CP;
+#pragma unroll
+      for (int i = 0; i < N2; ++i) {
+        const float w = wyz * w1[i];
+        const float4 *p = reinterpret_cast<const float4 *>(row + i * CP);
+#pragma unroll
+        for (int q4 = 0; q4 < CP / 4; ++q4) {
+          const float4 v = p[q4];
+          acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
+          acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
+          acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
+          acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < CP; ++c)
+    if (c < ncomp) store_out(out, pt + m * c, acc[c]);
 }
 
 // Gather for other widths: a point per thread over its N2^3 stencil in the tile.
@@ -744,47 +802,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
       phase[buf] ^= 1;
       pending[buf] = false;
-      const float *tile = reinterpret_cast<const float *>(smem + buf * tile_bytes);
       for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += blockDim.x) {
-        const float4 r = __ldg(rec + sl);
-        int lx, ly, lz;
-        unpack_local(r.w, lx, ly, lz);
-        float w1[N2], w2[N2], w3[N2];
-        weights_all<N2, M2>(s, r.x, w1);
-        weights_all<N2, M2>(s, r.y, w2);
-        weights_all<N2, M2>(s, r.z, w3);
-        float acc[CP];
-#pragma unroll
-        for (int c = 0; c < CP; ++c) acc[c] = 0.0f;
-#pragma unroll 1
-        for (int k = 0; k < N2; ++k) {
-          float w3k = w3[0];
-#pragma unroll
-          for (int q = 1; q < N2; ++q)
-            if (q == k) w3k = w3[q];
-#pragma unroll
-          for (int j = 0; j < N2; ++j) {
-            const float wyz = w2[j] * w3k;
-            const float *row = tile + (((lz + k) * g.w[1] + ly + j) * g.w[0] + lx) * CP;
-#pragma unroll
-            for (int i = 0; i < N2; ++i) {
-              const float w = wyz * w1[i];
-              const float4 *p = reinterpret_cast<const float4 *>(row + i * CP);
-#pragma unroll
-              for (int q4 = 0; q4 < CP / 4; ++q4) {
-                const float4 v = p[q4];
-                acc[4 * q4 + 0] = fmaf(w, v.x, acc[4 * q4 + 0]);
-                acc[4 * q4 + 1] = fmaf(w, v.y, acc[4 * q4 + 1]);
-                acc[4 * q4 + 2] = fmaf(w, v.z, acc[4 * q4 + 2]);
-                acc[4 * q4 + 3] = fmaf(w, v.w, acc[4 * q4 + 3]);
-              }
-            }
-          }
-        }
-        const int64_t p = perm[sl];
-#pragma unroll
-        for (int c = 0; c < CP; ++c)
-          if (c < g.ncomp) store_out(out, p + g.m * c, acc[c]);
+        gather_point<N2, M2, CP>(s, __ldg(rec + sl), perm[sl], reinterpret_cast<const float *>(smem + buf * tile_bytes),
+                                 g.w[0], g.w[0] * g.w[1], 0, out, g.m, g.ncomp);
       }
     }
     __syncthreads();
@@ -793,6 +813,59 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (failed && threadIdx.x == 0)
     for (int i = 0; i < nbuf; ++i)
       if (pending[i]) mbar_wait(bars + i, phase[i]);
+}
+
+// ------------------------------------------------------------ direct gather
+//
+// For point sets sparse on their grid (a few points per brick) a tile per brick costs more
+// than the points' own stencils: these kernels take the points in binned order, all in
+// flight at once, and read each point's nodes straight from the field, with the per-point
+// arithmetic of the staged kernels (so the same bits).  A point's brick comes from its
+// cell key.
+
+__device__ __forceinline__ int64_t direct_origin(const StagedGeo &g, int64_t pf, int64_t py, uint32_t key) {
+  const int64_t brick = key / (uint64_t)g.bvol;
+  int64_t bx, by, bz;
+  brick_coords(g, brick, bx, by, bz);
+  return (bx * g.b[0] + g.box_off) + pf * ((by * g.b[1] + g.box_off) + py * (bz * g.b[2] + g.box_off));
+}
+
+template <int M2, int CP, typename TO>
+__global__ void __launch_bounds__(kThreads)
+    k_gather_direct4(StagedGeo g, SchemeT<float, 4> s, const float *__restrict__ field, int64_t px, int64_t py,
+                     const float4 *__restrict__ rec, const uint32_t *__restrict__ perm,
+                     const uint32_t *__restrict__ keys, TO *__restrict__ out) {
+  const int lane = threadIdx.x & 31, sub = lane & 7, qi = sub & 3, jj = sub >> 2;
+  const unsigned seg_mask = 0xFFu << (lane & ~7);
+  float cx[M2 > 0 ? M2 : 1], cya[M2 > 0 ? M2 : 1], cyb[M2 > 0 ? M2 : 1];
+  if constexpr (M2 > 0) {
+#pragma unroll
+    for (int p = 0; p < M2; ++p) {
+      cx[p] = s.c[qi + 4 * p];
+      cya[p] = s.c[2 * jj + 4 * p];
+      cyb[p] = s.c[2 * jj + 1 + 4 * p];
+    }
+  }
+  const int64_t nq = ((int64_t)gridDim.x * blockDim.x) >> 3;
+  for (int64_t sl = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 3; sl < g.m; sl += nq) {
+    const float4 r = __ldg(rec + sl);
+    const int64_t pt = __ldg(perm + sl);
+    const int64_t origin = direct_origin(g, px, py, __ldg(keys + pt));
+    gather4_point<M2, CP>(s, cx, cya, cyb, qi, jj, sub, seg_mask, r, pt, field, px, px * py, origin, out, g.m, g.ncomp);
+  }
+}
+
+template <int N2, int M2, int CP, typename TO>
+__global__ void __launch_bounds__(kThreads)
+    k_gather_direct(StagedGeo g, SchemeT<float, N2> s, const float *__restrict__ field, int64_t px, int64_t py,
+                    const float4 *__restrict__ rec, const uint32_t *__restrict__ perm,
+                    const uint32_t *__restrict__ keys, TO *__restrict__ out) {
+  for (int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; sl < g.m; sl += (int64_t)gridDim.x * blockDim.x) {
+    const float4 r = __ldg(rec + sl);
+    const int64_t pt = __ldg(perm + sl);
+    const int64_t origin = direct_origin(g, px, py, __ldg(keys + pt));
+    gather_point<N2, M2, CP>(s, r, pt, field, px, px * py, origin, out, g.m, g.ncomp);
+  }
 }
 
 // ------------------------------------------------------------ staged scatter
@@ -1339,9 +1412,42 @@ StagedGeo staged_geo(const gbg_field_s *f, const gbg_bins_s *b, int width) {
   return g;
 }
 
+// Average points per brick below which a gather reads the field directly (the direct
+// kernels) instead of staging a tile per brick: at four points a brick a width-4 tile
+// (brick + 3 cells) of a 15x8x8 brick is about 8x the bytes of the points' own stencils.
+constexpr int64_t kDirectPerBrick = 4;
+
+template <int N2, int M2, typename TO>
+gbg_status launch_direct_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, TO *out, cudaStream_t st) {
+  const StagedGeo g = staged_geo(f, b, N2);
+  const SchemeT<float, N2> s = make_scheme<float, N2>(sch);
+  int sms = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int64_t lanes = N2 == 4 ? 8 * b->npoints : b->npoints;  // a quarter-warp per width-4 point
+  const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((lanes + kThreads - 1) / kThreads, (int64_t)sms * 8));
+  mark_main_start(st);
+  if constexpr (N2 == 4) {
+    if (f->cp == 4)
+      k_gather_direct4<M2, 4, TO><<<blocks, kThreads, 0, st>>>(g, s, f->data, f->px, f->py, b->rec, b->perm, b->keys, out);
+    else
+      k_gather_direct4<M2, 12, TO><<<blocks, kThreads, 0, st>>>(g, s, f->data, f->px, f->py, b->rec, b->perm, b->keys, out);
+  } else {
+    if (f->cp == 4)
+      k_gather_direct<N2, M2, 4, TO><<<blocks, kThreads, 0, st>>>(g, s, f->data, f->px, f->py, b->rec, b->perm, b->keys, out);
+    else
+      k_gather_direct<N2, M2, 12, TO><<<blocks, kThreads, 0, st>>>(g, s, f->data, f->px, f->py, b->rec, b->perm, b->keys, out);
+  }
+  mark_main_stop(st);
+  note_launch();
+  GBG_CUDA_TRY(cudaGetLastError());
+  return GBG_OK;
+}
+
 template <int N2, int M2, typename TO>
 gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, TO *out, int32_t *status,
                                 cudaStream_t st) {
+  if (b->npoints < kDirectPerBrick * b->nbricks) return launch_direct_gather<N2, M2>(f, b, sch, out, st);
   CUtensorMap *map = nullptr;
   GBG_TRY(tensor_map_for(f, N2, b->b, &map));
   const StagedGeo g = staged_geo(f, b, N2);

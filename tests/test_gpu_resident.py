@@ -191,6 +191,37 @@ def test_compensation_leaves_single_chunk_regions_unchanged(gbg, oracle, dev):
     assert torch.equal(out[0], out[1])
 
 
+@pytest.mark.parametrize("ncomp", [3, 12])
+@pytest.mark.parametrize("width", [2, 4, 6, 8])
+def test_direct_gather_of_sparse_points(gbg, oracle, dev, ncomp, width):
+    """A point set sparse on its grid (under four points a brick) is gathered straight from
+    the field, with the staged kernels' per-point arithmetic: it matches the oracle, and a
+    point's values are bitwise those it gets inside a dense set (staged tiles)."""
+    from gbgperiodicfields_gb300 import resident
+    rng = np.random.default_rng(90 + width)
+    n = (40, 36, 32)
+    grid = gbg.Grid3D(n, (TWO_PI,) * 3, origin=(0.2, -0.4, 0.6))
+    g = oracle.grid_dict(grid.grid_size, grid.domain_size, grid.origin)
+    f = np.asfortranarray(rng.standard_normal(n + (ncomp,)))
+    field = resident.ResidentField(grid, ncomp, max_stencil_width=8).load(torch.from_numpy(f).cuda())
+    scheme = {2: gbg.LalescuSpline(2, 0), 4: gbg.CatmullRom, 6: gbg.LalescuSpline(6), 8: gbg.LagrangeSpline(8)}[width]
+    dense = np.asfortranarray(np.array(grid.origin) + TWO_PI * (rng.random((60000, 3)) * 1.2 - 0.1))
+    sparse = np.asfortranarray(dense[:25])
+    got = {}
+    for name, pos in (("sparse", sparse), ("dense", dense)):
+        bins = resident.PointBins(grid, pos.shape[0], brick=(11, 8, 8)).build(torch.from_numpy(pos).cuda())
+        assert (pos.shape[0] < 4 * bins_count(bins)) == (name == "sparse")
+        got[name] = resident.interpolate_binned(field, bins, scheme, dtype=torch.float32).cpu()
+    assert torch.equal(got["sparse"], got["dense"][:25])
+    want = oracle.gather(g, f, sparse, scheme.coefficients)
+    assert relerr(got["sparse"].double().numpy(), want) <= 1e-5
+
+
+def bins_count(bins):
+    nb = [-(-n // b) for n, b in zip(bins.grid.grid_size, bins.brick)]
+    return nb[0] * nb[1] * nb[2]
+
+
 @pytest.mark.parametrize("comp", [True, False], ids=["compensated", "plain"])
 def test_multi_chunk_scatter_is_independent_of_the_launch_shape(gbg, oracle, dev, comp):
     """Dense points make every brick region span several chunks; the chunks, and so where
