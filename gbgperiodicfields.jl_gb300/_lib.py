@@ -141,6 +141,7 @@ SIGNATURES = {
     "gbg_bins_destroy": (_I32, [_P]),
     "gbg_bins_set_launch": (_I32, [_P, _I32, _I32]),
     "gbg_bins_set_compensated": (_I32, [_P, _I32]),
+    "gbg_bins_set_sparse_regions": (_I32, [_P, _I32]),
     "gbg_bins_set_wait_limit": (_I32, [_P, ctypes.c_uint32]),
     "gbg_points_displace": (_I32, [_GP, _I32, _P, _P, _I64, _I32, ctypes.POINTER(_D), ctypes.POINTER(_P), _P]),
     "gbg_bins_build_displaced": (_I32, [_P, _I32, _P, _P, _I64, _I32, ctypes.POINTER(_D), ctypes.POINTER(_P),

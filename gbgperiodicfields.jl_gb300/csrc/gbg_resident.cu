@@ -64,6 +64,7 @@ struct gbg_bins_s {
   bool async = false;  // block from cudaMallocAsync (serving loop)
   int32_t gather_threads = 0, scatter_threads = 0;  // 0: the defaults (gbg_bins_set_launch)
   int32_t compensated = 1;  // the scatter's compensated summation (gbg_bins_set_compensated)
+  int32_t sparse_regions = 1;  // sparse sets: regions from neighbour lists (gbg_bins_set_sparse_regions)
   uint32_t wait_polls = 0;  // the gather's tile-wait limit, 0: the default (gbg_bins_set_wait_limit)
   // work lists rebuilt with the bins: bricks holding a point (gathers), bricks a point's
   // stencil reaches (scatters with beta == 1; valid when reach_ok), and their lengths
@@ -919,6 +920,7 @@ struct FixGeo {
   int32_t comp;            // compensated: chunk partial sums folded into (sum, correction) by TwoSum
   float *cscratch;         // corrections of regions of several chunks: one slot per CTA
   int64_t cstride;         // floats per slot (>= bvol * CP)
+  int32_t sparse;          // few points a brick: regions from the neighbouring bricks' lists
 };
 
 // All N2 weights from coefficients in memory ([q + N2*p], M2 == N2 powers).
@@ -991,6 +993,16 @@ size_t scatter_nodes_budget(const FixGeo &g, int cp, int n2) {
   return want <= half ? half : std::min<size_t>(200 * 1024, 228 * 1024 - 4096);
 }
 
+// Few points a brick (as for the direct gather), and a region no wider than the grid on any
+// axis (each region cell a distinct cell): the scatter builds regions from the neighbouring
+// bricks' point lists.
+int32_t scatter_sparse(const gbg_bins_s *b, const gbg_grid &grid, int n2) {
+  if (!b->sparse_regions || b->npoints >= 4 * b->nbricks) return 0;
+  for (int d = 0; d < 3; ++d)
+    if (b->b[d] + n2 - 1 > grid.n[d]) return 0;
+  return 1;
+}
+
 // Deterministic scatter, output-driven.  A CTA owns a brick's nodes and a thread owns a
 // 2 x 2 quad of nodes in y and z (one node for width 8): it sums, in registers, the
 // contributions ((wx*wy)*wz)*alpha*q of every point whose stencil reaches each node, in a
@@ -1047,7 +1059,91 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   }
   if (!any && !beta_zero && beta == 1.0f) return;  // the brick keeps its values
   uint32_t count = 0;
-  if (any) {
+  // A point set sparse on its grid: the region's points are taken from the ranges of the
+  // 27 neighbouring bricks, kept when their cell lies in the region and put in region
+  // order (cell, then slot), instead of building the region's per-cell tables -- the same
+  // points in the same order as the tables give.  Too many candidates: the tables.
+  constexpr uint32_t kCandScan = 256, kCandKeep = 64;
+  uint32_t *sorted_e = off + 32 + kCandKeep, *sorted_s = r0s + 32 + kCandKeep;
+  bool sparse = false;
+  if (g.sparse && g.neighbour_skip && any && ecount >= 32 + 2 * (int)kCandKeep) {
+    uint32_t *nstart = r0s, *npre = off, *cand_e = off + 32, *cand_s = r0s + 32;
+    if (threadIdx.x < 32) {
+      const int t = threadIdx.x;
+      uint32_t a = 0, c = 0;
+      if (t < 27) {
+        const int dx = t % 3 - 1, dy = (t / 3) % 3 - 1, dz = t / 9 - 1;
+        // an axis of one brick has one neighbour (the brick itself), of two bricks two
+        const bool dup = (g.nb[0] == 1 && dx != 0) || (g.nb[0] == 2 && dx < 0) || (g.nb[1] == 1 && dy != 0) ||
+                         (g.nb[1] == 2 && dy < 0) || (g.nb[2] == 1 && dz != 0) || (g.nb[2] == 2 && dz < 0);
+        if (!dup) {
+          const uint64_t k = ((uint64_t)((bz + dz + g.nb[2]) % g.nb[2]) * (uint32_t)g.nb[1] +
+                              (uint32_t)((by + dy + g.nb[1]) % g.nb[1])) * (uint32_t)g.nb[0] +
+                             (uint32_t)((bx + dx + g.nb[0]) % g.nb[0]);
+          a = __ldg(cell_start + k * (uint64_t)bvol);
+          c = __ldg(cell_start + (k + 1) * (uint64_t)bvol) - a;
+        }
+      }
+      uint32_t x = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (t >= o) x += y;
+      }
+      if (t < 27) {
+        nstart[t] = a;
+        npre[t + 1] = x;
+      }
+      if (t == 0) {
+        npre[0] = 0;
+        warp_tot[1] = 0;
+      }
+      if (t == 31) warp_tot[0] = x;
+    }
+    __syncthreads();
+    const uint32_t total = warp_tot[0];
+    if (total <= kCandScan) {
+      for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+        int k = 0;
+        while (k < 26 && npre[k + 1] <= t) ++k;
+        const uint32_t slot = nstart[k] + (t - npre[k]);
+        int lx, ly, lz;
+        unpack_local(__ldg(rec + slot).w, lx, ly, lz);
+        const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+        // the point's cell, then its offset from the region's first cell (periodic)
+        const int cx = (int)((bx + dx + g.nb[0]) % g.nb[0]) * B0 + lx;
+        const int cy = (int)((by + dy + g.nb[1]) % g.nb[1]) * B1 + ly;
+        const int cz = (int)((bz + dz + g.nb[2]) % g.nb[2]) * g.b[2] + lz;
+        int ex = (cx - (bx * B0 - half)) % g.n[0], ey = (cy - (by * B1 - half)) % g.n[1],
+            ez = (cz - (bz * g.b[2] - half)) % g.n[2];
+        if (ex < 0) ex += g.n[0];
+        if (ey < 0) ey += g.n[1];
+        if (ez < 0) ez += g.n[2];
+        if (ex < E0 && ey < E1 && ez < E2) {
+          const uint32_t i = atomicAdd(warp_tot + 1, 1u);
+          if (i < kCandKeep) {
+            cand_e[i] = (uint32_t)((ez * E1 + ey) * E0 + ex);
+            cand_s[i] = slot;
+          }
+        }
+      }
+      __syncthreads();
+      const uint32_t kept = warp_tot[1];
+      if (kept <= kCandKeep) {
+        for (uint32_t i = threadIdx.x; i < kept; i += blockDim.x) {
+          const uint32_t e = cand_e[i], sl = cand_s[i];
+          uint32_t rank = 0;
+          for (uint32_t j = 0; j < kept; ++j) rank += (cand_e[j] < e || (cand_e[j] == e && cand_s[j] < sl)) ? 1u : 0u;
+          sorted_e[rank] = e;
+          sorted_s[rank] = sl;
+        }
+        sparse = true;
+        count = kept;
+      }
+      __syncthreads();
+    }
+  }
+  if (any && !sparse) {
     // per-axis key tables of the region's cells (periodic wrap, then brick and local index)
     for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
       const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
@@ -1118,6 +1214,7 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     // up to SU points per thread per round: every search first, then every global load,
     // then the weights, so the latencies of the points overlap
     for (uint32_t t0 = c0 + threadIdx.x; t0 < c1; t0 += SU * blockDim.x) {
+      if (sparse) break;
       uint32_t sl[SU];
       int cell[SU];
 #pragma unroll
@@ -1174,6 +1271,38 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
         if (!isfinite(r[u].x + r[u].y + r[u].z + qa)) nonfinite = 1;
       }
     }
+    if (sparse) {
+      // the sorted candidates, staged as above (one chunk: count <= kCandKeep)
+      for (uint32_t t = threadIdx.x; t < count; t += blockDim.x) {
+        const uint32_t sl = sorted_s[t];
+        const float4 r = __ldg(rec + sl);
+        scx[t] = (unsigned char)(sorted_e[t] % (uint32_t)E0);
+        float *wt = sw + t * kScatterWStride<N2>;
+        float w[N2];
+        if constexpr (FIXED) weights_ptr<N2>(coef, r.x, w); else weights_rt<N2>(coef, m2, r.x, w);
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[q] = w[q];
+        if constexpr (FIXED) weights_ptr<N2>(coef, r.y, w); else weights_rt<N2>(coef, m2, r.y, w);
+        wt[N2] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[N2 + 1 + q] = w[q];
+        wt[2 * N2 + 1] = 0.0f;
+        if constexpr (FIXED) weights_ptr<N2>(coef, r.z, w); else weights_rt<N2>(coef, m2, r.z, w);
+        wt[2 * N2 + 2] = 0.0f;
+#pragma unroll
+        for (int q = 0; q < N2; ++q) wt[2 * N2 + 3 + q] = w[q];
+        wt[3 * N2 + 3] = 0.0f;
+        const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+        float qa = 0.0f;
+#pragma unroll
+        for (int v = 0; v < CP / 4; ++v) {
+          const float4 x = __ldg(q4 + v);
+          reinterpret_cast<float4 *>(sq + t * CP)[v] = x;
+          qa += fabsf(x.x) + fabsf(x.y) + fabsf(x.z) + fabsf(x.w);
+        }
+        if (!isfinite(r.x + r.y + r.z + qa)) nonfinite = 1;
+      }
+    }
     // a chunk with a non-finite value takes the exact path: each point only touches the
     // nodes it reaches; otherwise a point adds w*q to all of a quad's nodes, with w == 0
     // exactly for the nodes it does not reach, and fmaf(0, q, s) == s for finite q
@@ -1198,7 +1327,39 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
           acc[n][4 * v + 3] = s4.w;
         }
       }
-      if (count > 0) {
+      if (count > 0 && sparse) {
+        // the staged candidates in region order: a point feeds this quad when its cell is
+        // in the quad's x window and one of its rows (the order of the rows path)
+        const int xk = lx + N2 - 1;
+        for (uint32_t t = 0; t < count; ++t) {
+          const uint32_t e = sorted_e[t];
+          const int ex = (int)(e % (uint32_t)E0), ey = (int)((e / (uint32_t)E0) % (uint32_t)E1),
+                    ez = (int)(e / (uint32_t)(E0 * E1));
+          const int jj = ey - ly, kk = ez - lz;
+          if (ex < lx || ex > xk || jj < 0 || jj >= RY || kk < 0 || kk >= RZ) continue;
+          const float *wp = sw + t * kScatterWStride<N2>;
+          const float *wy = wp + (2 * N2 - jj), *wz = wp + (3 * N2 + 2 - kk);
+          const float4 *qp = reinterpret_cast<const float4 *>(sq) + t * (CP / 4);
+          const float wx = wp[xk - ex];
+          float q[CP];
+#pragma unroll
+          for (int v = 0; v < CP / 4; ++v) {
+            const float4 t4 = qp[v];
+            q[4 * v] = t4.x;
+            q[4 * v + 1] = t4.y;
+            q[4 * v + 2] = t4.z;
+            q[4 * v + 3] = t4.w;
+          }
+#pragma unroll
+          for (int n = 0; n < BY * BZ; ++n) {
+            const int a = n % BY, bb = n / BY;
+            if (exact && !(jj - a >= 0 && jj - a <= N2 - 1 && kk - bb >= 0 && kk - bb <= N2 - 1)) continue;
+            const float wgt = (wx * wy[a]) * wz[bb];
+#pragma unroll
+            for (int c = 0; c < CP; ++c) acc[n][c] = fmaf(wgt, q[c], acc[n][c]);
+          }
+        }
+      } else if (count > 0) {
         // row (jj, kk) holds the region cells (lx..lx+N2-1, ly+jj, lz+kk); its bit in the
         // mask is kk*8 + jj, so bits rise with region order.  Node (lx, ly+a, lz+b) takes a
         // point of that row in region cell ex with stencil indices lx+N2-1-ex on x,
@@ -1520,6 +1681,7 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   g.neighbour_skip = neighbour_skip_ok(b->b, b->nb, f->grid.n, N2);
   g.comp = b->compensated;
   g.cscratch = b->cscratch;
+  g.sparse = scatter_sparse(b, f->grid, N2);
   g.cstride = b->bvol * 12;
   g.nbricks = b->nbricks;
   g.bvol = b->bvol;
@@ -2075,6 +2237,13 @@ gbg_status gbg_bins_set_compensated(gbg_bins b, int32_t compensated) {
   return GBG_OK;
 }
 
+gbg_status gbg_bins_set_sparse_regions(gbg_bins b, int32_t allow) {
+  clear_error();
+  if (!b) return set_error(GBG_EARG, "null bins");
+  b->sparse_regions = allow ? 1 : 0;
+  return GBG_OK;
+}
+
 gbg_status gbg_bins_set_launch(gbg_bins b, int32_t gather_threads, int32_t scatter_threads) {
   clear_error();
   if (!b) return set_error(GBG_EARG, "null bins");
@@ -2502,6 +2671,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
       }
       d.fg.neighbour_skip = neighbour_skip_ok(b->b, b->nb, ds->grid.n, w);
       d.fg.comp = b->compensated;
+      d.fg.sparse = scatter_sparse(b, ds->grid, w);
       d.fg.nbricks = b->nbricks;
       d.fg.bvol = b->bvol;
       d.fg.px = ds->px;

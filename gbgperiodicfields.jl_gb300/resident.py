@@ -141,6 +141,13 @@ class PointBins:
         self.compensated = bool(on)
         return self
 
+    def set_sparse_regions(self, allow: bool = True):
+        """Whether the binned scatter may take a sparse set's regions from the neighbouring
+        bricks' point lists (the default) or always builds per-cell region tables; the
+        results are the same bits (gbg_bins_set_sparse_regions)."""
+        _lib.check(_lib.load().gbg_bins_set_sparse_regions(self.handle, int(bool(allow))), "gbg_bins_set_sparse_regions")
+        return self
+
     def set_wait_limit(self, polls: int = 0):
         """Polls of a staged tile's barrier before the binned gather gives up on it (0 = the
         default; gbg_bins_set_wait_limit)."""

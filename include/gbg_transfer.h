@@ -257,6 +257,12 @@ gbg_status gbg_bins_set_launch(gbg_bins bins, int32_t gather_threads, int32_t sc
  * that fits in one chunk is summed the same way either way.  No counterpart in the
  * reference, whose scatter sums in its field's own precision. */
 gbg_status gbg_bins_set_compensated(gbg_bins bins, int32_t compensated);
+/* Regions of the binned scatter for point sets sparse on their grid (fewer than four points
+ * a brick): 1 (the default) lets a brick take its region's points from the point lists of
+ * its 27 neighbouring bricks when they hold few enough; 0 always builds the region's
+ * per-cell tables.  Both give the same points in the same order, so the same bits; the
+ * switch exists for tests and tuning.  No counterpart in the reference. */
+gbg_status gbg_bins_set_sparse_regions(gbg_bins bins, int32_t allow);
 /* Polls of a staged tile's mbarrier before gbg_interpolate_binned gives up on it (0 = the
  * default, 2^22 suspending polls; a smaller limit polls without suspending): the wait then
  * sets GBG_DEV_TIMEOUT, the CTA lets its copies land (always with the full limit) and

@@ -217,6 +217,38 @@ def test_direct_gather_of_sparse_points(gbg, oracle, dev, ncomp, width):
     assert relerr(got["sparse"].double().numpy(), want) <= 1e-5
 
 
+@pytest.mark.parametrize("ncomp", [3, 12])
+@pytest.mark.parametrize("width", [2, 4, 6, 8])
+@pytest.mark.parametrize("beta", [0.0, 1.0, 0.5])
+def test_sparse_scatter_regions_from_neighbour_lists(gbg, oracle, dev, ncomp, width, beta):
+    """A sparse set's scatter builds each brick's region from the neighbouring bricks' point
+    lists: bitwise the result of the per-cell tables, and within the bar of the oracle --
+    including points in one cell and across the periodic wrap."""
+    from gbgperiodicfields_gb300 import resident
+    rng = np.random.default_rng(120 + width)
+    n = (40, 36, 32)
+    grid = gbg.Grid3D(n, (TWO_PI,) * 3, origin=(0.2, -0.4, 0.6))
+    g = oracle.grid_dict(grid.grid_size, grid.domain_size, grid.origin)
+    scheme = {2: gbg.LalescuSpline(2, 0), 4: gbg.CatmullRom, 6: gbg.LalescuSpline(6), 8: gbg.LagrangeSpline(8)}[width]
+    pos = np.array(grid.origin) + TWO_PI * (rng.random((200, 3)) * 1.2 - 0.1)
+    pos[:5] = pos[5]                                   # a crowded cell
+    pos[10:14] = np.array(grid.origin) + 1e-9          # at the wrap
+    pos = np.asfortranarray(pos)
+    q = np.asfortranarray(rng.standard_normal((200, ncomp)))
+    prior = np.asfortranarray(rng.standard_normal(n + (ncomp,)))
+    bins = resident.PointBins(grid, 200, brick=(11, 8, 8)).build(torch.from_numpy(pos).cuda())
+    assert 200 < 4 * bins_count(bins)
+    outs = []
+    for allow in (True, False):
+        bins.set_sparse_regions(allow)
+        dest = resident.ResidentField(grid, ncomp, max_stencil_width=8).load(torch.from_numpy(prior).cuda())
+        resident.anterpolate_binned(dest, bins, scheme, torch.from_numpy(q).cuda(), 1.0, beta)
+        outs.append(dest.read())
+    assert torch.equal(outs[0], outs[1])
+    want = oracle.scatter(g, prior.copy(order="F"), pos, q, scheme.coefficients, 1.0, beta)
+    assert relerr(outs[0].cpu().numpy(), want) <= 1e-5
+
+
 def bins_count(bins):
     nb = [-(-n // b) for n, b in zip(bins.grid.grid_size, bins.brick)]
     return nb[0] * nb[1] * nb[2]
