@@ -696,8 +696,7 @@ def batched_form(gbg, dev):
                                  q=i["q"]) for i in insts])
 
     def step():
-        for i in insts:
-            i["bins"].build(i["pos"])
+        resident.build_bins([(i["bins"], i["pos"]) for i in insts])
         batch.run()
 
     def seq():
@@ -707,7 +706,7 @@ def batched_form(gbg, dev):
             resident.anterpolate_binned(i["dest"], i["bins"], i["scheme"], i["q"])
 
     t_seq = _time_ms(seq)
-    t_bins = _time_ms(lambda: [i["bins"].build(i["pos"]) for i in insts])
+    t_bins = _time_ms(lambda: resident.build_bins([(i["bins"], i["pos"]) for i in insts]))
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):

@@ -148,6 +148,7 @@ SIGNATURES = {
                                         _I32, _P, _P]),
     "gbg_bins_permute": (_I32, [_P, _I32, _I32, _P, _P, _P]),
     "gbg_bins_build": (_I32, [_P, _I32, _P, _I64, _P, _P]),
+    "gbg_bins_build_batch": (_I32, [_P, _P, _P, _P, _I32, _P, _P]),
     "gbg_bins_order": (_I32, [_P, _P, _P]),
     "gbg_interpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _P, _P]),
     "gbg_anterpolate_binned": (_I32, [_P, _P, _SP, _I32, _P, _D, _D, _P, _P]),

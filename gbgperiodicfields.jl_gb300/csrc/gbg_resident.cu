@@ -28,6 +28,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <type_traits>
 #include <vector>
@@ -101,6 +103,60 @@ namespace gbg {
 namespace {
 
 constexpr int kThreads = 256;
+
+// Side streams of the library, per device: independent instances of a batch and of a
+// batched bins build run on them at the same time, forked from the caller's stream by an
+// event and joined back by one event per side stream -- inside a stream capture this
+// records parallel branches of the graph.  They are made by gbg_bins_create and
+// gbg_batch_create (never inside a capture); the mutex keeps one fork/join at a time.
+constexpr int kSideStreams = 8;
+struct SidePool {
+  cudaStream_t s[kSideStreams];
+  cudaEvent_t fork, join[kSideStreams];
+  bool ready = false;
+};
+std::mutex g_side_mu;
+SidePool g_side[64];
+
+gbg_status side_pool_ready() {
+  int dev = 0;
+  GBG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(GBG_EUNSUPPORTED, "device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_side_mu);
+  SidePool &p = g_side[dev];
+  if (p.ready) return GBG_OK;
+  GBG_CUDA_TRY(cudaEventCreateWithFlags(&p.fork, cudaEventDisableTiming));
+  for (int i = 0; i < kSideStreams; ++i) {
+    GBG_CUDA_TRY(cudaStreamCreateWithFlags(&p.s[i], cudaStreamNonBlocking));
+    GBG_CUDA_TRY(cudaEventCreateWithFlags(&p.join[i], cudaEventDisableTiming));
+  }
+  p.ready = true;
+  return GBG_OK;
+}
+
+// The caller's stream forked over k side streams: side(i, stream) enqueues side stream i's
+// work and then main_work() the caller's stream's own, which overlaps it; every side
+// stream is then joined back.
+template <typename F, typename G>
+gbg_status side_run(cudaStream_t main, int k, F &&side, G &&main_work) {
+  int dev = 0;
+  GBG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64 || !g_side[dev].ready)
+    return set_error(GBG_EARG, "side streams not made on this device (gbg_bins_create or gbg_batch_create makes them)");
+  std::lock_guard<std::mutex> lock(g_side_mu);
+  SidePool &p = g_side[dev];
+  k = std::max(1, std::min(k, kSideStreams));
+  GBG_CUDA_TRY(cudaEventRecord(p.fork, main));
+  for (int i = 0; i < k; ++i) GBG_CUDA_TRY(cudaStreamWaitEvent(p.s[i], p.fork, 0));
+  gbg_status st = GBG_OK;
+  for (int i = 0; i < k && st == GBG_OK; ++i) st = side(i, p.s[i]);
+  if (st == GBG_OK) st = main_work();
+  for (int i = 0; i < k; ++i) {
+    GBG_CUDA_TRY(cudaEventRecord(p.join[i], p.s[i]));
+    GBG_CUDA_TRY(cudaStreamWaitEvent(main, p.join[i], 0));
+  }
+  return st;
+}
 // scatter CTAs per SM that a launch may use at most: each owns a slot of the compensated
 // scatter's correction scratch
 constexpr int kScatterSlotsPerSM = 4;
@@ -2219,6 +2275,11 @@ gbg_status gbg_bins_create(const gbg_grid *grid, int64_t max_points, const int32
   }
   bins_carve(b);
   cudaMemset(b->cell_start, 0, sizeof(uint32_t) * ((size_t)b->nkeys + 1));
+  if (gbg_status e = side_pool_ready()) {
+    cudaFree(b->block);
+    delete b;
+    return e;
+  }
   *out = b;
   return GBG_OK;
 }
@@ -2420,6 +2481,43 @@ gbg_status gbg_bins_build(gbg_bins b, gbg_dtype pos_dtype, const void *positions
   if (pos_dtype == GBG_F64)
     return bins_build_impl<double>(b, static_cast<const double *>(positions), npoints, device_status, st, nullptr);
   return bins_build_impl<float>(b, static_cast<const float *>(positions), npoints, device_status, st, nullptr);
+}
+
+gbg_status gbg_bins_build_batch(const gbg_bins *bins, const gbg_dtype *dtypes, const void *const *positions,
+                                const int64_t *npoints, int32_t count, int32_t *device_status, void *stream) {
+  clear_error();
+  if (count < 0 || (count > 0 && (!bins || !dtypes || !positions || !npoints))) return set_error(GBG_EARG, "null argument");
+  for (int32_t i = 0; i < count; ++i) {
+    if (!bins[i]) return set_error(GBG_EARG, "null bins");
+    if (npoints[i] < 0 || npoints[i] > bins[i]->max_points) return set_error(GBG_EDIM, "more points than the bins hold");
+    if (dtypes[i] != GBG_F32 && dtypes[i] != GBG_F64) return set_error(GBG_EARG, "bad dtype");
+    if (npoints[i] > 0 && !positions[i]) return set_error(GBG_EARG, "null positions");
+  }
+  if (count == 0) return GBG_OK;
+  // the same bins twice build in call order on one side stream
+  std::map<const gbg_bins_s *, int> lane;
+  std::vector<int> at(count);
+  for (int32_t i = 0; i < count; ++i) {
+    auto it = lane.find(bins[i]);
+    at[i] = it != lane.end() ? it->second : (int)(lane.size() % kSideStreams);
+    lane.emplace(bins[i], at[i]);
+  }
+  const int k = (int)std::min<size_t>(lane.size(), kSideStreams);
+  return side_run(
+      static_cast<cudaStream_t>(stream), k,
+      [&](int side, cudaStream_t s) -> gbg_status {
+        for (int32_t i = 0; i < count; ++i) {
+          if (at[i] != side) continue;
+          if (dtypes[i] == GBG_F64)
+            GBG_TRY(bins_build_impl<double>(bins[i], static_cast<const double *>(positions[i]), npoints[i],
+                                            device_status, s, nullptr));
+          else
+            GBG_TRY(bins_build_impl<float>(bins[i], static_cast<const float *>(positions[i]), npoints[i],
+                                           device_status, s, nullptr));
+        }
+        return GBG_OK;
+      },
+      [] { return GBG_OK; });
 }
 
 gbg_status gbg_bins_order(gbg_bins b, int32_t *order, void *stream) {
@@ -2839,6 +2937,7 @@ extern "C" {
 gbg_status gbg_batch_create(const gbg_batch_item *items, int32_t count, gbg_batch *out) {
   clear_error();
   if (!out) return set_error(GBG_EARG, "null argument");
+  GBG_TRY(side_pool_ready());
   std::vector<gbg_batch_item> pooled, direct;
   GBG_TRY(batch_split(items, count, pooled, direct));
   auto *bt = new (std::nothrow) gbg_batch_s;
@@ -2883,13 +2982,48 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
   clear_error();
   if (!bt) return set_error(GBG_EARG, "null batch");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  // every gather before any scatter, as one persistent gather launch followed by one
-  // persistent scatter launch would order them: the pooled instances' launches and the
-  // direct instances' single-instance kernels interleave accordingly
   const bool pooled = bt->count > 0;
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, bt->device);
-  if (pooled) {
+  // the direct instances spread over the side streams: gathers by output, scatters by bins
+  // (their sorted quantities) and destination, items sharing either on one side stream
+  std::vector<int> glane, slane;
+  int gk = 0, sk = 0;
+  {
+    std::map<const void *, int> seen;
+    for (const gbg_batch_item &it : bt->direct) {
+      int l = -1;
+      if (it.out) {
+        auto f = seen.find(it.out);
+        l = f != seen.end() ? f->second : gk++ % kSideStreams;
+        seen.emplace(it.out, l);
+      }
+      glane.push_back(l);
+    }
+    seen.clear();
+    for (const gbg_batch_item &it : bt->direct) {
+      int l = -1;
+      if (it.dest) {
+        auto fb = seen.find(it.bins), fd = seen.find(it.dest);
+        if (fb != seen.end() && fd != seen.end() && fb->second != fd->second) l = -2;  // tied to two lanes
+        else l = fb != seen.end() ? fb->second : fd != seen.end() ? fd->second : sk++ % kSideStreams;
+        if (l >= 0) {
+          seen.emplace(it.bins, l);
+          seen.emplace(it.dest, l);
+        }
+      }
+      slane.push_back(l);
+    }
+    gk = std::min(gk, kSideStreams);
+    sk = std::min(sk, kSideStreams);
+  }
+  // a destination shared with a pooled instance, or an item tied to two lanes: the direct
+  // scatters run one after another after the pooled scatter
+  bool serial_scatters = std::count(slane.begin(), slane.end(), -2) > 0;
+  for (const gbg_batch_item &it : bt->direct)
+    if (it.dest && std::find(bt->dests.begin(), bt->dests.end(), it.dest) != bt->dests.end()) serial_scatters = true;
+  auto pooled_gather = [&]() -> gbg_status {
+    if (!pooled) return GBG_OK;
     k_batch_reset<<<1, 256, 0, st>>>(bt->items, bt->counters, bt->qmax_out, bt->count, bt->gidx, bt->ng, bt->goff,
                                      bt->sidx, bt->ns, bt->soff);
     note_launch();
@@ -2909,10 +3043,10 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
       note_launch();
       GBG_CUDA_TRY(cudaGetLastError());
     }
-  }
-  for (const gbg_batch_item &it : bt->direct)
-    if (it.out) GBG_TRY(gbg_interpolate_binned(it.field, it.bins, &it.scheme, GBG_F32, it.out, device_status, stream));
-  if (pooled && bt->nswork > 0) {
+    return GBG_OK;
+  };
+  auto pooled_scatter = [&]() -> gbg_status {
+    if (!pooled || bt->nswork == 0) return GBG_OK;
     GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)bt->scatter_smem));
     GBG_CUDA_TRY(cudaFuncSetAttribute(k_batch_scatter, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
@@ -2930,9 +3064,36 @@ gbg_status gbg_batch_run(gbg_batch bt, int32_t *device_status, void *stream) {
       note_launch();
     }
     GBG_CUDA_TRY(cudaGetLastError());
+    return GBG_OK;
+  };
+  // every gather before any scatter, as one persistent gather launch followed by one
+  // persistent scatter launch would order them (a destination may be another item's field)
+  if (gk > 0) {
+    GBG_TRY(side_run(st, gk, [&](int side, cudaStream_t s) -> gbg_status {
+      for (size_t i = 0; i < bt->direct.size(); ++i)
+        if (glane[i] == side) {
+          const gbg_batch_item &it = bt->direct[i];
+          GBG_TRY(gbg_interpolate_binned(it.field, it.bins, &it.scheme, GBG_F32, it.out, device_status, s));
+        }
+      return GBG_OK;
+    }, pooled_gather));
+  } else {
+    GBG_TRY(pooled_gather());
   }
-  for (const gbg_batch_item &it : bt->direct)
-    if (it.dest) GBG_TRY(gbg_anterpolate_binned(it.dest, it.bins, &it.scheme, GBG_F32, it.q, it.alpha, it.beta, device_status, stream));
+  if (sk > 0 && !serial_scatters) {
+    GBG_TRY(side_run(st, sk, [&](int side, cudaStream_t s) -> gbg_status {
+      for (size_t i = 0; i < bt->direct.size(); ++i)
+        if (slane[i] == side) {
+          const gbg_batch_item &it = bt->direct[i];
+          GBG_TRY(gbg_anterpolate_binned(it.dest, it.bins, &it.scheme, GBG_F32, it.q, it.alpha, it.beta, device_status, s));
+        }
+      return GBG_OK;
+    }, pooled_scatter));
+  } else {
+    GBG_TRY(pooled_scatter());
+    for (const gbg_batch_item &it : bt->direct)
+      if (it.dest) GBG_TRY(gbg_anterpolate_binned(it.dest, it.bins, &it.scheme, GBG_F32, it.q, it.alpha, it.beta, device_status, stream));
+  }
   return GBG_OK;
 }
 

@@ -160,6 +160,27 @@ class PointBins:
         return o
 
 
+def build_bins(pairs, status: torch.Tensor | None = None):
+    """Builds many PointBins at once, each from its own positions: [(bins, positions), ...]
+    (gbg_bins_build_batch).  Independent bins build concurrently on the library's side
+    streams; the result is what bins.build(positions) gives for each."""
+    pairs = [(b, colmajor(p)) for b, p in pairs]
+    n = len(pairs)
+    if n == 0:
+        return []
+    handles = (ctypes.c_void_p * n)(*[b.handle.value for b, _ in pairs])
+    dtypes = (ctypes.c_int32 * n)(*[_DTYPE_CODE[p.dtype] for _, p in pairs])
+    ptrs = (ctypes.c_void_p * n)(*[p.data_ptr() for _, p in pairs])
+    counts = (ctypes.c_int64 * n)(*[int(p.shape[0]) for _, p in pairs])
+    for b, p in pairs:
+        b.npoints = int(p.shape[0])
+        b.status = status
+    _lib.check(_lib.load().gbg_bins_build_batch(handles, dtypes, ptrs, counts, n,
+                                                status.data_ptr() if status is not None else None, _stream()),
+               "gbg_bins_build_batch")
+    return [b for b, _ in pairs]
+
+
 def interpolate_binned(field: ResidentField, bins: PointBins, scheme, out: torch.Tensor | None = None,
                        dtype=torch.float32, status: torch.Tensor | None = None) -> torch.Tensor:
     if out is None:

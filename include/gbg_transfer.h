@@ -277,6 +277,14 @@ gbg_status gbg_bins_set_wait_limit(gbg_bins bins, uint32_t polls);
  * weights. */
 gbg_status gbg_bins_build(gbg_bins bins, gbg_dtype pos_dtype, const void *positions,
                           int64_t npoints, int32_t *device_status, void *stream);
+/* Many bins built in one call: count bins, each from its own positions (dtype, pointer,
+ * count), as gbg_bins_build would build them one after another.  Independent bins build
+ * at the same time on the library's side streams, forked from and joined back to stream
+ * (inside a stream capture: parallel branches of the graph); the same bins twice build in
+ * call order.  The side streams are made by gbg_bins_create and gbg_batch_create.  No
+ * counterpart in the reference. */
+gbg_status gbg_bins_build_batch(const gbg_bins *bins, const gbg_dtype *dtypes, const void *const *positions,
+                                const int64_t *npoints, int32_t count, int32_t *device_status, void *stream);
 /* The binned order as a 1-based traversal order (point_traversal_order's output). */
 gbg_status gbg_bins_order(gbg_bins bins, int32_t *order, void *stream);
 

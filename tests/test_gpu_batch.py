@@ -160,3 +160,22 @@ def test_batch_reports_nonfinite_from_a_direct_instance(gbg, oracle, dev):
     batch.run(status)
     torch.cuda.synchronize()
     assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE
+
+
+def test_batched_bins_builds_match_single_builds(gbg, oracle, dev):
+    """gbg_bins_build_batch over uneven instances (and one bins twice, built in call order)
+    gives every bins the binned order and the results of its own single build."""
+    from gbgperiodicfields_gb300 import resident
+    resident_, insts = make_instances(gbg, oracle, seed=11)
+    want = [i["bins"].order().clone() for i in insts]
+    fresh = [resident.PointBins(i["grid"], i["pos"].shape[0], brick=i["bins"].brick) for i in insts]
+    decoy = gbg.colmajor(torch.rand_like(insts[0]["pos_t"]) * TWO_PI)
+    pairs = [(fresh[0], decoy)] + [(b, i["pos_t"]) for b, i in zip(fresh, insts)]
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    resident.build_bins(pairs, status)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    for b, w, i in zip(fresh, want, insts):
+        assert torch.equal(b.order(), w)
+        assert torch.equal(resident.interpolate_binned(i["field"], b, i["scheme"]),
+                           resident.interpolate_binned(i["field"], i["bins"], i["scheme"]))
