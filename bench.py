@@ -669,13 +669,14 @@ def nufft_form(gbg, lib, dev, n=128, M=2_000_000, samples=32):
 
 def batched_form(gbg, dev):
     """64 instances of uneven sizes (grids 32^3..256^3, 1/3/9 components, 1e3..1e6
-    points log-uniform, cubic or quintic) as one batch, the whole step (bins builds +
-    batch) replayed from a CUDA graph; beside it the same work launched instance by
-    instance."""
+    points log-uniform, cubic or quintic) as one batch, the whole step (batched bins builds
+    + batch) replayed from a CUDA graph; beside it the same work launched instance by
+    instance, and a breakdown by phase.  Each instance class (grid, components, scheme,
+    density) takes the brick and launch shape the autotuner measures on its own points."""
     import torch
     from gbgperiodicfields_gb300 import autotune, resident
     rng = np.random.default_rng(7)
-    insts = []
+    insts, tuned = [], {}
     for _ in range(64):
         nn = int(rng.choice([32, 64, 128, 256]))
         C = int(rng.choice([1, 3, 9]))
@@ -686,14 +687,22 @@ def batched_form(gbg, dev):
             torch.randn((C, nn, nn, nn), device=dev).permute(3, 2, 1, 0))
         dest = resident.ResidentField(grid, C, max_stencil_width=6)
         pos = gbg.colmajor(torch.rand((M, 3), dtype=torch.float64, device=dev) * 2 * np.pi)
-        cfg = autotune.choose(grid.grid_size, C, scheme, M)
+        k = autotune.key(grid.grid_size, C, scheme, M)
+        if k not in tuned:
+            tuned[k] = autotune.tune(grid, C, scheme, pos, bricks=((11, 8, 8), (15, 8, 8), (7, 8, 8), (7, 4, 4)),
+                                     reps=1, persist=False)
+        cfg = tuned[k]
         bins = autotune.apply(resident.PointBins(grid, M, brick=cfg["brick"]).build(pos), cfg)
         insts.append(dict(field=field, dest=dest, bins=bins, scheme=scheme, pos=pos, M=M,
                           out=gbg.empty_colmajor((M, C), torch.float32, dev),
                           q=gbg.colmajor(torch.randn((M, C), device=dev))))
+        torch.cuda.empty_cache()
     total = sum(i["M"] for i in insts)
     batch = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"], dest=i["dest"],
                                  q=i["q"]) for i in insts])
+    gathers = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], out=i["out"]) for i in insts])
+    scatters = resident.Batch([dict(field=i["field"], bins=i["bins"], scheme=i["scheme"], dest=i["dest"], q=i["q"])
+                               for i in insts])
 
     def step():
         resident.build_bins([(i["bins"], i["pos"]) for i in insts])
@@ -706,7 +715,8 @@ def batched_form(gbg, dev):
             resident.anterpolate_binned(i["dest"], i["bins"], i["scheme"], i["q"])
 
     t_seq = _time_ms(seq)
-    t_bins = _time_ms(lambda: resident.build_bins([(i["bins"], i["pos"]) for i in insts]))
+    phases = {"bins_builds": _time_ms(lambda: resident.build_bins([(i["bins"], i["pos"]) for i in insts])),
+              "gathers": _time_ms(gathers.run), "scatters": _time_ms(scatters.run), "batch": _time_ms(batch.run)}
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
@@ -718,10 +728,15 @@ def batched_form(gbg, dev):
         step()
     t_graph = _time_ms(lambda: graph.replay())
     res = {"workload": "64 instances: grids {32,64,128,256}^3, C in {1,3,9}, M log-uniform 1e3..1e6, "
-                       "cubic/quintic, FP32 resident, bricks from the autotuner; bins + the batch, CUDA graph",
+                       "cubic/quintic, FP32 resident, bricks and threads from the autotuner per class; "
+                       "batched bins builds + the batch, CUDA graph",
            "points": int(total), "value": 2 * total / (t_graph / 1e3), "unit": UNIT,
-           "ms_per_step": t_graph, "sequential_ms": t_seq, "bins_builds_ms": t_bins}
-    del insts, batch, graph
+           "ms_per_step": t_graph, "sequential_ms": t_seq, "phase_ms": phases,
+           "tuned_classes": len(tuned),
+           "paths": {"pooled_instances": sum(1 for i in insts if i["M"] < 1024),
+                     "sparse_instances": sum(1 for i in insts if i["M"] < 4 * i["bins"].nbricks_count()),
+                     "instances": len(insts)}}
+    del insts, batch, gathers, scatters, graph
     torch.cuda.empty_cache()
     return res
 

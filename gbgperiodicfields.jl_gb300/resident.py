@@ -95,6 +95,12 @@ class PointBins:
                                               _stream()), "gbg_bins_build")
         return self
 
+    def nbricks_count(self) -> int:
+        """Bricks covering the grid (the brick is the one given, or the library's default)."""
+        import math
+        brick = self.brick or (11, 8, 8)
+        return math.prod(-(-n // b) for n, b in zip(self.grid.grid_size, brick))
+
     def set_launch(self, gather_threads: int = 0, scatter_threads: int = 0):
         """Threads per CTA of the binned gather and scatter (0 = default)."""
         _lib.check(_lib.load().gbg_bins_set_launch(self.handle, int(gather_threads), int(scatter_threads)),
