@@ -314,7 +314,10 @@ __device__ __forceinline__ bool split64(double x, double scale, double shift, in
   const double u = fma(x, scale, shift);
   const bool ok = isfinite(u) && fabs(u) < 9.2e18;
   const long long v = ok ? __double2ll_rd(u) : 0;
-  cell = imod((int64_t)(v >> 32), n);
+  // |u| < 2^63, so the cell word fits 32 bits, and so does n: the periodic wrap in 32-bit
+  // arithmetic (a 64-bit remainder costs several times more)
+  int32_t r = (int32_t)(v >> 32) % (int32_t)n;
+  cell = r < 0 ? r + n : r;
   t = ok ? __uint2float_rz((unsigned)(v & 0xffffffffLL)) * 0x1p-32f : __int_as_float(0x7fc00000);
   return ok;
 }
@@ -323,7 +326,8 @@ __device__ __forceinline__ bool split32(float x, float o, float d, int64_t n, in
   int64_t base;
   float tt;
   const bool ok = locate(x, o, d, base, tt);
-  cell = imod(base, n);
+  cell = base >= INT32_MIN && base <= INT32_MAX ? (int64_t)((int32_t)base % (int32_t)n) : imod(base, n);
+  if (cell < 0) cell += n;
   t = ok ? tt : __int_as_float(0x7fc00000);
   return ok;
 }
@@ -426,11 +430,13 @@ __global__ void __launch_bounds__(kThreads)
         ok &= split32((float)x, g.o32[d], g.d32[d], g.n[d], c[d], t[d]);
     }
     if (!ok && status) atomicOr(status, GBG_DEV_NONFINITE);
-    const int64_t bx = c[0] / g.b[0], by = c[1] / g.b[1], bz = c[2] / g.b[2];
-    const uint32_t lx = (uint32_t)(c[0] - bx * g.b[0]), ly = (uint32_t)(c[1] - by * g.b[1]),
-                   lz = (uint32_t)(c[2] - bz * g.b[2]);
+    // cells, bricks and keys all fit 32 bits (bins hold fewer than 2^32 cells)
+    const uint32_t bx = (uint32_t)c[0] / (uint32_t)g.b[0], by = (uint32_t)c[1] / (uint32_t)g.b[1],
+                   bz = (uint32_t)c[2] / (uint32_t)g.b[2];
+    const uint32_t lx = (uint32_t)c[0] - bx * (uint32_t)g.b[0], ly = (uint32_t)c[1] - by * (uint32_t)g.b[1],
+                   lz = (uint32_t)c[2] - bz * (uint32_t)g.b[2];
     const uint32_t local = (lz * (uint32_t)g.b[1] + ly) * (uint32_t)g.b[0] + lx;
-    const uint32_t key = (uint32_t)(((bz * g.nb[1] + by) * g.nb[0] + bx) * g.bvol + local);
+    const uint32_t key = ((bz * (uint32_t)g.nb[1] + by) * (uint32_t)g.nb[0] + bx) * (uint32_t)g.bvol + local;
     keys[p] = key;
     rank[p] = atomicAdd(counts + key, 1u);
     rec_user[p] = make_float4(t[0], t[1], t[2], __uint_as_float(pack_local(lx, ly, lz)));
@@ -938,11 +944,16 @@ __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__rest
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m;
        s += (int64_t)gridDim.x * blockDim.x) {
     const int64_t p = perm[s];
-    for (int c = 0; c < cp; ++c) {
-      const float v = c < ncomp ? alpha * (float)q[p + m * c] : 0.0f;
-      qs[s * cp + c] = v;
-      const unsigned bits = __float_as_uint(fabsf(v));
-      mx = bits > mx ? bits : mx;
+    // four components at a time into one 16-byte store (cp is 4 or 12)
+    for (int c4 = 0; c4 < cp; c4 += 4) {
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u] = c4 + u < ncomp ? alpha * (float)q[p + m * (c4 + u)] : 0.0f;
+        const unsigned bits = __float_as_uint(fabsf(v[u]));
+        mx = bits > mx ? bits : mx;
+      }
+      reinterpret_cast<float4 *>(qs + s * cp)[c4 / 4] = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 #pragma unroll
@@ -1689,7 +1700,7 @@ gbg_status launch_staged_gather(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme 
       const size_t sm = (size_t)nb * tile_bytes + 64 + 1024;  // + the block's static/reserved share
       return std::min<int>(by_regs, (int)(smem_sm / sm));
     };
-    const int nbuf = (2 * (size_t)tile_bytes + 64 <= 200 * 1024 && ctas(2) >= ctas(1)) ? 2 : 1;
+    const int nbuf = (2 * (size_t)tile_bytes + 64 <= 227 * 1024 && ctas(2) >= ctas(1)) ? 2 : 1;
     const size_t smem = (size_t)nbuf * tile_bytes + 64;
     GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 1;
@@ -2831,7 +2842,7 @@ gbg_status batch_plan(const gbg_batch_item *items, int32_t count, gbg_batch_s *b
   bt->ngwork = (uint32_t)ng;
   bt->nswork = (uint32_t)ns;
   bt->buf_bytes = buf_max;
-  bt->nbuf = 2 * (size_t)buf_max + 64 <= 200 * 1024 ? 2 : 1;
+  bt->nbuf = 2 * (size_t)buf_max + 64 <= 227 * 1024 ? 2 : 1;
   bt->gather_smem = (size_t)bt->nbuf * buf_max + 64;
   bt->scatter_smem = scat_max;
   if (bt->gather_smem > 227 * 1024 || bt->scatter_smem > 227 * 1024)
