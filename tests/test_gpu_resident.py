@@ -273,6 +273,28 @@ def test_multi_chunk_scatter_is_independent_of_the_launch_shape(gbg, oracle, dev
     assert relerr(outs[0].cpu().numpy(), want) <= 1e-5
 
 
+def test_plain_scatter_is_independent_of_brick_and_chunking(gbg, oracle, dev):
+    """Plain FP32 running sums carry across chunks exactly, and a node's order (its stencil's
+    rows z outer, y inner, then its points in binned order) is the same whatever brick holds
+    it; so dense points scattered with a brick whose regions fit one chunk and with one
+    whose regions need several give the same bits."""
+    from gbgperiodicfields_gb300 import resident
+    rng = np.random.default_rng(131)
+    n = (30, 24, 24)
+    grid = gbg.Grid3D(n, (TWO_PI,) * 3)
+    m = 2 * n[0] * n[1] * n[2]
+    pos = torch.from_numpy(np.asfortranarray(TWO_PI * rng.random((m, 3)))).cuda()
+    q = torch.from_numpy(np.asfortranarray(rng.standard_normal((m, 12)))).float().cuda()
+    outs = []
+    for brick in ((3, 4, 4), (15, 8, 8)):
+        bins = resident.PointBins(grid, m, brick=brick).build(pos)
+        bins.set_compensated(False)
+        dest = resident.ResidentField(grid, 12, max_stencil_width=4)
+        resident.anterpolate_binned(dest, bins, gbg.CatmullRom, q)
+        outs.append(dest.read())
+    assert torch.equal(outs[0], outs[1])
+
+
 def test_bounded_tile_wait_reports_timeout(gbg, oracle, dev):
     """A staged gather whose tile wait is allowed a single poll gives up on tiles still in
     flight: the status word says GBG_DEV_TIMEOUT, the call returns, and the context stays
