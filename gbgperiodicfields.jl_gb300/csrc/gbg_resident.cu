@@ -71,6 +71,7 @@ struct gbg_bins_s {
   // work lists rebuilt with the bins: bricks holding a point (gathers), bricks a point's
   // stencil reaches (scatters with beta == 1; valid when reach_ok), and their lengths
   uint32_t *active = nullptr, *reach = nullptr, *lists_n = nullptr;
+  uint32_t *overflow = nullptr;  // the sparse scatter's bricks with too many candidates (count in lists_n[3])
   bool reach_ok = false;
   // corrections of the compensated scatter's regions of several chunks: one slot of
   // bvol * 12 floats per scatter CTA; the scatter launches at most cslots CTAs
@@ -95,6 +96,7 @@ inline void bins_layout(Arena &a, gbg_bins_s *b) {
   b->active = a.take<uint32_t>((size_t)b->nbricks);
   b->reach = a.take<uint32_t>((size_t)b->nbricks);
   b->lists_n = a.take<uint32_t>(4);
+  b->overflow = a.take<uint32_t>((size_t)b->nbricks);
   b->cscratch = a.take<float>((size_t)b->cslots * b->bvol * 12);
 }
 }  // namespace gbg
@@ -1735,6 +1737,225 @@ int32_t neighbour_skip_ok(const int32_t *b, const int64_t *nb, const int64_t *n,
   return 1;
 }
 
+// Sparse scatter, a warp per brick: for point sets with few points a brick the CTA-wide
+// setup of a brick is mostly latency, so each warp takes a brick of its own.  It reads the
+// point ranges of the 27 neighbouring bricks, keeps the points whose cells lie in the
+// brick's region, puts them in region order (cell, then slot) and stages their weights and
+// quantities; each lane then owns node quads and adds the staged points in that order,
+// exactly as the CTA path does -- the same bits.  A brick with more candidates than a
+// warp stages goes to the overflow list, which the CTA kernel takes afterwards.
+constexpr uint32_t kWarpScan = 64, kWarpKeep = 32, kWarpMeta = 4 * kWarpKeep + 64;
+
+template <int N2, int CP>
+constexpr size_t sparse_warp_smem(int warps) {
+  return (size_t)warps * (kWarpKeep * (CP + kScatterWStride<N2>) * sizeof(float) + kWarpMeta * sizeof(uint32_t));
+}
+
+template <int N2, bool FIXED, int CP>
+__global__ void __launch_bounds__(kThreads)
+    k_scatter_sparse(FixGeo g, SchemeT<float, N2> s, const uint32_t *__restrict__ cell_start,
+                     const float4 *__restrict__ rec, const float *__restrict__ qs,
+                     const unsigned *__restrict__ qmax_bits, float *__restrict__ field, float beta, int beta_zero,
+                     int32_t *status, const uint32_t *__restrict__ list, const uint32_t *__restrict__ list_n,
+                     uint32_t *__restrict__ overflow, uint32_t *__restrict__ overflow_n) {
+  constexpr int W = kScatterWStride<N2>;
+  constexpr int BY = N2 <= 6 ? 2 : 1, BZ = BY;
+  constexpr int RY = N2 + BY - 1, RZ = N2 + BZ - 1;
+  constexpr int half = N2 / 2;
+  extern __shared__ __align__(16) unsigned char smem_sparse[];
+  __shared__ float coef[N2 * GBG_MAX_POWERS];
+  for (int i = threadIdx.x; i < N2 * s.m2; i += blockDim.x) coef[i] = s.c[i];
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0 && status && !isfinite(__uint_as_float(*qmax_bits)))
+    atomicOr(status, GBG_DEV_NONFINITE);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+  float *sq = reinterpret_cast<float *>(smem_sparse) + (size_t)wib * kWarpKeep * (CP + W);
+  float *sw = sq + kWarpKeep * CP;
+  uint32_t *meta = reinterpret_cast<uint32_t *>(reinterpret_cast<float *>(smem_sparse) +
+                                                (size_t)nwb * kWarpKeep * (CP + W)) + wib * kWarpMeta;
+  uint32_t *ce = meta, *cs = ce + kWarpKeep, *re = cs + kWarpKeep, *rs = re + kWarpKeep;
+  uint32_t *nst = rs + kWarpKeep, *npre = nst + 28;
+  const int B0 = g.b[0], B1 = g.b[1], B2 = g.b[2];
+  const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
+  const int QY = (B1 + BY - 1) / BY, QZ = (B2 + BZ - 1) / BZ, nquads = B0 * QY * QZ;
+  const uint32_t bvol = (uint32_t)g.bvol;
+  const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t ui = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; ui < nunits; ui += nw) {
+    const int64_t b = list ? (int64_t)__ldg(list + ui) : ui;
+    const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]),
+              bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
+    // the 27 neighbours' point ranges (an axis of one brick has one neighbour, of two two)
+    uint32_t a = 0, c = 0;
+    if (lane < 27) {
+      const int dx = lane % 3 - 1, dy = (lane / 3) % 3 - 1, dz = lane / 9 - 1;
+      const bool dup = (g.nb[0] == 1 && dx != 0) || (g.nb[0] == 2 && dx < 0) || (g.nb[1] == 1 && dy != 0) ||
+                       (g.nb[1] == 2 && dy < 0) || (g.nb[2] == 1 && dz != 0) || (g.nb[2] == 2 && dz < 0);
+      if (!dup) {
+        const uint64_t k = ((uint64_t)((bz + dz + g.nb[2]) % g.nb[2]) * (uint32_t)g.nb[1] +
+                            (uint32_t)((by + dy + g.nb[1]) % g.nb[1])) * (uint32_t)g.nb[0] +
+                           (uint32_t)((bx + dx + g.nb[0]) % g.nb[0]);
+        a = __ldg(cell_start + k * bvol);
+        c = __ldg(cell_start + (k + 1) * bvol) - a;
+      }
+    }
+    uint32_t x = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    const uint32_t total = __shfl_sync(0xffffffffu, x, 31);
+    if (lane < 27) {
+      nst[lane] = a;
+      npre[lane + 1] = x;
+    }
+    if (lane == 0) npre[0] = 0;
+    __syncwarp();
+    bool over = total > kWarpScan;
+    uint32_t kept = 0;
+    if (!over) {
+      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const uint32_t t = t0 + lane;
+        bool keep = false;
+        uint32_t e = 0, slot = 0;
+        if (t < total) {
+          int k = 0;
+          while (k < 26 && npre[k + 1] <= t) ++k;
+          slot = nst[k] + (t - npre[k]);
+          int lx, ly, lz;
+          unpack_local(__ldg(rec + slot).w, lx, ly, lz);
+          const int dx = k % 3 - 1, dy = (k / 3) % 3 - 1, dz = k / 9 - 1;
+          const int cx = ((bx + dx + g.nb[0]) % g.nb[0]) * B0 + lx;
+          const int cy = ((by + dy + g.nb[1]) % g.nb[1]) * B1 + ly;
+          const int cz = ((bz + dz + g.nb[2]) % g.nb[2]) * B2 + lz;
+          int ex = (cx - (bx * B0 - half)) % g.n[0], ey = (cy - (by * B1 - half)) % g.n[1],
+              ez = (cz - (bz * B2 - half)) % g.n[2];
+          if (ex < 0) ex += g.n[0];
+          if (ey < 0) ey += g.n[1];
+          if (ez < 0) ez += g.n[2];
+          keep = ex < E0 && ey < E1 && ez < E2;
+          e = (uint32_t)((ez * E1 + ey) * E0 + ex);
+        }
+        const unsigned ballot = __ballot_sync(0xffffffffu, keep);
+        const uint32_t pos = kept + __popc(ballot & ((1u << lane) - 1u));
+        if (keep && pos < kWarpKeep) {
+          re[pos] = e;
+          rs[pos] = slot;
+        }
+        kept += __popc(ballot);
+      }
+      over = kept > kWarpKeep;
+    }
+    if (over) {
+      if (lane == 0) overflow[atomicAdd(overflow_n, 1u)] = (uint32_t)b;
+      continue;
+    }
+    __syncwarp();
+    // region order: by cell, then slot (binned order within a cell)
+    if ((uint32_t)lane < kept) {
+      const uint32_t e = re[lane], sl = rs[lane];
+      uint32_t rank = 0;
+      for (uint32_t j = 0; j < kept; ++j) rank += (re[j] < e || (re[j] == e && rs[j] < sl)) ? 1u : 0u;
+      ce[rank] = e;
+      cs[rank] = sl;
+    }
+    __syncwarp();
+    // stage the candidates: weights (x, then y and z each with a zero either side) and the
+    // quantities, as the CTA path stages them
+    int nonfinite = 0;
+    if ((uint32_t)lane < kept) {
+      const uint32_t sl = cs[lane];
+      const float4 r = __ldg(rec + sl);
+      float *wt = sw + lane * W;
+      float w[N2];
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.x, w); else weights_rt<N2>(coef, s.m2, r.x, w);
+#pragma unroll
+      for (int q = 0; q < N2; ++q) wt[q] = w[q];
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.y, w); else weights_rt<N2>(coef, s.m2, r.y, w);
+      wt[N2] = 0.0f;
+#pragma unroll
+      for (int q = 0; q < N2; ++q) wt[N2 + 1 + q] = w[q];
+      wt[2 * N2 + 1] = 0.0f;
+      if constexpr (FIXED) weights_ptr<N2>(coef, r.z, w); else weights_rt<N2>(coef, s.m2, r.z, w);
+      wt[2 * N2 + 2] = 0.0f;
+#pragma unroll
+      for (int q = 0; q < N2; ++q) wt[2 * N2 + 3 + q] = w[q];
+      wt[3 * N2 + 3] = 0.0f;
+      const float4 *q4 = reinterpret_cast<const float4 *>(qs + (int64_t)sl * CP);
+      float qa = 0.0f;
+#pragma unroll
+      for (int v = 0; v < CP / 4; ++v) {
+        const float4 xq = __ldg(q4 + v);
+        reinterpret_cast<float4 *>(sq + lane * CP)[v] = xq;
+        qa += fabsf(xq.x) + fabsf(xq.y) + fabsf(xq.z) + fabsf(xq.w);
+      }
+      if (!isfinite(r.x + r.y + r.z + qa)) nonfinite = 1;
+    }
+    const bool exact = __any_sync(0xffffffffu, nonfinite);
+    __syncwarp();
+    const int vx = min(B0, g.n[0] - bx * B0), vy = min(B1, g.n[1] - by * B1), vz = min(B2, g.n[2] - bz * B2);
+    for (int qi = lane; qi < nquads; qi += 32) {
+      const int lx = qi % B0, ly = ((qi / B0) % QY) * BY, lz = (qi / (B0 * QY)) * BZ;
+      float acc[BY * BZ][CP];
+#pragma unroll
+      for (int n = 0; n < BY * BZ; ++n)
+#pragma unroll
+        for (int cc = 0; cc < CP; ++cc) acc[n][cc] = 0.0f;
+      const int xk = lx + N2 - 1;
+      for (uint32_t t = 0; t < kept; ++t) {
+        const uint32_t e = ce[t];
+        const int ex = (int)(e % (uint32_t)E0), ey = (int)((e / (uint32_t)E0) % (uint32_t)E1),
+                  ez = (int)(e / (uint32_t)(E0 * E1));
+        const int jj = ey - ly, kk = ez - lz;
+        if (ex < lx || ex > xk || jj < 0 || jj >= RY || kk < 0 || kk >= RZ) continue;
+        const float *wp = sw + t * W;
+        const float *wy = wp + (2 * N2 - jj), *wz = wp + (3 * N2 + 2 - kk);
+        const float4 *qp = reinterpret_cast<const float4 *>(sq) + t * (CP / 4);
+        const float wx = wp[xk - ex];
+        float q[CP];
+#pragma unroll
+        for (int v = 0; v < CP / 4; ++v) {
+          const float4 t4 = qp[v];
+          q[4 * v] = t4.x;
+          q[4 * v + 1] = t4.y;
+          q[4 * v + 2] = t4.z;
+          q[4 * v + 3] = t4.w;
+        }
+#pragma unroll
+        for (int n = 0; n < BY * BZ; ++n) {
+          const int aa = n % BY, bb = n / BY;
+          if (exact && !(jj - aa >= 0 && jj - aa <= N2 - 1 && kk - bb >= 0 && kk - bb <= N2 - 1)) continue;
+          const float wgt = (wx * wy[aa]) * wz[bb];
+#pragma unroll
+          for (int cc = 0; cc < CP; ++cc) acc[n][cc] = fmaf(wgt, q[cc], acc[n][cc]);
+        }
+      }
+#pragma unroll
+      for (int n = 0; n < BY * BZ; ++n) {
+        const int ny = ly + n % BY, nz = lz + n / BY;
+        if (ny >= B1 || nz >= B2 || lx >= vx || ny >= vy || nz >= vz) continue;
+        const int64_t X = (int64_t)bx * B0 + lx, Y = (int64_t)by * B1 + ny, Z = (int64_t)bz * B2 + nz;
+        float4 *d = reinterpret_cast<float4 *>(field + ((X + g.halo) + g.px * ((Y + g.halo) + g.py * (Z + g.halo))) * CP);
+#pragma unroll
+        for (int v4 = 0; v4 < CP / 4; ++v4) {
+          float v[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) v[u] = 4 * v4 + u < g.ncomp ? acc[n][4 * v4 + u] : 0.0f;
+          if (beta_zero) {
+            d[v4] = make_float4(v[0], v[1], v[2], v[3]);
+          } else {
+            const float4 o = d[v4];
+            d[v4] = make_float4(__fadd_rn(__fmul_rn(beta, o.x), v[0]), __fadd_rn(__fmul_rn(beta, o.y), v[1]),
+                                __fadd_rn(__fmul_rn(beta, o.z), v[2]), __fadd_rn(__fmul_rn(beta, o.w), v[3]));
+          }
+        }
+      }
+    }
+    __syncwarp();  // the warp's staging is free for its next brick
+  }
+}
+
 template <int N2, bool FIXED>
 gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme &sch, double beta,
                                  const unsigned *qmax_bits, int32_t *status, cudaStream_t st) {
@@ -1763,6 +1984,7 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int threads = b->scatter_threads ? b->scatter_threads : kThreads;
+  const bool reach = beta == 1.0 && b->reach_ok;
   auto go = [&](auto kernel) -> gbg_status {
     scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(g, f->cp, N2));
     const size_t smem = scatter_nodes_smem(g, f->cp, N2);
@@ -1773,7 +1995,6 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     const int blocks = (int)std::min<int64_t>(b->cslots, (int64_t)sms * std::max(per_sm, 1));
     mark_main_start(st);
-    const bool reach = beta == 1.0 && b->reach_ok;
     kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
                                            beta == 0.0, status, reach ? b->reach : nullptr, b->lists_n + 1);
     mark_main_stop(st);
@@ -1781,6 +2002,46 @@ gbg_status launch_staged_scatter(gbg_field_s *f, gbg_bins_s *b, const gbg_scheme
     GBG_CUDA_TRY(cudaGetLastError());
     return GBG_OK;
   };
+  if (g.sparse) {
+    // the warp kernel over every brick (or the bricks a point reaches), then the CTA kernel
+    // over the bricks it passed on
+    GBG_CUDA_TRY(cudaMemsetAsync(b->lists_n + 3, 0, sizeof(uint32_t), st));
+    auto sp = [&](auto kernel, size_t smem) -> gbg_status {
+      GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      int per_sm = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+      // a warp per brick; the list of bricks in reach, when there is one, may hold fewer
+      const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((b->nbricks + 7) / 8, (int64_t)sms * std::max(per_sm, 1)));
+      kernel<<<blocks, kThreads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
+                                              beta == 0.0, status, reach ? b->reach : nullptr, b->lists_n + 1,
+                                              b->overflow, b->lists_n + 3);
+      note_launch();
+      GBG_CUDA_TRY(cudaGetLastError());
+      return GBG_OK;
+    };
+    mark_main_start(st);
+    if (f->cp == 4) GBG_TRY(sp(k_scatter_sparse<N2, FIXED, 4>, sparse_warp_smem<N2, 4>(kThreads / 32)));
+    else GBG_TRY(sp(k_scatter_sparse<N2, FIXED, 12>, sparse_warp_smem<N2, 12>(kThreads / 32)));
+    auto over = [&](auto kernel) -> gbg_status {
+      scatter_nodes_chunk(g, f->cp, N2, scatter_nodes_budget(g, f->cp, N2));
+      const size_t smem = scatter_nodes_smem(g, f->cp, N2);
+      if (smem > 227 * 1024) return set_error(GBG_EUNSUPPORTED, "brick too large for the scatter's shared memory");
+      GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      GBG_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+      int per_sm = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+      const int blocks = (int)std::min<int64_t>(b->cslots, (int64_t)sms * std::max(per_sm, 1));
+      kernel<<<blocks, threads, smem, st>>>(g, s, b->cell_start, b->rec, b->qs, qmax_bits, f->data, (float)beta,
+                                             beta == 0.0, status, b->overflow, b->lists_n + 3);
+      note_launch();
+      GBG_CUDA_TRY(cudaGetLastError());
+      return GBG_OK;
+    };
+    if (f->cp == 4) GBG_TRY(over(k_scatter_nodes<N2, FIXED, 4>));
+    else GBG_TRY(over(k_scatter_nodes<N2, FIXED, 12>));
+    mark_main_stop(st);
+    return GBG_OK;
+  }
   if (f->cp == 4) return go(k_scatter_nodes<N2, FIXED, 4>);
   return go(k_scatter_nodes<N2, FIXED, 12>);
 }
