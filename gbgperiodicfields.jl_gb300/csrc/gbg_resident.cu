@@ -1744,7 +1744,7 @@ int32_t neighbour_skip_ok(const int32_t *b, const int64_t *nb, const int64_t *n,
 // quantities; each lane then owns node quads and adds the staged points in that order,
 // exactly as the CTA path does -- the same bits.  A brick with more candidates than a
 // warp stages goes to the overflow list, which the CTA kernel takes afterwards.
-constexpr uint32_t kWarpScan = 64, kWarpKeep = 32, kWarpMeta = 4 * kWarpKeep + 64;
+constexpr uint32_t kWarpScan = 128, kWarpKeep = 32, kWarpMeta = 4 * kWarpKeep + 64;
 
 template <int N2, int CP>
 constexpr size_t sparse_warp_smem(int warps) {
