@@ -13,7 +13,10 @@ package, so the format is implemented here.  What is covered:
   attributes in object headers or densely, contiguous and compact datasets (chunked
   ones with the version 1 B-tree chunk index, unfiltered or deflate-compressed), the
   fixed-point, floating-point, string, compound (a pair r/i of floats reads as
-  complex), enum, and variable-length string types; every checksum is verified;
+  complex), enum, and variable-length string types; every checksum is verified
+  (the chunked reader is checked by no file in the tests: HDF5.jl, MATLAB and this
+  writer store contiguous datasets by default, and no chunked file written by libhdf5
+  is at hand);
 * writing: superblock version 2, version 2 object headers, compact links and
   attributes, contiguous datasets, the same datatypes as the reader (strings as
   fixed-length UTF-8, complex as the compound {r, i} HDF5.jl uses); the result is a
