@@ -730,18 +730,33 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
     tma_load_tile(smem + buf * tile_bytes, &tmap, 0, (int)(bx * g.b[0]) + g.box_off,
                   (int)(by * g.b[1]) + g.box_off, (int)(bz * g.b[2]) + g.box_off, bars + buf);
   };
-  auto nonempty = [&](int64_t b) { return __ldg(cell_start + (b + 1) * g.bvol) > __ldg(cell_start + b * g.bvol); };
-
   // the bricks to visit: the bins' list of bricks holding points, or every brick
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
   auto unit = [&](int64_t i) -> int64_t { return i >= nunits ? -1 : (list ? (int64_t)__ldg(list + i) : i); };
   int64_t ui = blockIdx.x;
-  if (threadIdx.x == 0 && unit(ui) >= 0 && nonempty(unit(ui))) issue(unit(ui), 0);
+  // a brick's point range and each quarter-warp's first record are loaded one brick ahead
+  uint32_t s0 = 0, s1 = 0;
+  float4 r_next = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t p_next = 0u;
+  if (unit(ui) >= 0) {
+    s0 = __ldg(cell_start + unit(ui) * g.bvol);
+    s1 = __ldg(cell_start + (unit(ui) + 1) * g.bvol);
+    if (threadIdx.x == 0 && s1 > s0) issue(unit(ui), 0);
+    if (s0 + qw < s1) {
+      r_next = __ldg(rec + s0 + qw);
+      p_next = __ldg(perm + s0 + qw);
+    }
+  }
   for (int it = 0; ui < nunits; ++it, ui += gridDim.x) {
     const int buf = nbuf == 2 ? (it & 1) : 0;
-    const int64_t b = unit(ui), bn = unit(ui + gridDim.x);
-    const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
-    if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
+    const int64_t bn = unit(ui + gridDim.x);
+    uint32_t n0 = 0, n1 = 0;
+    if (bn >= 0) {
+      n0 = __ldg(cell_start + bn * g.bvol);
+      n1 = __ldg(cell_start + (bn + 1) * g.bvol);
+    }
+    if (nbuf == 2 && threadIdx.x == 0 && n1 > n0) issue(bn, buf ^ 1);
+    bool ahead = false;  // this quarter-warp's first record of the next brick is loading
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
       if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf], g.wait_polls))) {
@@ -751,23 +766,30 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
       }
       phase[buf] ^= 1;
       pending[buf] = false;
-      uint32_t sl = s0 + qw;
-      float4 r_next = sl < s1 ? __ldg(rec + sl) : make_float4(0.f, 0.f, 0.f, 0.f);
-      uint32_t p_next = sl < s1 ? __ldg(perm + sl) : 0u;
-      for (; sl < s1; sl += nqw) {
+      for (uint32_t sl = s0 + qw; sl < s1; sl += nqw) {
         const float4 r = r_next;
         const int64_t p = p_next;
         if (sl + nqw < s1) {
           r_next = __ldg(rec + sl + nqw);
           p_next = __ldg(perm + sl + nqw);
+        } else if (n0 + qw < n1) {
+          r_next = __ldg(rec + n0 + qw);
+          p_next = __ldg(perm + n0 + qw);
+          ahead = true;
         }
         gather4_point<M2, CP>(s, cx, cya, cyb, qi, jj, sub, seg_mask, r, p,
                               reinterpret_cast<const float *>(smem + buf * tile_bytes), g.w[0], g.w[0] * g.w[1], 0,
                               out, g.m, g.ncomp);
       }
     }
+    if (!ahead && n0 + qw < n1) {
+      r_next = __ldg(rec + n0 + qw);
+      p_next = __ldg(perm + n0 + qw);
+    }
     __syncthreads();  // every lane is done with this buffer before it is refilled
-    if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
+    if (nbuf == 1 && threadIdx.x == 0 && n1 > n0) issue(bn, 0);
+    s0 = n0;
+    s1 = n1;
   }
   if (failed && threadIdx.x == 0) {
     // a copy that did not complete in time: let every copy still in flight land (with the
@@ -847,17 +869,33 @@ __global__ void __launch_bounds__(kThreads, 1)
     tma_load_tile(smem + buf * tile_bytes, &tmap, 0, (int)(bx * g.b[0]) + g.box_off,
                   (int)(by * g.b[1]) + g.box_off, (int)(bz * g.b[2]) + g.box_off, bars + buf);
   };
-  auto nonempty = [&](int64_t b) { return __ldg(cell_start + (b + 1) * g.bvol) > __ldg(cell_start + b * g.bvol); };
   // the bricks to visit: the bins' list of bricks holding points, or every brick
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
   auto unit = [&](int64_t i) -> int64_t { return i >= nunits ? -1 : (list ? (int64_t)__ldg(list + i) : i); };
   int64_t ui = blockIdx.x;
-  if (threadIdx.x == 0 && unit(ui) >= 0 && nonempty(unit(ui))) issue(unit(ui), 0);
+  // a brick's point range and each thread's first record are loaded one brick ahead
+  uint32_t s0 = 0, s1 = 0;
+  float4 r_next = make_float4(0.f, 0.f, 0.f, 0.f);
+  uint32_t p_next = 0u;
+  if (unit(ui) >= 0) {
+    s0 = __ldg(cell_start + unit(ui) * g.bvol);
+    s1 = __ldg(cell_start + (unit(ui) + 1) * g.bvol);
+    if (threadIdx.x == 0 && s1 > s0) issue(unit(ui), 0);
+    if (s0 + threadIdx.x < s1) {
+      r_next = __ldg(rec + s0 + threadIdx.x);
+      p_next = __ldg(perm + s0 + threadIdx.x);
+    }
+  }
   for (int it = 0; ui < nunits; ++it, ui += gridDim.x) {
     const int buf = nbuf == 2 ? (it & 1) : 0;
-    const int64_t b = unit(ui), bn = unit(ui + gridDim.x);
-    const uint32_t s0 = __ldg(cell_start + b * g.bvol), s1 = __ldg(cell_start + (b + 1) * g.bvol);
-    if (nbuf == 2 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, buf ^ 1);
+    const int64_t bn = unit(ui + gridDim.x);
+    uint32_t n0 = 0, n1 = 0;
+    if (bn >= 0) {
+      n0 = __ldg(cell_start + bn * g.bvol);
+      n1 = __ldg(cell_start + (bn + 1) * g.bvol);
+    }
+    if (nbuf == 2 && threadIdx.x == 0 && n1 > n0) issue(bn, buf ^ 1);
+    bool ahead = false;  // this thread's first record of the next brick is loading
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
       if (__syncthreads_or(!mbar_wait(bars + buf, phase[buf], g.wait_polls))) {
@@ -868,12 +906,28 @@ __global__ void __launch_bounds__(kThreads, 1)
       phase[buf] ^= 1;
       pending[buf] = false;
       for (uint32_t sl = s0 + threadIdx.x; sl < s1; sl += blockDim.x) {
-        gather_point<N2, M2, CP>(s, __ldg(rec + sl), perm[sl], reinterpret_cast<const float *>(smem + buf * tile_bytes),
-                                 g.w[0], g.w[0] * g.w[1], 0, out, g.m, g.ncomp);
+        const float4 r = r_next;
+        const int64_t p = p_next;
+        if (sl + blockDim.x < s1) {
+          r_next = __ldg(rec + sl + blockDim.x);
+          p_next = __ldg(perm + sl + blockDim.x);
+        } else if (n0 + threadIdx.x < n1) {
+          r_next = __ldg(rec + n0 + threadIdx.x);
+          p_next = __ldg(perm + n0 + threadIdx.x);
+          ahead = true;
+        }
+        gather_point<N2, M2, CP>(s, r, p, reinterpret_cast<const float *>(smem + buf * tile_bytes), g.w[0],
+                                 g.w[0] * g.w[1], 0, out, g.m, g.ncomp);
       }
     }
+    if (!ahead && n0 + threadIdx.x < n1) {
+      r_next = __ldg(rec + n0 + threadIdx.x);
+      p_next = __ldg(perm + n0 + threadIdx.x);
+    }
     __syncthreads();
-    if (nbuf == 1 && threadIdx.x == 0 && bn >= 0 && nonempty(bn)) issue(bn, 0);
+    if (nbuf == 1 && threadIdx.x == 0 && n1 > n0) issue(bn, 0);
+    s0 = n0;
+    s1 = n1;
   }
   if (failed && threadIdx.x == 0)
     for (int i = 0; i < nbuf; ++i)
@@ -966,6 +1020,13 @@ __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__rest
   if ((threadIdx.x & 31) == 0) atomicMax(qmax_bits, mx);
 }
 
+// Four-byte asynchronous copies global -> shared (cp.async), their commit and wait.
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // One compensated step (Knuth's TwoSum, every operation rounded on its own): s + x into
 // the pair (s, c), c collecting the exact rounding error of each addition.
 __device__ __forceinline__ void twosum_add(float &s, float &c, float x) {
@@ -1021,8 +1082,8 @@ __device__ __forceinline__ void weights_rt(const float *c, int m2, float t, floa
 // several chunks keeps its sums' corrections in the CTA's own slot of a global scratch.)
 size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
   const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
-  return sizeof(float) * (size_t)g.bvol * cp + sizeof(uint32_t) * (2 * ecount + 1 + (size_t)(g.e[0] + g.e[1] + g.e[2])) +
-         16;
+  return sizeof(float) * (size_t)g.bvol * cp +
+         sizeof(uint32_t) * (2 * ecount + 1 + 2 * (size_t)(g.e[0] + g.e[1] + g.e[2])) + 16;
 }
 
 // Floats of weights per staged point: the N2 x weights, then the y and the z weights each
@@ -1090,10 +1151,11 @@ int32_t scatter_sparse(const gbg_bins_s *b, const gbg_grid &grid, int n2) {
 // All index arithmetic is 32-bit: the region's cell keys come from three per-axis tables
 // (key = kx[ex] + ky[ey] + kz[ez]).
 template <int N2, bool FIXED, int CP, int SU>
-__device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, int64_t b,
+__device__ bool scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, int64_t b,
                                     const uint32_t *__restrict__ cell_start, const float4 *__restrict__ rec,
                                     const float *__restrict__ qs, float *__restrict__ field, float beta,
-                                    int beta_zero, bool listed, unsigned char *smem, uint32_t *warp_tot) {
+                                    int beta_zero, bool listed, unsigned char *smem, uint32_t *warp_tot,
+                                    int64_t next = -1, bool have = false) {
   const int E0 = g.e[0], E1 = g.e[1], E2 = g.e[2];
   const int ecount = E0 * E1 * E2;
   const int bvol = (int)g.bvol;
@@ -1105,7 +1167,15 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   uint32_t *off = reinterpret_cast<uint32_t *>(sacc + bvol * CP + g.chunk * (CP + kScatterWStride<N2>));
   uint32_t *r0s = off + ecount + 1;
   uint32_t *kx = r0s + ecount, *ky = kx + E0, *kz = ky + E1;
-  unsigned char *scx = reinterpret_cast<unsigned char *>(kz + E2);
+  uint32_t *knx = kz + E2;  // the next brick's per-axis key tables (same layout)
+  unsigned char *scx = reinterpret_cast<unsigned char *>(knx + E0 + E1 + E2);
+  // the next brick's cell table, copied by cp.async while this brick computes: the last
+  // 2 * ecount words of the staging area (first slots, then ends)
+  uint32_t *pre_a = off - 2 * ecount, *pre_z = off - ecount;
+  if (have) {
+    cp_async_wait_all();
+    __syncthreads();
+  }
   constexpr int half = N2 / 2;
   const int bx = (int)(b % g.nb[0]), by = (int)((b / g.nb[0]) % g.nb[1]), bz = (int)(b / ((int64_t)g.nb[0] * g.nb[1]));
   const int B0 = g.b[0], B1 = g.b[1];
@@ -1126,7 +1196,7 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     }
     any = __syncthreads_or(mine);
   }
-  if (!any && !beta_zero && beta == 1.0f) return;  // the brick keeps its values
+  if (!any && !beta_zero && beta == 1.0f) return false;  // the brick keeps its values
   uint32_t count = 0;
   // A point set sparse on its grid: the region's points are taken from the ranges of the
   // 27 neighbouring bricks, kept when their cell lies in the region and put in region
@@ -1214,19 +1284,33 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   }
   if (any && !sparse) {
     // per-axis key tables of the region's cells (periodic wrap, then brick and local index)
-    for (int t = threadIdx.x; t < E0 + E1 + E2; t += blockDim.x) {
-      const int d = t < E0 ? 0 : (t < E0 + E1 ? 1 : 2);
-      const int e = t - (d == 0 ? 0 : (d == 1 ? E0 : E0 + E1));
-      const int bc = d == 0 ? bx : (d == 1 ? by : bz);
+    // this brick's tables (unless its cell table was copied ahead) and the next brick's
+    const int ET = E0 + E1 + E2;
+    for (int t = threadIdx.x; t < 2 * ET; t += blockDim.x) {
+      const bool nxt = t >= ET;
+      if (nxt ? next < 0 : have) continue;
+      const int tt = nxt ? t - ET : t;
+      const int64_t bb = nxt ? next : b;
+      const int d = tt < E0 ? 0 : (tt < E0 + E1 ? 1 : 2);
+      const int e = tt - (d == 0 ? 0 : (d == 1 ? E0 : E0 + E1));
+      const int bc = d == 0 ? (int)(bb % g.nb[0]) : (d == 1 ? (int)((bb / g.nb[0]) % g.nb[1]) : (int)(bb / ((int64_t)g.nb[0] * g.nb[1])));
       int c = (bc * g.b[d] - half + e) % g.n[d];
       if (c < 0) c += g.n[d];
       const uint32_t cb = (uint32_t)c / (uint32_t)g.b[d], cl = (uint32_t)c - cb * (uint32_t)g.b[d];
-      if (d == 0) kx[e] = cb * (uint32_t)bvol + cl;
-      else if (d == 1) ky[e] = (cb * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)g.b[0];
-      else kz[e] = (cb * (uint32_t)g.nb[1] * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)(g.b[0] * g.b[1]);
+      uint32_t key;
+      if (d == 0) key = cb * (uint32_t)bvol + cl;
+      else if (d == 1) key = (cb * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)g.b[0];
+      else key = (cb * (uint32_t)g.nb[1] * (uint32_t)g.nb[0]) * (uint32_t)bvol + cl * (uint32_t)(g.b[0] * g.b[1]);
+      (nxt ? knx : kx)[tt] = key;
     }
     __syncthreads();
-    {
+    if (have) {
+      for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+        const uint32_t a = pre_a[e];
+        r0s[e] = a;
+        off[e] = pre_z[e] - a;
+      }
+    } else {
       // eight cells per thread in flight (one round for a 15x8x8 brick's 2178 cells at
       // 256 threads): their keys first, then all sixteen loads
       constexpr int U = 8;
@@ -1273,6 +1357,7 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
   constexpr int RY = N2 + BY - 1, RZ = N2 + BZ - 1;
   const int QY = (B1 + BY - 1) / BY, QZ = (g.b[2] + BZ - 1) / BZ;
   const int nquads = B0 * QY * QZ, slab = E1 * E0;
+  bool issued = false;
   for (uint32_t c0 = 0;; c0 += (uint32_t)P) {
     const uint32_t c1 = min(count, c0 + (uint32_t)P);
     const bool first = c0 == 0, last = c1 == count;
@@ -1376,6 +1461,26 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     // nodes it reaches; otherwise a point adds w*q to all of a quad's nodes, with w == 0
     // exactly for the nodes it does not reach, and fmaf(0, q, s) == s for finite q
     const bool exact = __syncthreads_or(nonfinite);
+    // a region staged at once leaves the end of the staging area free while the quads run:
+    // the next brick's cell table goes there
+    if (one && next >= 0 && !sparse &&
+        P * CP + (int)count * kScatterWStride<N2> + 2 * ecount <= bvol * CP + g.chunk * (CP + kScatterWStride<N2>)) {
+      int ex = (int)threadIdx.x % E0, ey = ((int)threadIdx.x / E0) % E1, ez = (int)threadIdx.x / (E0 * E1);
+      const int sx = (int)blockDim.x % E0, sy = ((int)blockDim.x / E0) % E1, sz = (int)blockDim.x / (E0 * E1);
+      const uint32_t *kny = knx + E0, *knz = kny + E1;
+      for (int e = threadIdx.x; e < ecount; e += blockDim.x) {
+        const uint32_t key = knx[ex] + kny[ey] + knz[ez];
+        cp_async4(pre_a + e, cell_start + key);
+        cp_async4(pre_z + e, cell_start + key + 1);
+        ex += sx;
+        ey += sy;
+        ez += sz;
+        if (ex >= E0) { ex -= E0; ++ey; }
+        if (ey >= E1) { ey -= E1; ++ez; }
+      }
+      cp_async_commit();
+      issued = true;
+    }
     for (int qi = threadIdx.x; qi < nquads; qi += blockDim.x) {
       const int lx = qi % B0, ly = ((qi / B0) % QY) * BY, lz = (qi / (B0 * QY)) * BZ;
       float acc[BY * BZ][CP];
@@ -1582,6 +1687,7 @@ __device__ void scatter_brick_nodes(const FixGeo &g, const float *coef, int m2, 
     if (last) break;
   }
   __syncthreads();
+  return issued;
 }
 
 template <int N2, bool FIXED, int CP>
@@ -1601,9 +1707,14 @@ __global__ void __launch_bounds__(kThreads, 2)
     atomicOr(status, GBG_DEV_NONFINITE);
   // the bricks to write: those a point reaches (beta == 1 leaves the others unchanged), or all
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
-  for (int64_t ui = blockIdx.x; ui < nunits; ui += gridDim.x)
-    scatter_brick_nodes<N2, FIXED, CP, CP == 4 ? 3 : 1>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start, rec, qs,
-                                       field, beta, beta_zero, list != nullptr, smem_scatter, warp_tot);
+  bool have = false;  // this brick's cell table was copied during the previous brick
+  for (int64_t ui = blockIdx.x; ui < nunits; ui += gridDim.x) {
+    const int64_t un = ui + gridDim.x;
+    const int64_t next = (g.sparse || un >= nunits) ? -1 : (list ? (int64_t)__ldg(list + un) : un);
+    have = scatter_brick_nodes<N2, FIXED, CP, CP == 4 ? 3 : 1>(g, coef, s.m2, list ? (int64_t)__ldg(list + ui) : ui, cell_start,
+                                                        rec, qs, field, beta, beta_zero, list != nullptr, smem_scatter,
+                                                        warp_tot, next, have);
+  }
 }
 
 gbg_status check_field_bins(const gbg_field_s *f, const gbg_bins_s *b, const gbg_scheme *s) {

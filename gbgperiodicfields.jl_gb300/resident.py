@@ -45,8 +45,9 @@ class ResidentField:
         return int(n.value)
 
     def load(self, data: torch.Tensor):
-        """Import a reference-layout (Nx, Ny, Nz, ncomp) array (Float32 or Float64)."""
-        data = colmajor(data)
+        """Import a reference-layout (Nx, Ny, Nz, ncomp) array (Float32 or Float64); a host
+        array is copied to the device first (the import kernel reads device memory)."""
+        data = colmajor(data if data.is_cuda else data.cuda())
         if tuple(data.shape[:3]) != self.grid.grid_size or data.numel() != self.grid.npoints * self.ncomp:
             raise _lib.ArgumentError("field data does not match the resident field's shape")
         _lib.check(_lib.load().gbg_field_import(self.handle, _DTYPE_CODE[data.dtype], data.data_ptr(), _stream()),
@@ -54,10 +55,15 @@ class ResidentField:
         return self
 
     def read(self, dtype=torch.float64, device="cuda") -> torch.Tensor:
-        out = empty_colmajor(self.grid.grid_size + (self.ncomp,), dtype, device)
+        """The field in the reference layout (Nx, Ny, Nz, ncomp), column-major, on `device`.
+        The export kernel always writes device memory; a host result is copied from it
+        after the kernel (a host pointer handed to the kernel would be written
+        asynchronously where the GPU can address host memory, and read too early)."""
+        dev = torch.device(device)
+        out = empty_colmajor(self.grid.grid_size + (self.ncomp,), dtype, dev if dev.type == "cuda" else "cuda")
         _lib.check(_lib.load().gbg_field_export(self.handle, _DTYPE_CODE[dtype], out.data_ptr(), _stream()),
                    "gbg_field_export")
-        return out
+        return out if dev.type == "cuda" else out.to(dev)
 
 
 class PointBins:
@@ -87,6 +93,8 @@ class PointBins:
             self.handle = None
 
     def build(self, positions: torch.Tensor, status: torch.Tensor | None = None):
+        if not positions.is_cuda:
+            raise _lib.ArgumentError("positions must be a CUDA tensor")
         positions = colmajor(positions)
         self.npoints = int(positions.shape[0])
         self.status = status
@@ -132,6 +140,8 @@ class PointBins:
 
     def permute(self, src: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """An (M, ncols) array copied into the bins' sorted order (gbg_bins_permute)."""
+        if not src.is_cuda or (out is not None and not out.is_cuda):
+            raise _lib.ArgumentError("src and out must be CUDA tensors")
         src = colmajor(src)
         two = src if src.dim() == 2 else src.reshape(src.shape[0], -1)
         if out is None:

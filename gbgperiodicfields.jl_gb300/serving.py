@@ -82,14 +82,16 @@ class Server:
         m = int(positions.shape[0])
         if out is None:
             out = empty_colmajor((m, field.ncomp), torch.float32, "cuda")
-        if out.dtype != torch.float32 or tuple(out.shape) != (m, field.ncomp):
-            raise _lib.ArgumentError("out must be a Float32 (M, ncomp) tensor")
+        if out.dtype != torch.float32 or tuple(out.shape) != (m, field.ncomp) or not out.is_cuda:
+            raise _lib.ArgumentError("out must be a Float32 (M, ncomp) CUDA tensor")
         out = colmajor(out)
         return self._submit(_lib.GBG_REQ_INTERPOLATE, field, positions, scheme, out=out)
 
     def anterpolate(self, field: ResidentField, positions: torch.Tensor, scheme, q: torch.Tensor,
                     alpha: float = 1.0, beta: float = 0.0):
         """Queue field = alpha * W^T q + beta * field; q is FP32 (M, ncomp)."""
+        if not q.is_cuda:
+            raise _lib.ArgumentError("q must be a CUDA tensor")
         q = colmajor(q.to(torch.float32))
         if tuple(q.shape) != (int(positions.shape[0]), field.ncomp):
             raise _lib.DimensionMismatch("q must be (M, ncomp)")

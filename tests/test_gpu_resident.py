@@ -311,3 +311,23 @@ def test_bounded_tile_wait_reports_timeout(gbg, oracle, dev):
     torch.cuda.synchronize()
     assert int(status.item()) == 0
     assert relerr(got, oracle.gather(g, f, pos, gbg.CatmullRom.coefficients)) <= 1e-5
+
+
+def test_host_read_and_import_equal_the_device_path(gbg, dev):
+    """A field read to the host is the device read, bitwise, taken after the export kernel
+    has finished (a large field, so an early host read would see unwritten data); a host
+    array imports like the same array on the device."""
+    from gbgperiodicfields_gb300 import resident
+    grid = gbg.Grid3D((128, 128, 128), (TWO_PI,) * 3)
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    data = torch.randn((12, 128, 128, 128), device=dev, generator=g).permute(3, 2, 1, 0)
+    f = resident.ResidentField(grid, 12, max_stencil_width=4).load(data)
+    for _ in range(3):
+        host = f.read(dtype=torch.float32, device="cpu")
+        assert host.device.type == "cpu" and host.stride() == (1, 128, 128 * 128, 128 ** 3)
+        assert torch.equal(host, data.cpu())
+    h = resident.ResidentField(grid, 12, max_stencil_width=4).load(data.cpu())
+    assert torch.equal(h.read(dtype=torch.float32), data)
+    with pytest.raises(gbg.ArgumentError):
+        resident.PointBins(grid, 10).build(torch.zeros((10, 3), dtype=torch.float64))
