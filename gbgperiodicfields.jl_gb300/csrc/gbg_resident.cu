@@ -310,15 +310,42 @@ struct BinGeom {
   float o32[3], d32[3];       // Float32 positions: the reference's _locate in T
 };
 
+// floor(u) of a double with |u| < 9.2e18, from its bits by integer instructions (GB300
+// runs FP64 compares and conversions at the FP64 rate, a few per clock per SM); ok is
+// false for NaN, infinities and |u| >= 9.2e18, and the result is then 0.
+__device__ __forceinline__ long long floor_bits(double u, bool &ok) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(u);
+  const unsigned long long a = bits & 0x7FFFFFFFFFFFFFFFull;
+  ok = a < 0x43DFEB3DD0676600ull;  // the bits of 9.2e18 (positive doubles order as integers)
+  const int ex = (int)(a >> 52);
+  const unsigned long long man = (a & 0xFFFFFFFFFFFFFull) | (ex ? 0x10000000000000ull : 0ull);
+  const int sh = 1075 - ex;  // |u| = man * 2^-sh
+  unsigned long long ip, fr;
+  if (sh <= 0) {
+    ip = man << (-sh < 11 ? -sh : 0);
+    fr = 0;
+  } else if (sh >= 64) {
+    ip = 0;
+    fr = man;
+  } else {
+    ip = man >> sh;
+    fr = man & ((1ull << sh) - 1);
+  }
+  long long v = (long long)ip;
+  if (bits >> 63) v = -v - (fr != 0 ? 1 : 0);
+  return ok ? v : 0;
+}
+
 // Splits one FP64 coordinate into (cell, fraction) in FP64 fixed point.
 __device__ __forceinline__ bool split64(double x, double scale, double shift, int64_t n,
                                         int64_t &cell, float &t) {
   const double u = fma(x, scale, shift);
-  const bool ok = isfinite(u) && fabs(u) < 9.2e18;
-  const long long v = ok ? __double2ll_rd(u) : 0;
+  bool ok;
+  const long long v = floor_bits(u, ok);
   // |u| < 2^63, so the cell word fits 32 bits, and so does n: the periodic wrap in 32-bit
   // arithmetic (a 64-bit remainder costs several times more)
-  int32_t r = (int32_t)(v >> 32) % (int32_t)n;
+  const int32_t c = (int32_t)(v >> 32);
+  const int32_t r = (uint32_t)c < (uint32_t)n ? c : c % (int32_t)n;  // no division inside the box
   cell = r < 0 ? r + n : r;
   t = ok ? __uint2float_rz((unsigned)(v & 0xffffffffLL)) * 0x1p-32f : __int_as_float(0x7fc00000);
   return ok;
