@@ -497,9 +497,19 @@ __global__ void k_brick_lists(const uint32_t *__restrict__ cell_start, int64_t n
 
 __global__ void k_gather_records(const float4 *__restrict__ rec_user, const uint32_t *__restrict__ perm,
                                  int64_t m, float4 *__restrict__ rec) {
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m;
-       s += (int64_t)gridDim.x * blockDim.x)
-    rec[s] = __ldg(rec_user + perm[s]);
+  // four slots a trip: their indices, then their records, then the stores
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += 4 * stride) {
+    uint32_t p[4];
+    float4 r[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) p[u] = s + u * stride < m ? __ldg(perm + s + u * stride) : 0u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) r[u] = s + u * stride < m ? __ldg(rec_user + p[u]) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (s + u * stride < m) rec[s + u * stride] = r[u];
+  }
 }
 
 __global__ void k_order_from_perm(const uint32_t *__restrict__ perm, int32_t *__restrict__ order, int64_t m) {
@@ -1019,24 +1029,36 @@ __global__ void __launch_bounds__(kThreads)
 // Sorted, alpha-scaled quantities: qs[s*CP + c] = T(alpha) * q[perm[s] + M*c].
 // Also the largest |alpha q| (as ordered float bits; NaN orders above every number, so a
 // NaN quantity shows as a non-finite bound).
-template <typename TQ>
+template <typename TQ, int CP>
 __global__ void k_scatter_qprep(const TQ *__restrict__ q, const uint32_t *__restrict__ perm, int64_t m,
-                                int ncomp, int cp, float alpha, float *__restrict__ qs,
-                                unsigned *__restrict__ qmax_bits) {
+                                int ncomp, float alpha, float *__restrict__ qs, unsigned *__restrict__ qmax_bits) {
   unsigned mx = 0u;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m;
-       s += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t p = perm[s];
-    // four components at a time into one 16-byte store (cp is 4 or 12)
-    for (int c4 = 0; c4 < cp; c4 += 4) {
-      float v[4];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // two points a trip, every load of both issued before the stores (the loads of one point
+  // are independent, so a trip waits for memory once, not once per component group)
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += 2 * stride) {
+    const bool two = s + stride < m;
+    const int64_t p0 = perm[s], p1 = perm[two ? s + stride : s];
+    float v[2][CP];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        v[u] = c4 + u < ncomp ? alpha * (float)q[p + m * (c4 + u)] : 0.0f;
-        const unsigned bits = __float_as_uint(fabsf(v[u]));
-        mx = bits > mx ? bits : mx;
+    for (int c = 0; c < CP; ++c) {
+      v[0][c] = c < ncomp ? alpha * (float)q[p0 + m * c] : 0.0f;
+      v[1][c] = c < ncomp ? alpha * (float)q[p1 + m * c] : 0.0f;
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (k == 1 && !two) break;
+      // four components at a time into one 16-byte store
+#pragma unroll
+      for (int c4 = 0; c4 < CP; c4 += 4) {
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const unsigned bits = __float_as_uint(fabsf(v[k][c4 + u]));
+          mx = bits > mx ? bits : mx;
+        }
+        reinterpret_cast<float4 *>(qs + (s + k * stride) * CP)[c4 / 4] =
+            make_float4(v[k][c4], v[k][c4 + 1], v[k][c4 + 2], v[k][c4 + 3]);
       }
-      reinterpret_cast<float4 *>(qs + s * cp)[c4 / 4] = make_float4(v[0], v[1], v[2], v[3]);
     }
   }
 #pragma unroll
@@ -2978,12 +3000,15 @@ gbg_status gbg_anterpolate_binned(gbg_field f, gbg_bins b, const gbg_scheme *sch
   GBG_CUDA_TRY(cudaMemsetAsync(b->qmax_bits, 0, sizeof(unsigned), st));
   if (m > 0) {
     const int blocks = launch_blocks(m, kThreads);
-    if (q_dtype == GBG_F64)
-      k_scatter_qprep<double><<<blocks, kThreads, 0, st>>>(static_cast<const double *>(q), b->perm, m, f->ncomp, f->cp,
-                                                           (float)alpha, b->qs, b->qmax_bits);
-    else
-      k_scatter_qprep<float><<<blocks, kThreads, 0, st>>>(static_cast<const float *>(q), b->perm, m, f->ncomp, f->cp,
-                                                          (float)alpha, b->qs, b->qmax_bits);
+    if (q_dtype == GBG_F64) {
+      const double *qd = static_cast<const double *>(q);
+      if (f->cp == 4) k_scatter_qprep<double, 4><<<blocks, kThreads, 0, st>>>(qd, b->perm, m, f->ncomp, (float)alpha, b->qs, b->qmax_bits);
+      else k_scatter_qprep<double, 12><<<blocks, kThreads, 0, st>>>(qd, b->perm, m, f->ncomp, (float)alpha, b->qs, b->qmax_bits);
+    } else {
+      const float *qf = static_cast<const float *>(q);
+      if (f->cp == 4) k_scatter_qprep<float, 4><<<blocks, kThreads, 0, st>>>(qf, b->perm, m, f->ncomp, (float)alpha, b->qs, b->qmax_bits);
+      else k_scatter_qprep<float, 12><<<blocks, kThreads, 0, st>>>(qf, b->perm, m, f->ncomp, (float)alpha, b->qs, b->qmax_bits);
+    }
     note_launch();
     GBG_CUDA_TRY(cudaGetLastError());
   }

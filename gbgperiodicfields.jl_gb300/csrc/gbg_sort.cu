@@ -215,8 +215,22 @@ int sm_count_cached() {
 // exclusive scan of the counts: the slot starts[key] + rank is free for it.
 __global__ void k_place_unstable(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ rank,
                                  const uint32_t *__restrict__ starts, int64_t n, uint32_t *__restrict__ perm_u) {
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (int64_t)gridDim.x * blockDim.x)
-    perm_u[__ldg(starts + __ldg(keys + p)) + __ldg(rank + p)] = (uint32_t)p;
+  // four points a trip: keys and ranks, then the keys' starts, then the stores
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += 4 * stride) {
+    uint32_t k[4], r[4], a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const bool in = p + u * stride < n;
+      k[u] = in ? __ldg(keys + p + u * stride) : 0u;
+      r[u] = in ? __ldg(rank + p + u * stride) : 0u;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = p + u * stride < n ? __ldg(starts + k[u]) : 0u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (p + u * stride < n) perm_u[a[u] + r[u]] = (uint32_t)(p + u * stride);
+  }
 }
 
 // Makes the placement stable: the point in slot s moves to the position, within its key's
@@ -227,21 +241,36 @@ constexpr uint32_t kPlaceMaxRun = 1024;
 __global__ void k_place_stable(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ starts,
                                const uint32_t *__restrict__ perm_u, int64_t n, uint32_t *__restrict__ perm,
                                uint32_t *big) {
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t p = __ldg(perm_u + s);
-    const uint32_t k = __ldg(keys + p);
-    const uint32_t a = __ldg(starts + k), c = __ldg(starts + k + 1) - a;
-    if (c == 1u) {
-      perm[s] = p;
-      continue;
+  // two slots a trip, each level of their loads issued together
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s0 < n; s0 += 2 * stride) {
+    uint32_t pv[2], kv[2], av[2], cv[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) pv[u] = s0 + u * stride < n ? __ldg(perm_u + s0 + u * stride) : 0u;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) kv[u] = s0 + u * stride < n ? __ldg(keys + pv[u]) : 0u;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      av[u] = s0 + u * stride < n ? __ldg(starts + kv[u]) : 0u;
+      cv[u] = s0 + u * stride < n ? __ldg(starts + kv[u] + 1) - av[u] : 0u;
     }
-    if (c > kPlaceMaxRun) {
-      atomicOr(big, 1u);
-      continue;
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      const int64_t s = s0 + u * stride;
+      if (s >= n) continue;
+      const uint32_t p = pv[u], a = av[u], c = cv[u];
+      if (c == 1u) {
+        perm[s] = p;
+        continue;
+      }
+      if (c > kPlaceMaxRun) {
+        atomicOr(big, 1u);
+        continue;
+      }
+      uint32_t r = 0;
+      for (uint32_t t = 0; t < c; ++t) r += __ldg(perm_u + a + t) < p ? 1u : 0u;
+      perm[a + r] = p;
     }
-    uint32_t r = 0;
-    for (uint32_t t = 0; t < c; ++t) r += __ldg(perm_u + a + t) < p ? 1u : 0u;
-    perm[a + r] = p;
   }
 }
 
