@@ -344,8 +344,7 @@ __device__ __forceinline__ bool split64(double x, double scale, double shift, in
   const long long v = floor_bits(u, ok);
   // |u| < 2^63, so the cell word fits 32 bits, and so does n: the periodic wrap in 32-bit
   // arithmetic (a 64-bit remainder costs several times more)
-  const int32_t c = (int32_t)(v >> 32);
-  const int32_t r = (uint32_t)c < (uint32_t)n ? c : c % (int32_t)n;  // no division inside the box
+  int32_t r = (int32_t)(v >> 32) % (int32_t)n;
   cell = r < 0 ? r + n : r;
   t = ok ? __uint2float_rz((unsigned)(v & 0xffffffffLL)) * 0x1p-32f : __int_as_float(0x7fc00000);
   return ok;
