@@ -722,7 +722,9 @@ __device__ __forceinline__ void gather4_point(const SchemeT<float, 4> &s, const 
 }
 
 // Gather: width-4 stencils, a point per quarter-warp, 512 threads (64 quarter-warps) per
-// CTA; each quarter-warp loads its next point's record and index while it computes.
+// CTA; each quarter-warp loads its next point's record and index while it computes.  With
+// two tile buffers the warps run free of CTA barriers (the warp that releases a buffer last
+// refills it); with one (a large tile, two CTAs per SM) the CTA waits at each brick.
 constexpr int kGatherThreads = 512;
 template <int M2, int CP, typename TO>
 __global__ void __launch_bounds__(kGatherThreads, 1)
@@ -769,6 +771,113 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
   // the bricks to visit: the bins' list of bricks holding points, or every brick
   const int64_t nunits = list ? (int64_t)__ldg(list_n) : g.nbricks;
   auto unit = [&](int64_t i) -> int64_t { return i >= nunits ? -1 : (list ? (int64_t)__ldg(list + i) : i); };
+  if (nbuf == 2) {
+    // Two tile buffers and no CTA barrier between bricks: every warp waits for each
+    // non-empty brick's tile in turn (so it follows every phase of both mbarriers), takes its
+    // quarter-warps' points, and releases the buffer through a shared counter; the warp that
+    // releases it last issues the copy of the brick after next into it.  Warps drift across
+    // brick boundaries instead of waiting for the slowest one at each.
+    __shared__ uint32_t s_rel[2], s_nissue[2], s_fail;
+    const uint32_t nwarps = blockDim.x >> 5;
+    // the CTA's first non-empty unit at or after i (units i, i + gridDim.x, ...), or nunits
+    auto next_unit = [&](int64_t i, uint32_t &a, uint32_t &z) -> int64_t {
+      for (; i < nunits; i += gridDim.x) {
+        const int64_t b = unit(i);
+        a = __ldg(cell_start + b * g.bvol);
+        z = __ldg(cell_start + (b + 1) * g.bvol);
+        if (z > a) return i;
+      }
+      a = z = 0u;
+      return nunits;
+    };
+    uint32_t a0 = 0, z0 = 0, a1 = 0, z1 = 0;
+    int64_t cur = next_unit(blockIdx.x, a0, z0);
+    int64_t nx = cur < nunits ? next_unit(cur + gridDim.x, a1, z1) : nunits;
+    if (threadIdx.x == 0) {
+      s_rel[0] = s_rel[1] = 0u;
+      s_nissue[0] = s_nissue[1] = 0u;
+      s_fail = 0u;
+      if (cur < nunits) {
+        issue(unit(cur), 0);
+        s_nissue[0] = 1u;
+      }
+      if (nx < nunits) {
+        issue(unit(nx), 1);
+        s_nissue[1] = 1u;
+      }
+    }
+    __syncthreads();
+    float4 r_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    uint32_t p_next = 0u;
+    if (a0 + qw < z0) {
+      r_next = __ldg(rec + a0 + qw);
+      p_next = __ldg(perm + a0 + qw);
+    }
+    uint32_t ph[2] = {0u, 0u};
+    for (int j = 0; cur < nunits; ++j) {
+      const int buf = j & 1;
+      uint32_t a2 = 0, z2 = 0;
+      const int64_t nx2 = nx < nunits ? next_unit(nx + gridDim.x, a2, z2) : nunits;
+      // a warp that gave up stops the others at their next brick; the outcome of the bounded
+      // wait is voted so the warp takes one exit
+      bool stop = *(volatile uint32_t *)&s_fail != 0u;
+      if (!stop) stop = !mbar_wait(bars + buf, ph[buf], g.wait_polls);
+      if (__any_sync(0xffffffffu, stop)) {
+        if (lane == 0) {
+          s_fail = 1u;
+          if (status) atomicOr(status, GBG_DEV_TIMEOUT);
+        }
+        break;
+      }
+      ph[buf] ^= 1u;
+      bool ahead = false;  // this quarter-warp's first record of the next brick is loading
+      for (uint32_t sl = a0 + qw; sl < z0; sl += nqw) {
+        const float4 r = r_next;
+        const int64_t p = p_next;
+        if (sl + nqw < z0) {
+          r_next = __ldg(rec + sl + nqw);
+          p_next = __ldg(perm + sl + nqw);
+        } else if (a1 + qw < z1) {
+          r_next = __ldg(rec + a1 + qw);
+          p_next = __ldg(perm + a1 + qw);
+          ahead = true;
+        }
+        gather4_point<M2, CP>(s, cx, cya, cyb, qi, jj, sub, seg_mask, r, p,
+                              reinterpret_cast<const float *>(smem + buf * tile_bytes), g.w[0], g.w[0] * g.w[1], 0,
+                              out, g.m, g.ncomp);
+      }
+      if (!ahead && a1 + qw < z1) {
+        r_next = __ldg(rec + a1 + qw);
+        p_next = __ldg(perm + a1 + qw);
+      }
+      __syncwarp();
+      if (lane == 0) {
+        __threadfence_block();
+        if (atomicAdd(&s_rel[buf], 1u) == nwarps - 1u) {
+          // every warp is done with this buffer: refill it (reads of the generic proxy are
+          // ordered before the copy's writes)
+          atomicExch(&s_rel[buf], 0u);
+          if (nx2 < nunits) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(unit(nx2), buf);
+            s_nissue[buf] += 1u;
+          }
+        }
+      }
+      cur = nx;
+      a0 = a1;
+      z0 = z1;
+      nx = nx2;
+      a1 = a2;
+      z1 = z2;
+    }
+    __syncthreads();
+    // every copy issued lands before the CTA's shared memory is released (full limit)
+    if (threadIdx.x == 0)
+      for (int i = 0; i < 2; ++i)
+        if (s_nissue[i]) mbar_wait(bars + i, (s_nissue[i] - 1u) & 1u);
+    return;
+  }
   int64_t ui = blockIdx.x;
   // a brick's point range and each quarter-warp's first record are loaded one brick ahead
   uint32_t s0 = 0, s1 = 0;
