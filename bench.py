@@ -992,9 +992,10 @@ def run_reference(args, rank, world):
 
 # ------------------------------------------------------- profiling cases
 
-def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), threads=256):
+def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), gather_threads=512, scatter_threads=256):
     """256^3 x 12 FP32 resident field (0.85 GB), 4e6 uniform points in binned order,
-    bins + cubic gather and scatter, twice, at 15x8x8 bricks and 256 threads."""
+    bins + cubic gather and scatter, twice, at 15x8x8 bricks, 512 gather and 256 scatter
+    threads (the tuned launch shape)."""
     import torch
     from __graft_entry__ import load_package
     gbg = load_package()
@@ -1008,7 +1009,7 @@ def case_resident(n=256, C=12, M=4_000_000, brick=(15, 8, 8), threads=256):
     bins = resident.PointBins(grid, M, brick=brick).build(pos)
     pos = gbg.colmajor(pos[bins.order().long() - 1])
     bins.build(pos)
-    bins.set_launch(threads, threads)
+    bins.set_launch(gather_threads, scatter_threads)
     out = gbg.empty_colmajor((M, C), torch.float32, dev)
     q = gbg.colmajor(torch.randn((M, C), dtype=torch.float32, device=dev))
     for _ in range(2):
