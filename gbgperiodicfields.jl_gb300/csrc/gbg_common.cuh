@@ -262,10 +262,12 @@ gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, ui
 // starts[k] points per key).  perm[s] = the point in slot s, points of one key in index
 // order -- the order the stable radix sort gives.  *big must be zero on entry; a key with
 // more than 1024 points sets it and the radix sort (gated on it) redoes the order, writing
-// skeys too.  temp holds radix_sort_temp_bytes(n) bytes.
+// skeys too.  temp holds radix_sort_temp_bytes(n) bytes.  With rec_user and rec given, the
+// placement also writes rec[s] = rec_user[perm[s]] (when *big is left zero; the fallback's
+// order is then the caller's to gather).
 gbg_status stable_counting_sort(const uint32_t *keys, const uint32_t *rank, const uint32_t *starts, int64_t n,
                                 int key_bits, uint32_t *perm, uint32_t *skeys, uint32_t *big, void *temp,
-                                cudaStream_t stream);
+                                cudaStream_t stream, const float4 *rec_user = nullptr, float4 *rec = nullptr);
 
 // Grid-stride launch shape: a multiple of the SM count.
 int launch_blocks(int64_t work, int threads, int per_sm = 8);

@@ -495,7 +495,8 @@ __global__ void k_brick_lists(const uint32_t *__restrict__ cell_start, int64_t n
 }
 
 __global__ void k_gather_records(const float4 *__restrict__ rec_user, const uint32_t *__restrict__ perm,
-                                 int64_t m, float4 *__restrict__ rec) {
+                                 int64_t m, float4 *__restrict__ rec, const uint32_t *gate = nullptr) {
+  if (gate && __ldg(gate) == 0u) return;  // the stable placement wrote the records
   // four slots a trip: their indices, then their records, then the stores
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += 4 * stride) {
@@ -2933,8 +2934,10 @@ gbg_status bins_build_impl(gbg_bins_s *b, const T *positions, int64_t npoints, i
   // stable order; a cell of more than 1024 points sends the whole sort to the radix sort)
   GBG_TRY(exclusive_scan_u32(b->cell_start, b->cell_start, b->nkeys + 1, b->scan_tmp, st));
   GBG_TRY(stable_counting_sort(b->keys, b->skeys, b->cell_start, npoints, bits, b->perm, b->skeys, b->lists_n + 2,
-                               b->sort_tmp, st));
-  k_gather_records<<<blocks, kThreads, 0, st>>>(b->rec_user, b->perm, npoints, b->rec);
+                               b->sort_tmp, st, b->rec_user, b->rec));
+  // the records in sorted order come with the stable placement; only the radix fallback's
+  // order (a cell of more than 1024 points) gathers them again
+  k_gather_records<<<blocks, kThreads, 0, st>>>(b->rec_user, b->perm, npoints, b->rec, b->lists_n + 2);
   note_launch();
   k_brick_lists<<<launch_blocks(b->nbricks, kThreads), kThreads, 0, st>>>(
       b->cell_start, b->nb[0], b->nb[1], b->nb[2], b->bvol, b->reach_ok ? 1 : 0, b->active, b->reach, b->lists_n);

@@ -240,15 +240,19 @@ __global__ void k_place_unstable(const uint32_t *__restrict__ keys, const uint32
 constexpr uint32_t kPlaceMaxRun = 1024;
 __global__ void k_place_stable(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ starts,
                                const uint32_t *__restrict__ perm_u, int64_t n, uint32_t *__restrict__ perm,
-                               uint32_t *big) {
+                               uint32_t *big, const float4 *__restrict__ rec_user, float4 *__restrict__ rec) {
   // two slots a trip, each level of their loads issued together
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s0 < n; s0 += 2 * stride) {
     uint32_t pv[2], kv[2], av[2], cv[2];
+    float4 rv[2] = {make_float4(0.f, 0.f, 0.f, 0.f), make_float4(0.f, 0.f, 0.f, 0.f)};
 #pragma unroll
     for (int u = 0; u < 2; ++u) pv[u] = s0 + u * stride < n ? __ldg(perm_u + s0 + u * stride) : 0u;
 #pragma unroll
-    for (int u = 0; u < 2; ++u) kv[u] = s0 + u * stride < n ? __ldg(keys + pv[u]) : 0u;
+    for (int u = 0; u < 2; ++u) {
+      kv[u] = s0 + u * stride < n ? __ldg(keys + pv[u]) : 0u;
+      if (rec && s0 + u * stride < n) rv[u] = __ldg(rec_user + pv[u]);
+    }
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       av[u] = s0 + u * stride < n ? __ldg(starts + kv[u]) : 0u;
@@ -261,6 +265,7 @@ __global__ void k_place_stable(const uint32_t *__restrict__ keys, const uint32_t
       const uint32_t p = pv[u], a = av[u], c = cv[u];
       if (c == 1u) {
         perm[s] = p;
+        if (rec) rec[s] = rv[u];
         continue;
       }
       if (c > kPlaceMaxRun) {
@@ -270,6 +275,7 @@ __global__ void k_place_stable(const uint32_t *__restrict__ keys, const uint32_t
       uint32_t r = 0;
       for (uint32_t t = 0; t < c; ++t) r += __ldg(perm_u + a + t) < p ? 1u : 0u;
       perm[a + r] = p;
+      if (rec) rec[a + r] = rv[u];
     }
   }
 }
@@ -361,7 +367,7 @@ gbg_status radix_sort_pairs(const uint32_t *keys_in, const uint32_t *vals_in, ui
 
 gbg_status stable_counting_sort(const uint32_t *keys, const uint32_t *rank, const uint32_t *starts, int64_t n,
                                 int key_bits, uint32_t *perm, uint32_t *skeys, uint32_t *big, void *temp,
-                                cudaStream_t stream) {
+                                cudaStream_t stream, const float4 *rec_user, float4 *rec) {
   if (n <= 0) return GBG_OK;
   if (n > 0x7fffffffLL) return set_error(GBG_EUNSUPPORTED, "counting sort: more than 2^31-1 points");
   // the unstable placement lives at the start of the radix sort's scratch, which only the
@@ -370,7 +376,7 @@ gbg_status stable_counting_sort(const uint32_t *keys, const uint32_t *rank, cons
   const int blocks = launch_blocks(n, 256);
   k_place_unstable<<<blocks, 256, 0, stream>>>(keys, rank, starts, n, perm_u);
   note_launch();
-  k_place_stable<<<blocks, 256, 0, stream>>>(keys, starts, perm_u, n, perm, big);
+  k_place_stable<<<blocks, 256, 0, stream>>>(keys, starts, perm_u, n, perm, big, rec_user, rec);
   note_launch();
   GBG_CUDA_TRY(cudaGetLastError());
   return radix_sort_pairs(keys, nullptr, skeys, perm, n, key_bits, temp, stream, big);

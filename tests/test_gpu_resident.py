@@ -137,6 +137,9 @@ def test_bins_order_with_a_crowded_cell(gbg, oracle, dev):
     loc = c - br * b
     key = ((br[:, 2] * nb[1] + br[:, 1]) * nb[0] + br[:, 0]) * b.prod() + (loc[:, 2] * b[1] + loc[:, 1]) * b[0] + loc[:, 0]
     assert np.array_equal(order, np.argsort(key, kind="stable") + 1)
+    # the points' records follow that order too (the fallback gathers them again)
+    got = resident.interpolate_binned(field, bins, gbg.CatmullRom, dtype=torch.float64).cpu().numpy()
+    assert relerr(got, oracle.gather(g, f, crowd, gbg.CatmullRom.coefficients)) <= 1e-5
 
 
 def test_nonfinite_quantity_is_reported(gbg, oracle, dev):
