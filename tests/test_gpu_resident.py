@@ -334,3 +334,35 @@ def test_host_read_and_import_equal_the_device_path(gbg, dev):
     assert torch.equal(h.read(dtype=torch.float32), data)
     with pytest.raises(gbg.ArgumentError):
         resident.PointBins(grid, 10).build(torch.zeros((10, 3), dtype=torch.float64))
+
+
+def test_bins_split_at_extreme_positions(gbg, oracle, dev):
+    """The FP64 fixed-point split far from the box: u = x * n/L * 2^32 (one rounding, origin 0),
+    floor(u) split into cell and fraction.  Positions up to 5.7e8 (u near 6e18, close to the
+    9.2e18 limit) bin like the host's exact keys and gather like the same points in the box;
+    positions past the limit are reported as non-finite."""
+    from gbgperiodicfields_gb300 import resident
+    n = 16
+    grid = gbg.Grid3D((n, n, n), (TWO_PI,) * 3)
+    rng = np.random.default_rng(77)
+    pos = TWO_PI * rng.random((600, 3))
+    field = resident.ResidentField(grid, 3, max_stencil_width=4).load(
+        torch.from_numpy(np.asfortranarray(rng.standard_normal((n, n, n, 3)))).cuda())
+    inside = resident.PointBins(grid, 600, brick=(8, 8, 8)).build(torch.from_numpy(np.asfortranarray(pos)).cuda())
+    want = resident.interpolate_binned(field, inside, gbg.CatmullRom).cpu().numpy()
+    for shift in ([1e7, -3e7, 9e7], [-9e7, 5e6, -1e3]):
+        far = np.asfortranarray(pos + TWO_PI * np.array(shift))
+        bins = resident.PointBins(grid, 600, brick=(8, 8, 8)).build(torch.from_numpy(far).cuda())
+        # host keys: the same single-rounding product and floor, then the periodic cell
+        u = far * (n / TWO_PI * 4294967296.0)
+        c = np.mod(np.floor(u).astype(np.int64) >> 32, n)
+        br, loc = c // 8, c % 8
+        key = ((br[:, 2] * 2 + br[:, 1]) * 2 + br[:, 0]) * 512 + (loc[:, 2] * 8 + loc[:, 1]) * 8 + loc[:, 0]
+        assert np.array_equal(bins.order().cpu().numpy(), np.argsort(key, kind="stable") + 1)
+        got = resident.interpolate_binned(field, bins, gbg.CatmullRom).cpu().numpy()
+        assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    beyond = torch.tensor([[1.0, 2.0, 3.0], [9e8, 0.5, 0.5], [0.5, -9e8, 0.5]], dtype=torch.float64, device=dev)
+    resident.PointBins(grid, 3, brick=(8, 8, 8)).build(beyond, status)
+    torch.cuda.synchronize()
+    assert int(status.item()) & gbg._lib.GBG_DEV_NONFINITE
