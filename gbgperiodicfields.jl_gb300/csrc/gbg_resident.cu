@@ -879,6 +879,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
         if (s_nissue[i]) mbar_wait(bars + i, (s_nissue[i] - 1u) & 1u);
     return;
   }
+  // One buffer: the CTA waits at each brick, and thread 0 refills the buffer after the barrier.
   int64_t ui = blockIdx.x;
   // a brick's point range and each quarter-warp's first record are loaded one brick ahead
   uint32_t s0 = 0, s1 = 0;
@@ -893,15 +894,14 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
       p_next = __ldg(perm + s0 + qw);
     }
   }
-  for (int it = 0; ui < nunits; ++it, ui += gridDim.x) {
-    const int buf = nbuf == 2 ? (it & 1) : 0;
+  for (; ui < nunits; ui += gridDim.x) {
+    constexpr int buf = 0;
     const int64_t bn = unit(ui + gridDim.x);
     uint32_t n0 = 0, n1 = 0;
     if (bn >= 0) {
       n0 = __ldg(cell_start + bn * g.bvol);
       n1 = __ldg(cell_start + (bn + 1) * g.bvol);
     }
-    if (nbuf == 2 && threadIdx.x == 0 && n1 > n0) issue(bn, buf ^ 1);
     bool ahead = false;  // this quarter-warp's first record of the next brick is loading
     if (s1 > s0) {
       // every thread must take the same exit, so the outcome of the bounded wait is voted
@@ -933,7 +933,7 @@ __global__ void __launch_bounds__(kGatherThreads, 1)
       p_next = __ldg(perm + n0 + qw);
     }
     __syncthreads();  // every lane is done with this buffer before it is refilled
-    if (nbuf == 1 && threadIdx.x == 0 && n1 > n0) issue(bn, 0);
+    if (threadIdx.x == 0 && n1 > n0) issue(bn, 0);
     s0 = n0;
     s1 = n1;
   }
