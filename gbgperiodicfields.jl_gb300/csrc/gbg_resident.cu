@@ -1236,8 +1236,10 @@ __device__ __forceinline__ void weights_rt(const float *c, int m2, float t, floa
 // Shared memory of one scatter CTA, in this order: the brick's running sums (CP floats per
 // node), one chunk of the region's points (CP quantities and 3*N2+4 weights each), the
 // region's per-cell point offsets (+ the total) and first slots, the per-axis key tables
-// of the region's cells, and the points' region x cells.  (With compensation, a region of
-// several chunks keeps its sums' corrections in the CTA's own slot of a global scratch.)
+// of the region's cells (this brick's, then the next brick's), and the points' region x
+// cells.  (With compensation, a region of several chunks keeps its sums' corrections in the
+// CTA's own slot of a global scratch; the next brick's cell table, copied ahead, uses the
+// free end of the staging area.)
 size_t scatter_nodes_fixed(const FixGeo &g, int cp) {
   const size_t ecount = (size_t)g.e[0] * g.e[1] * g.e[2];
   return sizeof(float) * (size_t)g.bvol * cp +
