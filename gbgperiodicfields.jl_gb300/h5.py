@@ -13,14 +13,16 @@ package, so the format is implemented here.  What is covered:
   attributes in object headers or densely, contiguous and compact datasets (chunked
   ones with the version 1 B-tree chunk index, unfiltered or deflate-compressed), the
   fixed-point, floating-point, string, compound (a pair r/i of floats reads as
-  complex), enum, and variable-length string types; every checksum is verified
-  (the chunked reader is checked by no file in the tests: HDF5.jl, MATLAB and this
-  writer store contiguous datasets by default, and no chunked file written by libhdf5
-  is at hand);
+  complex), enum, and variable-length string types; every checksum is verified;
 * writing: superblock version 2, version 2 object headers, compact links and
-  attributes, contiguous datasets, the same datatypes as the reader (strings as
-  fixed-length UTF-8, complex as the compound {r, i} HDF5.jl uses); the result is a
-  file libhdf5 1.8 or later opens.
+  attributes, contiguous datasets, and chunked ones on request (a version 1 B-tree of
+  chunk records, up to 64 a node, each chunk optionally deflated), the same datatypes
+  as the reader (strings as fixed-length UTF-8, complex as the compound {r, i} HDF5.jl
+  uses), to the version of the specification libhdf5 1.8 and later read.  No libhdf5
+  is at hand to open the results, so writing is checked against this module's reader,
+  which is itself pinned to files libhdf5 wrote (contiguous ones: HDF5.jl, MATLAB and
+  the default here store datasets contiguously, and no chunked file written by libhdf5
+  is at hand, so the chunked layout is checked by round trips alone).
 
 Arrays follow Julia's (and HDF5.jl's) convention: an array of shape S, column-major,
 is stored as the dataspace reversed(S) over the same bytes, so a file written here
@@ -369,6 +371,10 @@ class Dataset(Node):
         self._value = value      # a scalar or string value, kept as given
         self._stored = stored    # (reader, Datatype, HDF5 dims, layout) in the file read
         self._written = written  # (address, byte count, numpy dtype, HDF5 dims) in the output
+        # a chunked dataset written here: {"chunk": HDF5-order chunk dims, "level": deflate
+        # level or None, "entries": [(HDF5 offsets, address, bytes), ...]}; the address in
+        # _written is then its chunk B-tree's
+        self._chunked = None
 
     @property
     def ndim(self):
@@ -377,6 +383,18 @@ class Dataset(Node):
     def read(self):
         if self._value is not None:
             return self._value
+        if self._written is not None and self._chunked is not None:
+            _, _, dt, dims = self._written
+            c = self._chunked
+            full = np.zeros(tuple(dims), dtype=dt)
+            for offs, caddr, n in c["entries"]:
+                raw = self._file._read_output(caddr, n)
+                if c["level"] is not None:
+                    raw = zlib.decompress(raw)
+                block = np.frombuffer(raw, dtype=dt).reshape(c["chunk"])
+                sl = tuple(slice(o, min(o + k, d)) for o, k, d in zip(offs, c["chunk"], dims))
+                full[sl] = block[tuple(slice(0, q.stop - q.start) for q in sl)]
+            return np.asfortranarray(full.T)
         if self._written is not None:
             addr, nbytes, dt, dims = self._written
             raw = self._file._read_output(addr, nbytes)
@@ -463,13 +481,32 @@ class Group(Node):
     def require_group(self, path) -> "Group":
         return self[path] if path in self else self.create_group(path)
 
-    def create_dataset(self, path, value) -> Dataset:
+    def create_dataset(self, path, value, chunks=None, compression=None) -> Dataset:
+        """A dataset holding value.  A numeric array may be stored in chunks (`chunks`, one
+        extent per axis in the array's own, Julia, order; edge chunks are stored whole) and
+        each chunk deflate-compressed (`compression`, a zlib level 0-9, chunked only);
+        otherwise the data is one contiguous block."""
         self._file._writable()
         parent, leaf = self._parent_and_leaf(path)
         if leaf in parent._links:
             raise H5Error(f"an object named {path!r} already exists")
         dt, dims, raw = _from_value(value)
-        if raw is not None:
+        if compression is not None and chunks is None:
+            raise H5Error("compression needs a chunked layout (chunks=...)")
+        if chunks is not None:
+            a = np.asarray(value)
+            chunks = tuple(int(c) for c in chunks)
+            if raw is not None or dt.kind not in "biufc" or a.ndim == 0 or a.size == 0:
+                raise H5Error("chunks: only non-empty numeric arrays are stored in chunks")
+            if len(chunks) != a.ndim or any(c < 1 for c in chunks):
+                raise H5Error(f"chunks: {len(chunks)} extents >= 1 expected for an array of {a.ndim} axes")
+            if compression is not None and not 0 <= int(compression) <= 9:
+                raise H5Error("compression: a deflate level 0-9")
+            level = None if compression is None else int(compression)
+            btree, nbytes, entries, cdims = self._file._append_chunked(a, dt, chunks, level)
+            ds = Dataset(self._file, leaf, dt, tuple(a.shape), written=(btree, nbytes, dt, dims))
+            ds._chunked = {"chunk": cdims, "level": level, "entries": entries}
+        elif raw is not None:
             ds = Dataset(self._file, leaf, dt, (), value=value)
         else:
             a = np.asarray(value)
@@ -1109,7 +1146,15 @@ class _Writer:
             msgs += _message(0x01, _encode_dataspace(dims))
             msgs += _message(0x03, _encode_datatype(dt), flags=0x01)
             msgs += _message(0x05, struct.pack("<BB", 3, 0x09), flags=0x01)
-            msgs += _message(0x08, struct.pack("<BBQQ", 3, 1, addr if nbytes else UNDEF, nbytes))
+            c = getattr(node, "_chunked", None)
+            if c is not None:
+                if c["level"] is not None:
+                    # filter pipeline, version 2: deflate (id 1), one client value: the level
+                    msgs += _message(0x0B, struct.pack("<BBHHHI", 2, 1, 1, 0, 1, c["level"]), flags=0x01)
+                cd = tuple(c["chunk"]) + (np.dtype(dt).itemsize,)
+                msgs += _message(0x08, struct.pack(f"<BBBQ{len(cd)}I", 3, 2, len(cd), addr, *cd))
+            else:
+                msgs += _message(0x08, struct.pack("<BBQQ", 3, 1, addr if nbytes else UNDEF, nbytes))
         for aname, value in node.attrs.items():
             msgs += _message(0x0C, _attribute_message(aname, value))
         return msgs
@@ -1200,6 +1245,67 @@ class File(Group):
         self._writable()
         buf = _array_bytes(a, dt)
         return self._append_raw(buf)
+
+    def _append_chunked(self, a: np.ndarray, dt: np.dtype, chunks, level):
+        """Writes the array's chunks (deflated when level is given) and a version 1 B-tree
+        of type 1 indexing them; returns (B-tree address, data bytes, chunk entries,
+        HDF5-order chunk dims)."""
+        self._writable()
+        import itertools
+        hdf = np.ascontiguousarray(np.asfortranarray(a.astype(dt, copy=False)).T)  # HDF5 (C) order
+        cdims = tuple(reversed(chunks))
+        entries, total = [], 0
+        for offs in itertools.product(*[range(0, n, c) for n, c in zip(hdf.shape, cdims)]):
+            sl = tuple(slice(o, min(o + c, n)) for o, c, n in zip(offs, cdims, hdf.shape))
+            block = np.zeros(cdims, dtype=hdf.dtype)
+            block[tuple(slice(0, q.stop - q.start) for q in sl)] = hdf[sl]
+            raw = block.tobytes()
+            if level is not None:
+                raw = zlib.compress(raw, level)
+            addr, n = self._append_raw(raw)
+            entries.append((offs, addr, n))
+            total += n
+        return self._append_chunk_btree(entries, cdims), total, entries, cdims
+
+    def _append_chunk_btree(self, entries, cdims):
+        """A version 1 B-tree of chunk records: leaves of up to 64 chunks (2K, K = 32 being
+        the format's default), internal levels of up to 64 children, siblings linked, each
+        node written at its full size; returns the root's address."""
+        nd = len(cdims)
+        fan = 64
+        ksize = 8 + 8 * (nd + 1)
+        node_size = 24 + fan * (ksize + 8) + ksize
+
+        def key(offs, size=0):
+            return struct.pack("<II", size, 0) + struct.pack(f"<{nd + 1}Q", *offs, 0)
+
+        # (first offsets, end offsets, [(key bytes, child address)], level) per node
+        level = 0
+        nodes = [(grp[0][0], tuple(o + c for o, c in zip(grp[-1][0], cdims)),
+                  [(key(offs, n), addr) for offs, addr, n in grp], 0)
+                 for grp in (entries[i:i + fan] for i in range(0, len(entries), fan))]
+        while True:
+            first = self._append_raw(b"")[0]
+            addrs = [first + i * node_size for i in range(len(nodes))]
+            for i, (_, end, kids, lev) in enumerate(nodes):
+                left = addrs[i - 1] if i > 0 else UNDEF
+                right = addrs[i + 1] if i + 1 < len(nodes) else UNDEF
+                body = b"".join(k + struct.pack("<Q", c) for k, c in kids) + key(end)
+                head = b"TREE" + struct.pack("<BBHQQ", 1, lev, len(kids), left, right)
+                out = self._out
+                out.seek(0, os.SEEK_END)
+                assert out.tell() == addrs[i]
+                out.write(head + body + bytes(node_size - len(head) - len(body)))
+            if len(nodes) == 1:
+                return addrs[0]
+            # the next level: a node per run of up to 64 children, keyed by each child's
+            # first chunk, ending at its last child's end
+            level += 1
+            parents = []
+            for j in range(0, len(nodes), fan):
+                run = list(zip(nodes[j:j + fan], addrs[j:j + fan]))
+                parents.append((run[0][0][0], run[-1][0][1], [(key(child[0]), caddr) for child, caddr in run], level))
+            nodes = parents
 
     def _copy_stored(self, ds: Dataset):
         """Copies a dataset of the file that was read into the output; returns its

@@ -167,6 +167,55 @@ def test_dataset_data_is_captured_when_written(mods, tmp_path):
         np.testing.assert_array_equal(f["a"].read(), 0)
 
 
+@pytest.mark.parametrize("level", [None, 0, 6])
+def test_chunked_datasets_round_trip(mods, tmp_path, level):
+    """Chunked datasets (edge chunks stored whole; deflated when a level is given) read back
+    exactly through the reader's chunk B-tree walk: before close from the chunk list, after
+    close from the file, and after a rewrite in append mode (which stores them whole).  300
+    chunks need a second B-tree level (64 chunks a leaf)."""
+    _, h5, _ = mods
+    rng = np.random.default_rng(5)
+    cases = {"f64": (rng.standard_normal((13, 7, 5)), (4, 3, 2)),
+             "i32": (rng.integers(-9, 9, (40, 30, 3)).astype(np.int32), (2, 2, 3)),
+             "c128": (rng.standard_normal((9, 4)) + 1j * rng.standard_normal((9, 4)), (5, 4)),
+             "f32": (rng.standard_normal(100).astype(np.float32), (7,))}
+    p = tmp_path / "chunked.h5"
+    with h5.File(p, "w") as f:
+        for name, (a, ch) in cases.items():
+            ds = f.create_dataset(name, np.asfortranarray(a), chunks=ch, compression=level)
+            np.testing.assert_array_equal(ds.read(), a)
+    with h5.File(p) as f:
+        for name, (a, ch) in cases.items():
+            layout = f[name]._stored[3]
+            assert layout["class"] == "chunked" and layout["filters"] == ([] if level is None else [1])
+            assert tuple(layout["chunk"]) == tuple(reversed(ch))
+            got = f[name].read()
+            assert got.dtype == a.dtype and got.shape == a.shape
+            np.testing.assert_array_equal(got, a)
+            out = np.empty(a.shape, a.dtype, order="F")
+            np.testing.assert_array_equal(f[name].read_into(out), a)
+    with h5.File(p, "a") as f:
+        f.create_dataset("more", np.arange(3.0))
+    with h5.File(p) as f:
+        for name, (a, _) in cases.items():
+            np.testing.assert_array_equal(f[name].read(), a)
+
+
+def test_chunked_dataset_refusals(mods, tmp_path):
+    _, h5, _ = mods
+    with h5.File(tmp_path / "r.h5", "w") as f:
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("a", np.zeros((4, 4)), chunks=(2,))           # one extent per axis
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("b", np.zeros((4, 4)), chunks=(0, 2))         # extents >= 1
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("c", np.zeros((4, 4)), compression=4)         # deflate needs chunks
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("d", "text", chunks=(1,))                     # numeric arrays only
+        with pytest.raises(h5.H5Error):
+            f.create_dataset("e", np.zeros((4, 4)), chunks=(2, 2), compression=12)
+
+
 # ------------------------------------------------------------------ fields
 
 
