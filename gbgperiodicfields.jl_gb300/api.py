@@ -121,7 +121,12 @@ class Grid3D:
 # ----------------------------------------------------------------- schemes
 
 
-class _SplineScheme:
+class AbstractTransferScheme:
+    """The supertype of the transfer schemes (the reference exports `AbstractTransferScheme`):
+    the local splines, the NUFFT plan and the DirectDFT record are its subtypes."""
+
+
+class _SplineScheme(AbstractTransferScheme):
     kind_name = "spline"
 
     def __init__(self, c: _lib.SchemeC):
@@ -194,6 +199,23 @@ def _catmull_rom():
 # ----------------------------------------------------------------- points
 
 
+def Point(x, y, z, dtype=torch.float64) -> torch.Tensor:
+    """One position as a 3-vector (Points.jl:107, `Point{T} = SVector{3, T}`), of the
+    positions' real type; the callable field(x) and point sets take it."""
+    if dtype not in (torch.float32, torch.float64):
+        raise ArgumentError("Point: the coordinates are Float32 or Float64")
+    return torch.tensor([float(x), float(y), float(z)], dtype=dtype)
+
+
+def fiber_shape(R: int) -> tuple:
+    """The per-point (or per-node) shape of a tensor of order R: (3,) * R
+    (FiberSections.jl:1100-1108)."""
+    R = int(R)
+    if R < 0:
+        raise ArgumentError("fiber_shape: the tensor order is a non-negative integer")
+    return (3,) * R
+
+
 class PointSet:
     """M positions, stored (M, 3) column-major (Points.jl:124-133)."""
 
@@ -244,6 +266,23 @@ def VectorPointValues(data):
 
 
 def TensorPointValues(data, R: int = 2):
+    return AbstractPointValues(data, R)
+
+
+def point_value_tensor_order(v: AbstractPointValues) -> int:
+    """The tensor order R of point values (Points.jl:268-273)."""
+    return int(v.tensor_order)
+
+
+def similar_point_values(reference: AbstractPointValues, data_or_order=None) -> AbstractPointValues:
+    """Point values shaped like `reference` (Points.jl:341-365): given an array, that array
+    wrapped with the reference's tensor order; otherwise fresh (uninitialized) storage of
+    (M, fiber_shape(R)...) -- R the order given, by default the reference's -- with the
+    reference's element type and device."""
+    if isinstance(data_or_order, torch.Tensor):
+        return AbstractPointValues(data_or_order, reference.tensor_order)
+    R = reference.tensor_order if data_or_order is None else int(data_or_order)
+    data = empty_colmajor((npoints(reference),) + fiber_shape(R), reference.data.dtype, reference.data.device)
     return AbstractPointValues(data, R)
 
 
@@ -302,6 +341,41 @@ def VectorFieldPhysical(data, grid):
 
 def TensorFieldPhysical(data, grid, R: int = 2):
     return AbstractFieldPhysical(data, grid, R)
+
+
+def field_tensor_order(f) -> int:
+    """The tensor order R of a field, physical or spectral (Fields.jl:349-350)."""
+    return int(f.tensor_order)
+
+
+def field_scalar_type(f) -> torch.dtype:
+    """The real scalar type T of a field, physical or spectral (Fields.jl:341-342)."""
+    return {torch.complex64: torch.float32, torch.complex128: torch.float64}.get(f.data.dtype, f.data.dtype)
+
+
+def field_physical_shape(grid: Grid3D, R: int) -> tuple:
+    """The storage shape of a field of tensor order R in physical space on `grid`:
+    (grid_size..., fiber_shape(R)...) (Fields.jl:365-369)."""
+    return tuple(grid.grid_size) + fiber_shape(R)
+
+
+def similar_field(reference, data_or_order=None):
+    """A field like `reference` (Fields.jl:1013-1070): given an array, that array wrapped as a
+    field of the reference's kind (physical or spectral, with its grid and Fourier layout) and
+    tensor order; otherwise fresh (uninitialized) storage of order R -- by default the
+    reference's -- with the reference's element type and device."""
+    from .nufft import AbstractFieldSpectral, field_spectral_shape
+    spectral = isinstance(reference, AbstractFieldSpectral)
+    if isinstance(data_or_order, torch.Tensor):
+        if spectral:
+            return AbstractFieldSpectral(data_or_order, reference.grid, reference.tensor_order, reference.layout)
+        return AbstractFieldPhysical(data_or_order, reference.grid, reference.tensor_order)
+    R = reference.tensor_order if data_or_order is None else int(data_or_order)
+    dev, dt = reference.data.device, reference.data.dtype
+    if spectral:
+        data = empty_colmajor(field_spectral_shape(reference.grid, reference.layout, R), dt, dev)
+        return AbstractFieldSpectral(data, reference.grid, R, reference.layout)
+    return AbstractFieldPhysical(empty_colmajor(field_physical_shape(reference.grid, R), dt, dev), reference.grid, R)
 
 
 def field_data(f: AbstractFieldPhysical) -> torch.Tensor:

@@ -29,7 +29,7 @@ import torch
 
 from . import _lib
 from ._lib import ArgumentError, DimensionMismatch, MethodError
-from .api import (AbstractPointValues, Grid3D, PointSet, PointTraversalOrder, _DTYPE_CODE, _check_npoints_match,
+from .api import (AbstractPointValues, AbstractTransferScheme, Grid3D, PointSet, PointTraversalOrder, _DTYPE_CODE, _check_npoints_match,
                   _check_traversal, _raise_device_status, _require_cuda, _status_buffer, colmajor, empty_colmajor)
 
 _COMPLEX = {torch.float32: torch.complex64, torch.float64: torch.complex128}
@@ -167,6 +167,53 @@ def to_physical(spectral: AbstractFieldSpectral, plans: Optional[FieldTransformP
     return AbstractFieldPhysical(data, spectral.grid, spectral.tensor_order)
 
 
+def _check_matches_plans(field, plans: FieldTransformPlans):
+    """_check_field_matches_context (Fields.jl:1295-1305): the field was made for the plans'
+    grid (and, spectral, Fourier layout), with their tensor order."""
+    if field.grid != plans.grid:
+        raise ArgumentError("field grid must be equal to FieldTransformPlans grid")
+    if isinstance(field, AbstractFieldSpectral) and field.layout != plans.layout:
+        raise ArgumentError("field Fourier layout must be equal to FieldTransformPlans Fourier layout")
+    if field.tensor_order != plans.tensor_order:
+        raise ArgumentError("field tensor order must be equal to FieldTransformPlans tensor order")
+
+
+def _check_pair_precision(physical, spectral):
+    want = {torch.float32: torch.complex64, torch.float64: torch.complex128}.get(physical.data.dtype)
+    if spectral.data.dtype != want:
+        raise ArgumentError("the physical and spectral fields must have one scalar type")
+
+
+def to_physical_(physical, spectral: AbstractFieldSpectral, plans: FieldTransformPlans,
+                 spectral_scratch: Optional[AbstractFieldSpectral] = None):
+    """to_physical! (Fields.jl:1546-1620): the inverse transform written into `physical`.  With
+    `spectral_scratch` the coefficients are copied there first and `spectral` is left as it
+    was (the scratch may not share `spectral`'s storage); without it the source may serve as
+    the transform's scratch (here it is left unchanged as well)."""
+    _check_matches_plans(physical, plans)
+    _check_matches_plans(spectral, plans)
+    _check_pair_precision(physical, spectral)
+    src = spectral.data
+    if spectral_scratch is not None:
+        _check_matches_plans(spectral_scratch, plans)
+        if spectral_scratch.data.data_ptr() == spectral.data.data_ptr():
+            raise ArgumentError("spectral_scratch must not alias spectral: a shared array would let the "
+                                "transform consume the source this argument exists to preserve")
+        spectral_scratch.data.copy_(spectral.data)
+        src = spectral_scratch.data
+    physical.data.copy_(_fft_inverse(src, spectral.grid.grid_size, spectral.layout))
+    return physical
+
+
+def to_spectral_(spectral: AbstractFieldSpectral, physical, plans: FieldTransformPlans):
+    """to_spectral! (Fields.jl:1623-1657): the forward transform written into `spectral`."""
+    _check_matches_plans(spectral, plans)
+    _check_matches_plans(physical, plans)
+    _check_pair_precision(physical, spectral)
+    spectral.data.copy_(_fft_forward(physical.data, spectral.layout))
+    return spectral
+
+
 # ------------------------------------------------------------------ NUFFT
 
 
@@ -200,7 +247,7 @@ def _shared_slices(n: int, nf: int, is_half: bool):
     return pairs
 
 
-class NUFFT:
+class NUFFT(AbstractTransferScheme):
     """The fast spectral transfer scheme (Interpolation.jl:1718-1860).
 
     NUFFT(reference_spectral_field; tolerance=1e-10, oversampling=2, window_width=None,
@@ -422,7 +469,7 @@ def anterpolate_nufft(grid: Grid3D, points: PointSet, quantities: AbstractPointV
 # ------------------------------------------------ the exact spectral scheme, as a record
 
 
-class DirectDFT:
+class DirectDFT(AbstractTransferScheme):
     """The reference's exact spectral transfer scheme (src/Interpolation.jl:1382-1433), a
     parameterless singleton.  This package carries it as a scheme record -- it round-trips
     through write_scheme/read_scheme, so checkpoints that name it stay readable -- but the
