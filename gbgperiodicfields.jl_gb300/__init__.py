@@ -17,8 +17,8 @@ from .api import (AbstractFieldPhysical, AbstractPointValues, AbstractTransferSc
                   point_traversal_order, point_traversal_order_, point_value_tensor_order, point_values,
                   sample_field, similar_field, similar_point_values, wrap_, zeros_colmajor)
 from .nufft import (NUFFT, AbstractFieldSpectral, DirectDFT, FieldTransformPlans, RealFourierLayout,
-                    ScalarFieldSpectral, TensorFieldSpectral, VectorFieldSpectral, field_layout, field_spectral_shape,
-                    to_physical, to_physical_, to_spectral, to_spectral_)
+                    ScalarFieldSpectral, TensorFieldSpectral, VectorFieldSpectral, embed_modes_, extract_modes_,
+                    field_layout, field_spectral_shape, to_physical, to_physical_, to_spectral, to_spectral_)
 from .checkpoint import (read_field, read_field_, read_points, read_scheme, write_field, write_points,
                          write_scheme)
 from .h5 import h5open

@@ -214,6 +214,90 @@ def to_spectral_(spectral: AbstractFieldSpectral, physical, plans: FieldTransfor
     return spectral
 
 
+def _shared_axis(n_coarse: int, n_fine: int, folded: bool, device):
+    """One axis of the modes a coarse and a fine grid over one box share (Fields.jl:3157-3185):
+    the coarse stored indices kept and the fine stored indices of the same frequencies.  A full
+    axis stores frequencies 0, 1, ..., then the negative ones (fftfreq order); the folded axis
+    stores 0 .. N//2.  The coarse Nyquist mode of an even axis is left out: the fine grid holds
+    +N/2 and -N/2 apart where the coarse grid holds one sampled wave."""
+    stored = n_coarse // 2 + 1 if folded else n_coarse
+    coarse, fine = [], []
+    for i in range(stored):
+        if n_coarse % 2 == 0 and i == n_coarse // 2:
+            continue
+        if folded:
+            coarse.append(i)
+            fine.append(i)
+            continue
+        freq = i if i < (n_coarse + 1) // 2 else i - n_coarse
+        coarse.append(i)
+        fine.append(freq if freq >= 0 else n_fine + freq)
+    return (torch.tensor(coarse, dtype=torch.long, device=device), torch.tensor(fine, dtype=torch.long, device=device))
+
+
+def _check_shared_modes(coarse: AbstractFieldSpectral, fine: AbstractFieldSpectral):
+    """_check_shared_mode_compatibility (Fields.jl:3287-3310): one scalar type, tensor order,
+    device, box and Fourier layout; the coarse grid no larger on any axis and not equal."""
+    if coarse.data.dtype != fine.data.dtype:
+        raise ArgumentError("field scalar types must be equal")
+    if coarse.tensor_order != fine.tensor_order:
+        raise ArgumentError("field tensor orders must be equal")
+    if coarse.data.device != fine.data.device:
+        raise ArgumentError(f"fields must live on one device; got {coarse.data.device} and {fine.data.device}")
+    cg, fg = coarse.grid, fine.grid
+    if tuple(cg.domain_size) != tuple(fg.domain_size) or tuple(cg.origin) != tuple(fg.origin):
+        raise ArgumentError(f"fields must cover the same box; got domain size {cg.domain_size} at origin "
+                            f"{cg.origin} and {fg.domain_size} at {fg.origin}")
+    if coarse.layout != fine.layout:
+        raise ArgumentError("field Fourier layouts must be equal")
+    if any(c > f for c, f in zip(cg.grid_size, fg.grid_size)):
+        raise ArgumentError(f"the coarse grid {cg.grid_size} must be no larger than the fine grid {fg.grid_size} on any axis")
+    if tuple(cg.grid_size) == tuple(fg.grid_size):
+        raise ArgumentError(f"the two grids are equal ({cg.grid_size}); moving between grid resolutions needs "
+                            "a coarser and a finer field, and two fields on one grid combine by addition")
+
+
+def _shared_modes(destination: AbstractFieldSpectral, source: AbstractFieldSpectral, to_fine: bool, alpha, beta):
+    """The body both resolution verbs share (Fields.jl:3329-3355): destination = alpha' * source
+    on the shared modes (beta == 0), else beta * destination + alpha' * source, where alpha'
+    is alpha times the ratio of the destination's to the source's point count in the fields'
+    real type (stored coefficients are point count x physical amplitude); no other mode is
+    read or written."""
+    coarse, fine = (source, destination) if to_fine else (destination, source)
+    _check_shared_modes(coarse, fine)
+    real = torch.float32 if destination.data.dtype == torch.complex64 else torch.float64
+    ratio = math.prod(destination.grid.grid_size) / math.prod(source.grid.grid_size)
+    scale = float(torch.tensor(float(alpha), dtype=real) * torch.tensor(ratio, dtype=real))
+    b = float(torch.tensor(float(beta), dtype=real))
+    h = coarse.layout.half_axis
+    dev = destination.data.device
+    axes = [_shared_axis(coarse.grid.grid_size[d], fine.grid.grid_size[d], d == h, dev) for d in range(3)]
+    ci = [ax[0] for ax in axes]
+    fi = [ax[1] for ax in axes]
+    grid = lambda idx: (idx[0][:, None, None], idx[1][None, :, None], idx[2][None, None, :])
+    di, si = (grid(fi), grid(ci)) if to_fine else (grid(ci), grid(fi))
+    src = source.data[si]
+    if b == 0.0:
+        destination.data[di] = scale * src
+    else:
+        destination.data[di] = b * destination.data[di] + scale * src
+    return destination
+
+
+def embed_modes_(destination: AbstractFieldSpectral, source: AbstractFieldSpectral, alpha=1, beta=0):
+    """embed_modes! (Fields.jl:3360-3405): a coarser field's modes written into a finer one over
+    the same box (added when beta is nonzero), physical amplitudes kept; the fine field's other
+    modes, and the coarse grid's even-axis Nyquist modes, are left alone."""
+    return _shared_modes(destination, source, True, alpha, beta)
+
+
+def extract_modes_(destination: AbstractFieldSpectral, source: AbstractFieldSpectral, alpha=1, beta=0):
+    """extract_modes! (Fields.jl:3408-3446): a finer field's modes the coarser destination can
+    hold read into it, physical amplitudes kept; the destination's other modes (its even-axis
+    Nyquist modes among them) are left as they were."""
+    return _shared_modes(destination, source, False, alpha, beta)
+
+
 # ------------------------------------------------------------------ NUFFT
 
 

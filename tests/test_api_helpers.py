@@ -81,3 +81,104 @@ def test_in_place_transforms(gbg, dtype):
     wrong_order = gbg.similar_field(f, 0)
     with pytest.raises(gbg.ArgumentError):
         gbg.to_physical_(wrong_order, fh, plans)                    # another tensor order
+
+
+# ------------------------------------------------------------ embed_modes! / extract_modes!
+
+L = (TWO_PI, 3.0, 2.5)
+
+
+def _wave(x, y, z):
+    """A field band-limited below the coarse grids' Nyquist frequencies (kx <= 3, ky <= 2, kz <= 2)."""
+    return (torch.cos(3 * TWO_PI * x / L[0] + 0.3) * torch.sin(2 * TWO_PI * y / L[1])
+            + 0.5 * torch.cos(TWO_PI * x / L[0] - 2 * TWO_PI * z / L[2] + 1.1) + 0.25)
+
+
+@pytest.mark.parametrize("fft_dims", [(1, 2, 3), (2, 1, 3), (3, 1, 2)])
+def test_embed_and_extract_keep_the_field(gbg, fft_dims):
+    """A band-limited field sampled on a coarse grid, embedded into a finer one's modes, transforms
+    back to the same field sampled on the fine grid; extracted from the fine grid's modes, to the
+    same field on the coarse grid (Fields.jl:3360-3446: physical amplitudes kept)."""
+    lay = gbg.RealFourierLayout(fft_dims)
+    coarse = gbg.Grid3D((8, 6, 5), L, origin=(0.2, -0.1, 0.4))
+    fine = gbg.Grid3D((16, 12, 9), L, origin=(0.2, -0.1, 0.4))
+    fc = gbg.sample_field(_wave, coarse, device="cpu")
+    ff = gbg.sample_field(_wave, fine, device="cpu")
+    ch = gbg.to_spectral(fc, layout=lay)
+    fh = gbg.to_spectral(ff, layout=lay)
+    up = gbg.similar_field(fh, torch.zeros_like(fh.data))
+    assert gbg.embed_modes_(up, ch) is up
+    assert torch.allclose(gbg.to_physical(up).data, ff.data, rtol=0, atol=1e-12)
+    down = gbg.similar_field(ch, torch.zeros_like(ch.data))
+    assert gbg.extract_modes_(down, fh) is down
+    assert torch.allclose(gbg.to_physical(down).data, fc.data, rtol=0, atol=1e-12)
+    # extract after embed gives the coarse modes back (up to the two scalings' rounding)
+    back = gbg.similar_field(ch, torch.zeros_like(ch.data))
+    gbg.extract_modes_(back, up)
+    assert torch.allclose(back.data, ch.data, rtol=1e-14, atol=1e-12)
+
+
+def test_shared_modes_leave_the_rest_alone_and_scale(gbg):
+    """Only the shared modes are written: the fine field's other modes and the coarse grid's
+    even-axis Nyquist modes keep their values; alpha and beta act as in mul!(C, A, B, a, b),
+    with alpha carrying the ratio of the two grids' point counts."""
+    coarse = gbg.Grid3D((8, 6, 5), L)
+    fine = gbg.Grid3D((12, 10, 7), L)
+    g = torch.Generator().manual_seed(3)
+    c = gbg.ScalarFieldSpectral(gbg.colmajor(torch.randn(5, 6, 5, dtype=torch.complex128, generator=g)), coarse)
+    sentinel = complex(7.0, -7.0)
+    f = gbg.ScalarFieldSpectral(gbg.colmajor(torch.full((7, 10, 7), sentinel, dtype=torch.complex128)), fine)
+    ratio = (12 * 10 * 7) / (8 * 6 * 5)
+    pairs = []                               # (coarse index, fine index) of every shared mode
+    for i in range(5):                       # folded x: 0..4, the coarse Nyquist (4) left out
+        for j in range(6):                   # full y: 0, 1, 2, (3: Nyquist), -2, -1
+            for k in range(5):               # full z, odd: 0, 1, 2, -2, -1
+                if i == 4 or j == 3:
+                    continue
+                pairs.append(((i, j, k), (i, j if j < 3 else 10 + j - 6, k if k < 3 else 7 + k - 5)))
+    shared = torch.zeros((7, 10, 7), dtype=torch.bool)
+    for _, fi in pairs:
+        shared[fi] = True
+    gbg.embed_modes_(f, c)
+    for ci, fi in pairs:
+        assert torch.isclose(f.data[fi], ratio * c.data[ci], rtol=1e-15, atol=0)
+    assert bool((f.data[~shared] == sentinel).all())
+    before = f.data.clone()
+    gbg.embed_modes_(f, c, 2.0, 0.5)
+    for ci, fi in pairs:
+        assert torch.isclose(f.data[fi], 0.5 * before[fi] + (2.0 * ratio) * c.data[ci], rtol=1e-15, atol=0)
+    assert bool((f.data[~shared] == sentinel).all())
+    # extract leaves the coarse destination's Nyquist modes as they were
+    d = gbg.ScalarFieldSpectral(gbg.colmajor(torch.full((5, 6, 5), sentinel, dtype=torch.complex128)), coarse)
+    gbg.extract_modes_(d, f)
+    assert bool((d.data[4] == sentinel).all()) and bool((d.data[:, 3] == sentinel).all())
+    for ci, fi in pairs:
+        assert torch.isclose(d.data[ci], f.data[fi] / ratio, rtol=1e-15, atol=0)
+
+
+def test_shared_modes_refusals(gbg):
+    coarse = gbg.Grid3D((8, 6, 5), L)
+    fine = gbg.Grid3D((12, 10, 7), L)
+    spec = lambda grid, R=0, dtype=torch.complex128, lay=None: gbg.similar_field(
+        gbg.to_spectral(gbg.AbstractFieldPhysical(
+            gbg.colmajor(torch.zeros(tuple(grid.grid_size) + (3,) * R, dtype=torch.float64 if dtype == torch.complex128 else torch.float32)),
+            grid, R), layout=lay))
+    c, f = spec(coarse), spec(fine)
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(c, f)                                  # the destination of embed is the finer field
+    with pytest.raises(gbg.ArgumentError):
+        gbg.extract_modes_(f, c)                                # the destination of extract is the coarser one
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(coarse), c)                       # equal grids
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(gbg.Grid3D((12, 4, 7), L)), c)    # coarser on one axis, finer on another
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(gbg.Grid3D((12, 10, 7), (TWO_PI, 3.0, 2.0))), c)     # another box
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(gbg.Grid3D((12, 10, 7), L, origin=(0.1, 0, 0))), c)  # another origin
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(fine, lay=gbg.RealFourierLayout((2, 1, 3))), c)    # another Fourier layout
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(fine, R=1), c)                    # another tensor order
+    with pytest.raises(gbg.ArgumentError):
+        gbg.embed_modes_(spec(gbg.Grid3D((12, 10, 7), L, dtype=torch.float32), dtype=torch.complex64), c)
